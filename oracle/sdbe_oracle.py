@@ -1,0 +1,417 @@
+"""CPU oracle for the APHIDS GPU stage (SWARM B-engine VDIF -> R2DBE 2-bit VDIF).
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` legs
+of ``bench.py`` may import it.  The product path (``sdbe_gb300``) never calls it.
+
+It restates, in numpy, the algorithm of the reference's GPU stage
+``software/aphids/vdif_inout_gpu_thread.cu`` (Smithsonian/sdbe) for the
+SWARM 11/11 rate build, with every function citing the reference lines it
+follows.  FFT arithmetic in the reference is cuFFT (closed); here it is
+numpy/pocketfft in FP64 (``precision="f64"``, the oracle of record) or
+scipy.fft in FP32 (``precision="f32"``, the timed CPU path).  Scaling follows
+cuFFT's unnormalised convention so that intermediate values equal the
+reference's device buffers.
+
+Pinned against reference code run in this container on seeded inputs: see
+``tests/golden/make_golden.py`` (bit layout of ``swarm.DBEFrame.from_bin``,
+``sdbe_preprocess.quantize_to_2bit`` + ``vdif.VDIFFrame.to_bin`` packing and
+header words, the Mar-2015 reorder check of ``prototyping/cuda/reorder.py`` and
+the cuFFT scale convention of the FFT-resample check in
+``prototyping/cuda/resample.py``).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+try:  # scipy gives multi-threaded FP32 FFTs for the timed CPU path
+    import scipy.fft as _sfft
+except Exception:  # pragma: no cover - numpy fallback for the oracle itself
+    _sfft = None
+
+# --- constants: software/aphids/sample_rates.h:17-20,52-53,59,70,74 and
+#     software/aphids/vdif_inout_gpu_thread.h:10-53 (SWARM_RATE_FRAC 11/11) ---
+SWARM_RATE = 4576e6                  # sample_rates.h:17,20 (FRAC 11 of 11)
+R2DBE_RATE = 4096e6                  # sample_rates.h:18
+DECIMATION_FACTOR = 143              # sample_rates.h:52
+EXPANSION_FACTOR = 128               # sample_rates.h:53
+BENG_FRAMES_PER_GROUP = 143          # sample_rates.h:70
+VDIF_OUT_PKTS_PER_BLOCK = 16384      # sample_rates.h:59
+VDIF_OUT_FRAMES_PER_SECOND = 125000  # sample_rates.h:74
+BENG_CHANNELS_ = 16384               # vdif_inout_gpu_thread.h:20
+BENG_CHANNELS = BENG_CHANNELS_ + 1   # vdif_inout_gpu_thread.h:21
+BENG_SNAPSHOTS = 128                 # vdif_inout_gpu_thread.h:22
+VDIF_PER_BENG = 2048                 # vdif_inout_gpu_thread.h:17
+IN_PKT_BYTES = 1056                  # vdif_inout_gpu_thread.h:10
+IN_HDR_BYTES = 32                    # vdif_inout_gpu_thread.h:11
+OUT_PKT_DATA_BYTES = 8192            # vdif_out_databuf.h:61
+OUT_PKT_BYTES = 8224                 # sizeof(vdif_out_packet_t), vdif_out_databuf.h:66-69
+BATCH_SNAPSHOTS = DECIMATION_FACTOR  # RESAMPLE_BATCH_SNAPSHOTS, vdif_inout_gpu_thread.h:31
+N_A = 2 * BENG_CHANNELS_             # FFT_SIZE_SWARM_C2R = 32768, .h:35
+N_B = DECIMATION_FACTOR * 256        # FFT_SIZE_SWARM_R2C = 36608, .h:45-47
+N_C = EXPANSION_FACTOR * 256         # FFT_SIZE_R2DBE_C2R = 32768, .h:51
+CHUNKS_PER_BATCH = BATCH_SNAPSHOTS * N_A // N_B   # FFT_BATCHES_SWARM_R2C = 128, .h:49
+OUT_SAMPLES_PER_BATCH = CHUNKS_PER_BATCH * N_C    # 4,194,304
+MAX_SKIP_CHAN = N_B // 2 - BENG_CHANNELS_         # 1920: bins left after 16385 kept
+
+
+def skip_chan_from_mhz(trim_mhz: int) -> int:
+    """Bins trimmed from DC: ``(int)(skip_mhz*1e6/(SWARM_RATE/FFT_SIZE_SWARM_R2C))``.
+
+    Follows ``vdif_inout_gpu_thread.cu:269``.  Bin width is 125 kHz, so this is
+    ``8*trim_mhz``.  Raises if the trimmed window would run past the 18305 bins
+    the R2C produces (the reference would read past its buffer).
+    """
+    skip = int(trim_mhz * 1e6 / (SWARM_RATE / N_B))
+    if skip < 0 or skip > MAX_SKIP_CHAN:
+        raise ValueError(f"trim {trim_mhz} MHz -> skip {skip} outside [0, {MAX_SKIP_CHAN}]")
+    return skip
+
+
+# ---------------------------------------------------------------- headers ---
+def decode_beng_headers(packets: np.ndarray):
+    """Per-packet (invalid, c, f, b) from the B-engine VDIF header.
+
+    c = w5 & 0xFF, f = (w5 >> 16) & 0xFF (``vdif_inout_gpu_thread.cu:353-362``);
+    b is the 40-bit counter ``(w4 << 8) | (w5 >> 24)`` of
+    ``vdif_in_databuf.c:66-74`` (``get_packet_b_count``; the GPU kernel keeps
+    only its low 32 bits, ``.cu:367-369``, which changes nothing for packets
+    inside one group); invalid = w0 bit 31 (``vdif_in_databuf.h:30-34``).
+    """
+    words = np.ascontiguousarray(packets).reshape(-1, IN_PKT_BYTES).view("<u4")
+    w0, w4, w5 = words[:, 0], words[:, 4].astype(np.uint64), words[:, 5].astype(np.uint64)
+    invalid = (w0 >> 31) & 1
+    c = (w5 & 0xFF).astype(np.int64)
+    f = ((w5 >> 16) & 0xFF).astype(np.int64)
+    b = ((w4 << np.uint64(8)) | (w5 >> np.uint64(24))).astype(np.int64)
+    return invalid.astype(np.int64), c, f, b
+
+
+def channel_base_aphids(c, f):
+    """First of the 8 channels a packet carries, APHIDS 11/11 map.
+
+    ``((c>>1)*16 + (c&1) + 2*f) * 8`` from ``vdif_inout_gpu_thread.cu:442``.
+    """
+    return ((c >> 1) * 16 + (c & 1) + 2 * f) * 8
+
+
+def channel_base_mar2015(c, f):
+    """First channel of a packet in the Mar-2015 SDBE format.
+
+    ``SWARM_XENG_PARALLEL_CHAN*(chan_id*SWARM_N_FIDS + fid)`` from
+    ``prototyping/read_sdbe_vdif.py:193``.
+    """
+    return 8 * (c * 8 + f)
+
+
+def packet_frame_index(packets, b_zero: int, n_frames: int):
+    """Frame slot of each packet and whether it is scattered at all.
+
+    The reference writes frame ``(b - b_zero) % 143`` (``.cu:437,443``) for
+    packets its ingest already placed in the group window
+    (``vdif_in_databuf.c:96-156``).  Here a packet is kept iff it is not flagged
+    invalid, f < 8 and 0 <= b - b_zero < n_frames; anything else would land
+    outside the reference's buffers, so it is dropped instead.
+    """
+    invalid, c, f, b = decode_beng_headers(packets)
+    frame = b - int(b_zero)
+    ok = (invalid == 0) & (f < 8) & (frame >= 0) & (frame < n_frames)
+    return frame, c, f, ok
+
+
+# --------------------------------------------------------------- unpack ----
+def vdif_to_beng(packets, b_zero: int, n_frames: int = BENG_FRAMES_PER_GROUP,
+                 channel_map: str = "aphids"):
+    """Unpack + channel scatter into the reference's int8 B-engine buffers.
+
+    Follows ``vdif_to_beng`` (``vdif_inout_gpu_thread.cu:404-507``) including
+    the pre-zeroing memset (``.cu:897-898``): returns ``beng0, beng1`` of shape
+    ``[n_frames, 128, 16384, 2]`` int8 holding (imag, real) = 2-bit code - 2
+    (``.cu:387-392``).  Per snapshot the packet holds two 32-bit words; bytes
+    0..3 of word 0 carry channels 3,2,1,0 and of word 1 channels 7,6,5,4
+    (``.cu:464-495``); within a byte, bits 0-1/2-3 are pol-1 imag/real and
+    bits 4-5/6-7 pol-0 imag/real (``.cu:482-485``).
+    """
+    pk = np.ascontiguousarray(packets, dtype=np.uint8).reshape(-1, IN_PKT_BYTES)
+    frame, c, f, ok = packet_frame_index(pk, b_zero, n_frames)
+    base = channel_base_aphids(c, f) if channel_map == "aphids" else channel_base_mar2015(c, f)
+    beng = np.zeros((2, n_frames, BENG_SNAPSHOTS, BENG_CHANNELS_, 2), dtype=np.int8)
+    sel = np.nonzero(ok)[0]
+    if sel.size == 0:
+        return beng[0], beng[1]
+    payload = pk[sel, IN_HDR_BYTES:].view("<u4").reshape(sel.size, BENG_SNAPSHOTS, 2)
+    fr = frame[sel]
+    bs = base[sel]
+    for half in range(2):              # word 0 -> channels 3..0, word 1 -> 7..4
+        w = payload[:, :, half].astype(np.uint32)
+        for isample in range(4):
+            byte = (w >> np.uint32(8 * isample)) & np.uint32(0xFF)
+            ch = bs + (4 * half + 3 - isample)
+            vals = [((byte >> np.uint32(2 * q)) & np.uint32(3)).astype(np.int16) - 2 for q in range(4)]
+            # order of extraction: pol1 im, pol1 re, pol0 im, pol0 re
+            beng[1, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 0] = vals[0]
+            beng[1, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 1] = vals[1]
+            beng[0, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 0] = vals[2]
+            beng[0, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 1] = vals[3]
+    return beng[0], beng[1]
+
+
+def completion_bitmap(packets, b_zero: int, n_frames: int):
+    """Per-frame channel completion bytes: bit f of byte c set per packet seen.
+
+    Same layout as ``beng_frame_completion_t.cc[256]`` set by
+    ``insert_vdif_in_beng_group_buffer`` (``vdif_in_databuf.c:141-144``), plus
+    the per-frame packet count (``:143``).
+    """
+    frame, c, f, ok = packet_frame_index(packets, b_zero, n_frames)
+    cc = np.zeros((n_frames, 256), dtype=np.uint8)
+    counts = np.zeros(n_frames, dtype=np.int64)
+    for fr, cc_i, ff in zip(frame[ok], c[ok], f[ok]):
+        cc[fr, cc_i] |= np.uint8(1 << ff)
+        counts[fr] += 1
+    return cc, counts
+
+
+def reorder_mar2015(spec):
+    """Mar-2015 SDBE snapshot fix on ``[n_frames, 128, channels]`` spectra.
+
+    Channels with ``(cid/4)`` even are rolled by -2 snapshots inside each
+    128-snapshot B-frame, then snapshots >= 69 are taken from the next B-frame;
+    the last frame is dropped.  Restates the numpy check of
+    ``prototyping/cuda/reorder.py:284-293`` (kernel ``reorder``, ``:13-43``) on
+    a snapshot-major layout.  Returns ``[n_frames-1, 128, channels]``.
+    """
+    spec = np.asarray(spec)
+    out = spec.copy()
+    ch = np.arange(spec.shape[2])
+    shifted = ((ch // 4) & 1) == 0
+    out[:, :, shifted] = np.roll(spec[:, :, shifted], -2, axis=1)
+    res = out.copy()
+    res[:-1, 69:, :] = out[1:, 69:, :]
+    return res[:-1]
+
+
+# ----------------------------------------------------------- spectra -------
+def beng_to_complex(beng, dtype=np.complex128):
+    """int8 (imag, real) pairs -> complex spectra with a zero Nyquist bin.
+
+    ``beng_int8_to_cufftComplex`` (``vdif_inout_gpu_thread.cu:532-556``) plus
+    the memset that zeroes channel 16384 (``.cu:925-926``).  Input
+    ``[..., 16384, 2]``, output ``[..., 16385]``.
+    """
+    beng = np.asarray(beng)
+    out = np.zeros(beng.shape[:-2] + (BENG_CHANNELS,), dtype=dtype)
+    out[..., :BENG_CHANNELS_] = beng[..., 1].astype(np.float64) + 1j * beng[..., 0].astype(np.float64)
+    return out
+
+
+def _irfft(x, n, precision, workers):
+    if precision == "f32":
+        if _sfft is not None:
+            return _sfft.irfft(x.astype(np.complex64), n=n, axis=-1, workers=workers)
+        return np.fft.irfft(x, n=n, axis=-1).astype(np.float32)
+    return np.fft.irfft(x, n=n, axis=-1)
+
+
+def _rfft(x, precision, workers):
+    if precision == "f32":
+        if _sfft is not None:
+            return _sfft.rfft(x.astype(np.float32), axis=-1, workers=workers)
+        return np.fft.rfft(x, axis=-1).astype(np.complex64)
+    return np.fft.rfft(x, axis=-1)
+
+
+def swarm_c2r(spectra, precision="f64", workers=1):
+    """FFT A, ``SwarmC2R``: per snapshot, C2R 32768, unnormalised.
+
+    Plan ``vdif_inout_gpu_thread.cu:271-286``, exec ``:589-625``.  cuFFT's C2R
+    is ``N * numpy.irfft`` (the scale the reference's own numpy check divides
+    out, ``prototyping/cuda/resample.py:138``); imaginary parts of the DC and
+    Nyquist bins do not contribute.  ``[n, 16385] -> [n, 32768]``.
+    """
+    y = _irfft(spectra, N_A, precision, workers)
+    return y * (np.float32(N_A) if precision == "f32" else float(N_A))
+
+
+def swarm_r2c(timeseries, n_fft=N_B, precision="f64", workers=1):
+    """FFT B, ``SwarmR2C``: R2C over consecutive 36608-sample chunks.
+
+    Plan ``vdif_inout_gpu_thread.cu:294-309`` (batch 128, contiguous input),
+    exec ``:631-667``.  Each chunk is transformed on its own (no overlap), so
+    chunks span snapshot boundaries exactly as the reference's flat buffer does.
+    ``[..., n_chunks*36608] -> [..., n_chunks, 18305]``.
+    """
+    x = np.asarray(timeseries)
+    n_chunks = x.shape[-1] // n_fft
+    x = x[..., : n_chunks * n_fft].reshape(x.shape[:-1] + (n_chunks, n_fft))
+    return _rfft(x, precision, workers)
+
+
+def r2dbe_c2r(spectra, skip_chan: int, n_out=N_C, precision="f64", workers=1):
+    """FFT C, ``R2dbeC2R``: C2R 32768 of bins ``[skip, skip+16385)``.
+
+    Plan ``vdif_inout_gpu_thread.cu:317-333`` (input batch stride 18305 = the
+    R2C output stride), exec ``:673-709`` with input pointer ``+skip_chan``.
+    Unnormalised (cuFFT), DC/Nyquist imaginary parts ignored.  Bins the window
+    asks for beyond the spectrum read as zero (the zero-padded upsampling of
+    ``prototyping/cuda/resample.py:132-134`` is the same call with skip 0).
+    """
+    spec = np.asarray(spectra)
+    need = n_out // 2 + 1
+    win = spec[..., skip_chan: skip_chan + need]
+    if win.shape[-1] < need:
+        pad = np.zeros(win.shape[:-1] + (need - win.shape[-1],), dtype=win.dtype)
+        win = np.concatenate([win, pad], axis=-1)
+    y = _irfft(win, n_out, precision, workers)
+    return y * (np.float32(n_out) if precision == "f32" else float(n_out))
+
+
+# ------------------------------------------------------------ statistics ---
+def summary_stats(y):
+    """Offset and threshold: mean and sqrt(sample variance), in FP64.
+
+    The reference merges (n, mean, M2) with Chan's formula in float through
+    ``thrust::transform_reduce`` (``vdif_inout_gpu_thread.cu:66-137``) and sets
+    ``quantizeThreshold = sqrt(M2/(n-1))``, ``quantizeOffset = mean``
+    (``.cu:953-977``).  Returns ``(offset, threshold)``.
+    """
+    y = np.asarray(y, dtype=np.float64).ravel()
+    return float(y.mean()), float(np.sqrt(y.var(ddof=1)))
+
+
+def quantize2bit_codes(y, threshold, offset, compute_dtype=np.float64):
+    """2-bit offset-binary codes per ``quantize2bit`` (``.cu:565-583``).
+
+    ``code = ((|v| >= th) | 2) ^ (3*(v < 0))`` with ``v = x - offset``:
+    0 for v <= -th, 1 for -th < v < 0, 2 for 0 <= v < th, 3 for v >= th
+    (00=-2, 01=-1, 10=0, 11=+1).  ``sdbe_preprocess.quantize_to_2bit``
+    (``prototyping/sdbe_preprocess.py:668-692``) differs only at v == -th
+    exactly.  ``compute_dtype=np.float32`` reproduces the device's FP32 compare.
+    """
+    cd = compute_dtype
+    v = np.asarray(y).astype(cd) - cd(offset)
+    th = cd(threshold)
+    above = (np.abs(v) >= th).astype(np.uint8)
+    neg = (v < 0).astype(np.uint8)
+    return ((above | 2) ^ (3 * neg)) & 3
+
+
+def pack2bit(codes):
+    """Pack 2-bit codes 16 per little-endian uint32, sample i at bits 2i..2i+1.
+
+    ``quantize2bit`` shifts by ``threadIdx.x*2`` and ORs into one word
+    (``.cu:578-580``); ``vdif.VDIFFrame.to_bin`` packs offset-binary samples
+    LSB-first the same way (``prototyping/vdif.py:224-240``).
+    """
+    c = np.asarray(codes, dtype=np.uint32).reshape(-1, 16)
+    shifts = (2 * np.arange(16, dtype=np.uint32))[None, :]
+    return np.bitwise_or.reduce(c << shifts, axis=1).astype("<u4")
+
+
+def unpack2bit(words):
+    """Inverse of :func:`pack2bit`: uint32 words -> codes."""
+    w = np.asarray(words, dtype=np.uint32).reshape(-1, 1)
+    return ((w >> (2 * np.arange(16, dtype=np.uint32))[None, :]) & 3).astype(np.uint8).ravel()
+
+
+# ------------------------------------------------------------- pipeline ----
+class StreamState:
+    """Per-stream state the reference keeps between groups.
+
+    Thresholds/offsets (set once, ``.cu:151-152,954``) and the snapshots left
+    over when the snapshot count is not a multiple of 143 (carried, not
+    emitted; the reference's 143-frame groups never leave any).
+    """
+
+    def __init__(self):
+        self.threshold = [0.0, 0.0]
+        self.offset = [0.0, 0.0]
+        self.carry = [np.zeros((0, BENG_CHANNELS), np.complex128) for _ in range(2)]
+
+
+def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
+                  state: StreamState | None = None, precision="f64", workers=1,
+                  pol1_uses_pol0_threshold=False, channel_map="aphids",
+                  return_float=False):
+    """One call of the GPU stage on ``n_frames`` B-frames of packets.
+
+    Follows the body of ``run_method`` (``vdif_inout_gpu_thread.cu:894-1017``):
+    unpack (K1), then for every 143-snapshot batch FFT A, FFT B, FFT C, the
+    one-off threshold from the first batch ever seen, and quantize2bit.  Output
+    is ``uint8 [2, n_batches*128, 8192]`` = ``vdif_out_data_group_t`` payloads
+    (``vdif_out_databuf.h:110-116``), packet ``iter*128 + k`` holding chunk k
+    of batch iter (``.cu:994``).  The reference applies pol 0's threshold to
+    pol 1 (``.cu:1004-1005``); ``pol1_uses_pol0_threshold`` reproduces that,
+    the default uses each pol's own.
+    """
+    if state is None:
+        state = StreamState()
+    skip = skip_chan_from_mhz(trim_mhz)
+    beng0, beng1 = vdif_to_beng(packets, b_zero, n_frames, channel_map)
+    spec_dtype = np.complex64 if precision == "f32" else np.complex128
+    outs, floats = [], []
+    for pol, beng in enumerate((beng0, beng1)):
+        spec = beng_to_complex(beng.reshape(-1, BENG_CHANNELS_, 2), spec_dtype)
+        spec = np.concatenate([state.carry[pol].astype(spec_dtype), spec], axis=0)
+        n_batches = spec.shape[0] // BATCH_SNAPSHOTS
+        state.carry[pol] = spec[n_batches * BATCH_SNAPSHOTS:].copy()
+        words = np.zeros((n_batches * CHUNKS_PER_BATCH, OUT_PKT_DATA_BYTES // 4), np.uint32)
+        fl = []
+        for it in range(n_batches):
+            block = spec[it * BATCH_SNAPSHOTS:(it + 1) * BATCH_SNAPSHOTS]
+            ts = swarm_c2r(block, precision, workers).reshape(-1)
+            y = r2dbe_c2r(swarm_r2c(ts, N_B, precision, workers), skip, N_C, precision, workers)
+            if state.threshold[pol] == 0.0:
+                state.offset[pol], state.threshold[pol] = summary_stats(y)
+            th_pol = 0 if pol1_uses_pol0_threshold else pol
+            if pol1_uses_pol0_threshold and state.threshold[0] == 0.0:
+                raise RuntimeError("pol 0 threshold unset")
+            cd = np.float32 if precision == "f32" else np.float64
+            codes = quantize2bit_codes(y, state.threshold[th_pol], state.offset[th_pol], cd)
+            words[it * CHUNKS_PER_BATCH:(it + 1) * CHUNKS_PER_BATCH] = pack2bit(codes).reshape(CHUNKS_PER_BATCH, -1)
+            if return_float:
+                fl.append(y)
+        outs.append(words.view(np.uint8).reshape(n_batches * CHUNKS_PER_BATCH, OUT_PKT_DATA_BYTES))
+        if return_float:
+            floats.append(np.concatenate(fl, axis=0) if fl else np.zeros((0, N_C)))
+    out = np.stack(outs, axis=0)
+    if return_float:
+        return out, floats
+    return out
+
+
+# ------------------------------------------------------------ output VDIF --
+def vdif_out_header_words(n_pkts: int, pol: int, secs: int, df: int, psn: int,
+                          ref_epoch: int = 0, station: int = (ord("S") << 8) | ord("m"),
+                          bdc_sideband: int = 0, rx_sideband: int = 0, bit_depth: int = 2):
+    """Eight header words per output frame, per the reference's output thread.
+
+    Field layout ``vdif_out_header_t`` (``vdif_out_databuf.h:19-52``); constant
+    fields from ``init_vdif_out`` (``vdif_out_databuf.c:35-64``: df_len =
+    8224/8, edv5 = 2, real data); per-packet fields from
+    ``vdif_out_net_thread.c:295-317``: secs/df advance per packet with df
+    wrapping at 125000, threadID 0, bps = bit_depth-1, pol, sidebands, psn
+    incrementing per packet.  Returns ``uint32 [n_pkts, 8]``.
+    """
+    ii = np.arange(n_pkts, dtype=np.int64)
+    dfs = df + ii
+    secs_ii = secs + dfs // VDIF_OUT_FRAMES_PER_SECOND
+    df_ii = dfs % VDIF_OUT_FRAMES_PER_SECOND
+    psn_ii = (psn + ii).astype(np.uint64)
+    w = np.zeros((n_pkts, 8), dtype=np.uint32)
+    w[:, 0] = (secs_ii & 0x3FFFFFFF).astype(np.uint32)
+    w[:, 1] = ((df_ii & 0xFFFFFF) | ((ref_epoch & 0x3F) << 24)).astype(np.uint32)
+    w[:, 2] = (OUT_PKT_BYTES // 8) & 0xFFFFFF
+    w[:, 3] = (station & 0xFFFF) | (0 << 16) | (((bit_depth - 1) & 0x1F) << 26)
+    w[:, 4] = (pol & 1) | ((bdc_sideband & 1) << 1) | ((rx_sideband & 1) << 2) | (2 << 24)
+    w[:, 5] = 0
+    w[:, 6] = (psn_ii & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    w[:, 7] = (psn_ii >> np.uint64(32)).astype(np.uint32)
+    return w
+
+
+def frame_vdif(payloads, pol: int, **hdr):
+    """Prepend output headers: ``[n, 8192] -> uint8 [n, 8224]`` VDIF frames."""
+    payloads = np.asarray(payloads, dtype=np.uint8).reshape(-1, OUT_PKT_DATA_BYTES)
+    words = vdif_out_header_words(payloads.shape[0], pol, **hdr)
+    return np.concatenate([words.view(np.uint8).reshape(-1, 32), payloads], axis=1)
