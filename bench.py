@@ -1,0 +1,314 @@
+"""Benchmark of the GB300 SWARM -> R2DBE resampling stage.
+
+Workload (one step): a fresh packet stream of 512 B-frames of 1056-B B-engine
+VDIF packets (seeded synthetic data, 3 CW tones at 0.1-0.5 sigma), i.e. 65536
+snapshots -> 458 batches of 143 -> 58624 output packets per phased sum, both
+phased sums, FP32 radix-FFT path, trim 150 MHz.  Metric: output GS/s (2-bit
+output samples written per second, all streams); x real time = GS/s / (4.096 *
+streams).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` times sdbe_process with packets already in HBM; ``e2e`` times the
+same call with pinned host buffers (host->device copy of the packets and
+device->host copy of the payloads inside the timed region).  Under torchrun
+each rank processes its own stream (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES = 512
+TRIM_MHZ = 150
+REALTIME_GSPS = 4.096
+OUT_SAMPLES_PER_BATCH = 128 * 32768
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(sample_frames=4, workers=None):
+    """The oracle's FP32 path (numpy unpack + scipy.fft) on a bounded sample."""
+    from oracle import sdbe_oracle as O
+    from sdbe_gb300 import synth
+
+    workers = workers or os.cpu_count() or 1
+    spec = synth.config2(n_frames=sample_frames)
+    p = synth.generate(spec)
+    t0 = time.perf_counter()
+    out = O.process_group(p, spec.b_start, sample_frames, TRIM_MHZ, precision="f32", workers=workers)
+    dt = time.perf_counter() - t0
+    samples = out.shape[0] * out.shape[1] * 32768
+    return {"value": samples / dt / 1e9, "unit": "GS/s", "cores": workers, "kind": "port",
+            "sample": f"{sample_frames} B-frames ({out.shape[1] // 128} batches x 2 phased sums) of the same "
+                      f"synthetic stream, oracle FP32 path (numpy unpack, scipy.fft workers={workers}), "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores (CPU oracle port)."""
+    rank, _, world = _env_rank()
+    if rank != 0:
+        return 0
+    from oracle import sdbe_oracle as O
+    from sdbe_gb300 import synth
+
+    workers = os.cpu_count() or 1
+    frames = 2
+    spec = synth.config2(n_frames=frames)
+    p = synth.generate(spec)
+    for _ in range(args.warmup):
+        O.process_group(p, spec.b_start, frames, TRIM_MHZ, precision="f32", workers=workers)
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(args.steps):
+        out = O.process_group(p, spec.b_start, frames, TRIM_MHZ, precision="f32", workers=workers)
+        n += out.shape[0] * out.shape[1] * 32768
+    dt = time.perf_counter() - t0
+    v = n / dt / 1e9
+    line = {
+        "impl": "reference", "metric": "output GS/s", "value": v, "unit": "GS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"bounded sample per step: {frames} B-frames (1 batch x 2 phased sums) of the "
+                               f"512-frame stream, trim {TRIM_MHZ} MHz", "frames_per_step": frames},
+        "x_realtime": v / (REALTIME_GSPS * 2),
+        "cpu_baseline": {"value": v, "unit": "GS/s", "cores": workers, "kind": "port",
+                         "sample": f"{frames} B-frames per step, oracle FP32 path, scipy.fft workers={workers}"},
+        "e2e": {"value": v, "unit": "GS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, local_rank, world = _env_rank()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    from sdbe_gb300 import Resampler, host_buffer, synth
+
+    frames = args.frames
+    spec = synth.config2(stream=rank, n_frames=frames)
+    pkts = synth.generate(spec)
+    n_pkts = pkts.shape[0]
+    rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=args.wave)
+    out_bytes = rs.output_bytes(frames)
+    n_batches = out_bytes // (2 * 128 * 8192)
+    samples_per_step = n_batches * OUT_SAMPLES_PER_BATCH * 2
+    d_pkts = torch.from_numpy(pkts).cuda()
+    d_out = torch.empty(out_bytes, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step_dev():
+        rs.reset()
+        rs.process(d_pkts, frames, spec.b_start, out=d_out, stream=stream, want_result=False)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing (value) + live per-kernel roofline ----
+    for _ in range(max(args.warmup, 3)):
+        step_dev()
+    barrier()
+    rs.read_profile()
+    rs.profile(True)
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
+                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
+    clocks.start()
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step_dev()
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    prof = rs.read_profile()
+    rs.profile(False)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * samples_per_step / (ms_max * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with pinned host buffers (e2e) ----
+    h_pkts = host_buffer(pkts.nbytes).reshape(pkts.shape)
+    h_pkts[...] = pkts
+    h_out = host_buffer(out_bytes)
+    for _ in range(2):
+        rs.reset()
+        rs.process(h_pkts, frames, spec.b_start, out=h_out, want_result=False)
+    barrier()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rs.reset()
+        rs.process(h_pkts, frames, spec.b_start, out=h_out, want_result=False)  # synchronizes
+    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+    t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = world * samples_per_step / (float(t.item()) * 1e-3) / 1e9
+
+    if rank == 0:
+        peak, peak_kind = _load_peaks()
+        a_ms = prof.stage_a_ms / max(prof.stage_a_launches, 1)
+        bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
+        # algorithmic bytes: stage A reads 8 KB packed + writes 128 KB per snapshot;
+        # stage BC reads 36608 floats + writes 8 KB per chunk
+        a_bytes = prof.stage_a_snapshots / max(prof.stage_a_launches, 1) * (8192 + 131072)
+        bc_bytes = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) * (36608 * 4 + 8192)
+        dominant = "stage_bc" if prof.stage_bc_ms >= prof.stage_a_ms else "stage_a"
+        dom_bytes, dom_ms = (bc_bytes, bc_ms) if dominant == "stage_bc" else (a_bytes, a_ms)
+        achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            try:
+                traffic = json.load(open(tpath)).get(dominant)
+            except ValueError:
+                traffic = None
+        # FP32 work per launch (nominal 2.5 N log2 N per real transform)
+        a_flop = 2.5 * 32768 * 15
+        bc_flop = 2.5 * 36608 * np.log2(36608) + 2.5 * 32768 * 15
+        nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+        fp32 = {"stage_a_tflops": prof.stage_a_snapshots * a_flop / (prof.stage_a_ms * 1e-3) / 1e12
+                if prof.stage_a_ms else None,
+                "stage_bc_tflops": prof.stage_bc_chunks * bc_flop / (prof.stage_bc_ms * 1e-3) / 1e12
+                if prof.stage_bc_ms else None,
+                "peak_tflops": nominal_fp32, "peak_kind": "nominal (152 SM x 128 FP32 lanes x 2 x 2.07 GHz)"}
+        cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
+        line = {
+            "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{frames} B-frames x 1 packet stream per GPU (2 phased sums), "
+                                   f"FP32 radix-FFT path, trim {TRIM_MHZ} MHz, first-batch thresholds per step",
+                       "frames": frames, "batches": int(n_batches), "streams_per_gpu": 2,
+                       "packets_per_step": int(n_pkts), "wave_batches": args.wave,
+                       "l2": "inputs larger than L2 (packets 1.08 GB/step, payload 0.96 GB/step)"},
+            "x_realtime": value / (REALTIME_GSPS * 2 * world),
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "ms_per_launch": dom_ms, "algorithmic_bytes_per_launch": dom_bytes,
+                         "stage_ms_per_step": {"stage_a": prof.stage_a_ms / args.steps,
+                                               "stage_bc": prof.stage_bc_ms / args.steps},
+                         "fp32": fp32},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "GS/s", "ms_per_step": float(t.item()),
+                    "h2d_bytes_per_step": int(n_pkts * 1056), "d2h_bytes_per_step": int(out_bytes)},
+            "gpu_launches": int(prof.launches),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    rs.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=FRAMES)
+    ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

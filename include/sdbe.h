@@ -1,0 +1,236 @@
+/*
+ * sdbe.h -- C ABI of the GB300 SWARM->R2DBE resampling stage.
+ *
+ * Drop-in for the GPU stage of APHIDS in Smithsonian/sdbe:
+ *   software/aphids/vdif_inout_gpu_thread.cu (hashpipe thread "VDIFIO",
+ *   .cu:1047-1059) with its buffer layouts from vdif_in_databuf.h and
+ *   vdif_out_databuf.h.  Every entry point is plain C: pointers, sizes and
+ *   int status codes; nothing aborts.  Device pointers live on the device the
+ *   handle was created for.  "stream" arguments are cudaStream_t values passed
+ *   as void* (NULL = the handle's own stream, or the legacy default stream for
+ *   handle-less calls).
+ *
+ * Layouts (byte-compatible with the reference):
+ *   input packet  : 1056 B = 32 B VDIF header + 1024 B payload
+ *                   (vdif_in_packet_t, vdif_in_databuf.h:29-67); B-engine
+ *                   counter b = (w4 << 8) | (w5 >> 24), c = w5 & 0xFF,
+ *                   f = (w5 >> 16) & 0xFF.
+ *   output payload: [2 pols][n_batches*128 packets][8192 B], 16 two-bit
+ *                   samples per little-endian u32, sample i at bits 2i..2i+1
+ *                   (vdif_out_data_group_t, vdif_out_databuf.h:110-116).
+ *   output frame  : 8224 B = 32 B header + 8192 B payload (vdif_out_packet_t).
+ */
+#ifndef SDBE_H
+#define SDBE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (reference: STATE_PROC=1 / STATE_ERROR=-1, .cu:37-39) -- */
+#define SDBE_OK 0
+#define SDBE_ERR_ARG -1        /* bad argument or size                      */
+#define SDBE_ERR_CUDA -2       /* a CUDA runtime call failed                */
+#define SDBE_ERR_STATE -3      /* call not valid in the handle's state      */
+#define SDBE_ERR_CAPACITY -4   /* input or output larger than configured    */
+#define SDBE_ERR_NOMEM -5      /* device or host allocation failed          */
+
+/* ---- constants of the SWARM 11/11 build (sample_rates.h, .h:10-53) ------- */
+#define SDBE_IN_PKT_BYTES 1056
+#define SDBE_OUT_PKT_DATA_BYTES 8192
+#define SDBE_OUT_PKT_BYTES 8224
+#define SDBE_PKTS_PER_FRAME 2048
+#define SDBE_SNAPSHOTS_PER_FRAME 128
+#define SDBE_CHANNELS 16384
+#define SDBE_BATCH_SNAPSHOTS 143      /* DECIMATION_FACTOR                    */
+#define SDBE_PKTS_PER_BATCH 128       /* EXPANSION_FACTOR: out packets/batch  */
+#define SDBE_FRAMES_PER_GROUP 143     /* BENG_FRAMES_PER_GROUP                */
+#define SDBE_SAMPLES_PER_OUT_PKT 32768
+#define SDBE_MAX_SKIP_CHAN 1920       /* 18304 - 16384 bins                    */
+
+/* threshold modes */
+#define SDBE_THRESH_FIRST_BATCH 0  /* reference: mean/std of the first batch, set once (.cu:953-986) */
+#define SDBE_THRESH_FIXED 1        /* thresholds supplied by sdbe_set_state                          */
+
+/* channel maps */
+#define SDBE_MAP_APHIDS 0          /* ((c>>1)*16 + (c&1) + 2f)*8, .cu:442                */
+#define SDBE_MAP_MAR2015 1         /* 8*(8c + f), prototyping/read_sdbe_vdif.py:193      */
+
+/* sdbe_process flags */
+#define SDBE_IN_HOST 1u            /* packets are in host memory (copied in)             */
+#define SDBE_OUT_HOST 2u           /* output goes to host memory (copied out)            */
+#define SDBE_OUT_FRAMED 4u         /* write 8224-B VDIF frames with headers              */
+#define SDBE_SYNC 8u               /* synchronize the stream before returning            */
+
+typedef struct sdbe_config {
+    int32_t device;            /* CUDA device ordinal (resampler->deviceId, .cu:147)        */
+    int32_t trim_mhz;          /* MHz trimmed from DC, Redis key trim_from_dc (.cu:770,269) */
+    int32_t max_frames;        /* most B-frames per sdbe_process call (143 = one group)     */
+    int32_t threshold_mode;    /* SDBE_THRESH_*                                             */
+    int32_t pol1_uses_pol0_threshold; /* 1 reproduces .cu:1004-1005 (pol 1 quantized with
+                                         pol 0's threshold/offset); 0 = each pol its own    */
+    int32_t channel_map;       /* SDBE_MAP_*                                                */
+    int32_t wave_batches;      /* batches per FFT wave (0 = default); bounds scratch        */
+    int32_t reserved[9];
+} sdbe_config;
+
+typedef struct sdbe_state {
+    float threshold[2];        /* quantizeThreshold_0/1 (.cu:151), own value per pol       */
+    float offset[2];           /* quantizeOffset_0/1 (.cu:152)                             */
+    int32_t thresholds_set;    /* 0 until computed or supplied                             */
+    int32_t carry_snapshots;   /* snapshots held for the next call (< 143)                 */
+    /* output VDIF header counters (vdif_out_net_thread.c:199-317) */
+    uint32_t secs_inre;
+    uint32_t df_num_insec;
+    uint64_t edh_psn;
+    uint32_t ref_epoch;
+    uint32_t station_id;
+    uint32_t bdc_sideband;
+    uint32_t rx_sideband;
+    int32_t reserved[6];
+} sdbe_state;
+
+typedef struct sdbe_result {
+    int64_t n_batches;         /* 143-snapshot batches processed                            */
+    int64_t n_out_packets;     /* output packets per pol (= 128 * n_batches)                */
+    int64_t packets_accepted;  /* scattered into the group                                  */
+    int64_t packets_rejected;  /* invalid flag, f >= 8 or b outside the window              */
+    int64_t frames_incomplete; /* frames with fewer than 2048 distinct (c,f) packets        */
+    int64_t carry_snapshots;
+} sdbe_result;
+
+typedef struct sdbe_resampler sdbe_resampler;
+
+/* Create: device buffers, twiddle tables, stream.
+ * Replaces aphids_resampler_init (vdif_inout_gpu_thread.cu:184-347). */
+int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out);
+
+/* Destroy: frees everything the handle owns.
+ * Replaces aphids_resampler_destroy (.cu:712-743); does not reset the device. */
+int sdbe_destroy(sdbe_resampler *h);
+
+/* Output payload bytes one sdbe_process call on n_frames B-frames writes
+ * (both pols), given the current carry; frames with flag SDBE_OUT_FRAMED use
+ * 8224-B slots.  Lets the caller size its buffer. */
+int64_t sdbe_output_bytes(const sdbe_resampler *h, int32_t n_frames, uint32_t flags);
+
+/* Process n_frames consecutive B-frames of packets starting at counter b_zero
+ * (packet order arbitrary, missing packets read as zero).
+ * Replaces one pass of run_method's STATE_PROC body (.cu:874-1017): the
+ * vdif_to_beng unpack (K1, .cu:894-906), then per 143-snapshot batch
+ * beng_int8_to_cufftComplex, SwarmC2R, SwarmR2C, R2dbeC2R, the one-off
+ * threshold and quantize2bit (.cu:923-1008).  With n_frames = 143 and no
+ * carry the output is exactly vdif_out_data_group_t.
+ *   packets   : n_packets*1056 B, host (SDBE_IN_HOST) or device memory
+ *   out       : host (SDBE_OUT_HOST) or device; out_bytes = its capacity
+ *   result    : optional; filling it synchronizes the stream
+ * With SDBE_OUT_FRAMED the headers come from the handle's header counters,
+ * which advance by the packets written. */
+int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames,
+                 uint64_t b_zero, void *out, int64_t out_bytes, uint32_t flags, void *stream,
+                 sdbe_result *result);
+
+/* State of the stream.  get/set synchronize the device first (work may be in
+ * flight on any stream).  set: thresholds/offsets (marked set if any
+ * threshold != 0), header counters; clears the carry when carry_snapshots == 0. */
+int sdbe_get_state(sdbe_resampler *h, sdbe_state *st);
+int sdbe_set_state(sdbe_resampler *h, const sdbe_state *st);
+/* Forget thresholds and carry (a new stream).  Host-side only: the next
+ * sdbe_process recomputes the thresholds on its stream, so this is safe while
+ * earlier calls are still running. */
+int sdbe_reset(sdbe_resampler *h);
+
+/* Per-stage GPU timing, the counterpart of the reference's GPU_DEBUG event
+ * timing (vdif_inout_gpu_thread.cu:594-621).  While enabled, sdbe_process
+ * records CUDA events around every stage-A (SwarmC2R) and stage-BC (fused
+ * SwarmR2C + R2dbeC2R + quantize2bit) launch on the stream it runs on.
+ * sdbe_profile_read waits for the recorded events, returns the totals since
+ * the last read and clears them.  launches counts every kernel sdbe_process
+ * launched since the last read, enabled or not. */
+typedef struct sdbe_profile {
+    int64_t launches;
+    int64_t stage_a_launches;
+    int64_t stage_a_snapshots;   /* transforms done by those launches */
+    double stage_a_ms;
+    int64_t stage_bc_launches;
+    int64_t stage_bc_chunks;
+    double stage_bc_ms;
+    int64_t reserved[4];
+} sdbe_profile;
+int sdbe_profile_enable(sdbe_resampler *h, int32_t enable);
+int sdbe_profile_read(sdbe_resampler *h, sdbe_profile *out);
+/* Last error message of the handle (or of the thread for handle-less calls). */
+int sdbe_last_error(const sdbe_resampler *h, char *buf, size_t n);
+
+/* Pinned host buffers for packet groups and output groups.
+ * Replace get_bgv_cpu_memory_cuda / get_vdg_cpu_memory_cuda
+ * (vdif_in_databuf_cuda.cu:48-58, vdif_out_databuf_cuda.cu:48-58). */
+int sdbe_host_alloc(void **ptr, size_t bytes);
+int sdbe_host_free(void *ptr);
+
+/* ---- stage entry points (device pointers), one per reference function ---- */
+
+/* vdif_to_beng (.cu:404-507) with its pre-zeroing memset (.cu:897-898):
+ * int8 [n_frames][128][16384][2] (imag, real) per pol. */
+int sdbe_vdif_to_beng(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t n_frames,
+                      int32_t channel_map, int8_t *beng0, int8_t *beng1, void *stream);
+
+/* The packed form the fused path uses: per pol [snapshot][2048 u32], each
+ * u32 = 8 channels x (2-bit real << 2 | 2-bit imag) nibbles, channel k of the
+ * group in bits 4k..4k+3; missing packets filled with code 2 (value 0).
+ * bitmap: [n_frames][256] bytes, bit f of byte c set per packet seen
+ * (beng_frame_completion_t.cc, vdif_in_databuf.h:126-130); frame_counts:
+ * [n_frames] int32; rejected: int32[1].  Arrays are accumulated into. */
+int sdbe_unpack(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t n_frames,
+                int32_t channel_map, uint32_t *spec, int64_t pol_stride_words, int64_t snap0,
+                uint32_t *bitmap, int32_t *frame_counts, int32_t *rejected, void *stream);
+int sdbe_fill_missing(const uint32_t *bitmap, int32_t n_frames, int32_t channel_map, uint32_t *spec,
+                      int64_t pol_stride_words, int64_t snap0, void *stream);
+
+/* beng_int8_to_cufftComplex (.cu:532-556) + Nyquist zero (.cu:925-926):
+ * int8 [n][16384][2] -> complex64 [n][16385]. */
+int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, void *stream);
+
+/* SwarmC2R (.cu:589-625): packed spectra [n_snapshots][2048 u32] ->
+ * float [n_snapshots][32768], unnormalised C2R. */
+int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out,
+                   void *stream);
+
+/* SwarmR2C (.cu:631-667): float [n_chunks][36608] -> complex64 [n_chunks][18305]. */
+int sdbe_swarm_r2c(sdbe_resampler *h, const float *in, int64_t n_chunks, void *out_c64, void *stream);
+
+/* R2dbeC2R (.cu:673-709): complex64 [n_chunks][18305] from bin skip_chan ->
+ * float [n_chunks][32768]. */
+int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int32_t skip_chan,
+                   float *out, void *stream);
+
+/* SwarmR2C and R2dbeC2R fused, chunk in -> resampled float chunk out. */
+int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out,
+                         void *stream);
+
+/* summary_stats + transform_reduce (.cu:66-137,953-977) in FP64:
+ * out[0] = mean (quantizeOffset), out[1] = sqrt(M2/(n-1)) (quantizeThreshold). */
+int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *stream);
+
+/* quantize2bit (.cu:565-583): n floats -> n/16 words (n multiple of 16). */
+int sdbe_quantize2bit(const float *in, uint32_t *out, int64_t n, float thresh, float offset,
+                      void *stream);
+
+/* Output VDIF headers (vdif_out_databuf.c:35-64 + vdif_out_net_thread.c:295-317)
+ * for n_pkts frames of 8224 B per pol at frames + pol*pol_stride_bytes; packet
+ * i gets df = (df0+i) mod 125000 with secs carried, psn = psn0+i. */
+int sdbe_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride_bytes, uint32_t secs0,
+                      uint32_t df0, uint64_t psn0, uint32_t ref_epoch, uint32_t station_id,
+                      uint32_t bdc_sideband, uint32_t rx_sideband, void *stream);
+
+/* Mar-2015 snapshot reorder on packed spectra (prototyping/cuda/reorder.py:13-43):
+ * [n_frames][128][2048 u32] -> [n_frames-1][128][2048 u32]. */
+int sdbe_reorder_mar2015(const uint32_t *spec_in, int32_t n_frames, uint32_t *spec_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDBE_H */

@@ -1,0 +1,563 @@
+// C ABI of libsdbe: the drop-in for the APHIDS GPU stage
+// (software/aphids/vdif_inout_gpu_thread.cu, Smithsonian/sdbe).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "launchers.cuh"
+#include "sdbe_internal.cuh"
+
+namespace sdbe {
+static thread_local std::string g_thread_error;
+void set_thread_error(const std::string &msg) { g_thread_error = msg; }
+const std::string &thread_error() { return g_thread_error; }
+}  // namespace sdbe
+
+using namespace sdbe;
+
+struct sdbe_resampler {
+    sdbe_config cfg{};
+    int skip = 0;
+    int wave = 4;
+    cudaStream_t stream = nullptr;
+    Twiddles tw{};
+    float2 *tw_storage = nullptr;
+    int64_t max_snaps = 0;
+    uint32_t *spec = nullptr;     // [2][max_snaps][2048] packed spectra
+    int64_t spec_pol_stride = 0;  // words
+    uint32_t *bitmap = nullptr;   // [max_frames][64]
+    int32_t *counts = nullptr;    // [max_frames] per-frame packets, then [1] rejected
+    float *ts = nullptr;          // [2][wave*143*32768] stage-A time series
+    int64_t ts_pol_stride = 0;
+    float *fout = nullptr;        // [2][128*32768] first-batch floats
+    double *partials = nullptr;   // [2][128][3]
+    float *thr = nullptr;         // device [8], see k_finalize_thresholds
+    uint8_t *pkt_stage = nullptr;
+    int64_t pkt_stage_bytes = 0;
+    uint8_t *out_stage = nullptr;
+    int64_t out_stage_bytes = 0;
+    bool thresholds_set = false;
+    int64_t carry = 0;
+    uint32_t secs = 0, df = 0, ref_epoch = 0, station = (uint32_t('S') << 8) | uint32_t('m'), bdc = 0, rx = 0;
+    uint64_t psn = 1;
+    std::string err;
+    // profiling (sdbe_profile_enable / sdbe_profile_read)
+    bool prof = false;
+    struct Timed {
+        cudaEvent_t a, b;
+        int kind;       // 0 = stage A, 1 = stage BC
+        int64_t units;  // snapshots or chunks
+    };
+    std::vector<Timed> timed;     // pool; first n_timed in use
+    size_t n_timed = 0;
+    int64_t launches = 0;
+};
+
+namespace {
+
+int fail(sdbe_resampler *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    set_thread_error(msg);
+    return code;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+#define SDBE_CK(h, call)                                                                             \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail((h), SDBE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Event pair around one timed launch (profiling only).
+cudaError_t timed_begin(sdbe_resampler *h, int kind, int64_t units, cudaStream_t st, size_t *slot) {
+    *slot = SIZE_MAX;
+    if (!h->prof) return cudaSuccess;
+    if (h->n_timed == h->timed.size()) {
+        sdbe_resampler::Timed t{};
+        cudaError_t e = cudaEventCreate(&t.a);
+        if (e == cudaSuccess) e = cudaEventCreate(&t.b);
+        if (e != cudaSuccess) return e;
+        h->timed.push_back(t);
+    }
+    *slot = h->n_timed++;
+    h->timed[*slot].kind = kind;
+    h->timed[*slot].units = units;
+    return cudaEventRecord(h->timed[*slot].a, st);
+}
+
+cudaError_t timed_end(sdbe_resampler *h, size_t slot, cudaStream_t st) {
+    if (slot == SIZE_MAX) return cudaSuccess;
+    return cudaEventRecord(h->timed[slot].b, st);
+}
+
+void free_all(sdbe_resampler *h) {
+    for (auto &t : h->timed) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    cudaFree(h->tw_storage);
+    cudaFree(h->spec);
+    cudaFree(h->bitmap);
+    cudaFree(h->counts);
+    cudaFree(h->ts);
+    cudaFree(h->fout);
+    cudaFree(h->partials);
+    cudaFree(h->thr);
+    cudaFree(h->pkt_stage);
+    cudaFree(h->out_stage);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+cudaStream_t pick(sdbe_resampler *h, void *stream) {
+    return stream ? static_cast<cudaStream_t>(stream) : h->stream;
+}
+
+int64_t batches_for(const sdbe_resampler *h, int32_t n_frames) {
+    return (h->carry + static_cast<int64_t>(n_frames) * kSnapsPerFrame) / kBatchSnaps;
+}
+
+int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what) {
+    if (*cap >= need) return SDBE_OK;
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    if (cudaMalloc(buf, static_cast<size_t>(need)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, SDBE_ERR_NOMEM, std::string("cannot allocate ") + what);
+    }
+    *cap = need;
+    return SDBE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
+    if (!cfg || !out) return fail(nullptr, SDBE_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->max_frames < 1 || cfg->max_frames > (1 << 16))
+        return fail(nullptr, SDBE_ERR_ARG, "max_frames must be in [1, 65536]");
+    const int skip = static_cast<int>(cfg->trim_mhz * 1e6 / (4576e6 / kNB));  // .cu:269
+    if (cfg->trim_mhz < 0 || skip > kMaxSkip) return fail(nullptr, SDBE_ERR_ARG, "trim_mhz must be in [0, 240]");
+    if (cfg->threshold_mode != SDBE_THRESH_FIRST_BATCH && cfg->threshold_mode != SDBE_THRESH_FIXED)
+        return fail(nullptr, SDBE_ERR_ARG, "unknown threshold_mode");
+    if (cfg->channel_map != SDBE_MAP_APHIDS && cfg->channel_map != SDBE_MAP_MAR2015)
+        return fail(nullptr, SDBE_ERR_ARG, "unknown channel_map");
+    if (cfg->wave_batches < 0 || cfg->wave_batches > 64) return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
+        cudaGetLastError();
+        return fail(nullptr, SDBE_ERR_ARG, "no such CUDA device");
+    }
+    DeviceGuard g(cfg->device);
+    if (!g.ok) return fail(nullptr, SDBE_ERR_CUDA, "cudaSetDevice failed");
+    sdbe_resampler *h = new sdbe_resampler();
+    h->cfg = *cfg;
+    h->skip = skip;
+    h->wave = cfg->wave_batches > 0 ? cfg->wave_batches : 4;
+    h->max_snaps = static_cast<int64_t>(cfg->max_frames) * kSnapsPerFrame + kBatchSnaps;
+    h->spec_pol_stride = h->max_snaps * kGroups;
+    h->ts_pol_stride = static_cast<int64_t>(h->wave) * kBatchSnaps * kNA;
+    auto bail = [&](int code, const std::string &m) {
+        free_all(h);
+        delete h;
+        cudaGetLastError();
+        return fail(nullptr, code, m);
+    };
+    if (configure_fft_kernels() != cudaSuccess) return bail(SDBE_ERR_CUDA, "kernel attribute setup failed");
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(SDBE_ERR_CUDA, "stream creation failed");
+    if (build_twiddles(h->tw, &h->tw_storage) != cudaSuccess) return bail(SDBE_ERR_NOMEM, "twiddle tables");
+    bool ok = cudaMalloc(&h->spec, 2 * h->spec_pol_stride * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMalloc(&h->bitmap, static_cast<size_t>(cfg->max_frames) * 256) == cudaSuccess &&
+              cudaMalloc(&h->counts, (static_cast<size_t>(cfg->max_frames) + 1) * sizeof(int32_t)) == cudaSuccess &&
+              cudaMalloc(&h->ts, 2 * h->ts_pol_stride * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&h->fout, 2 * static_cast<size_t>(kChunks) * kNC * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&h->partials, 2 * kChunks * 3 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&h->thr, 8 * sizeof(float)) == cudaSuccess;
+    if (!ok) return bail(SDBE_ERR_NOMEM, "device buffer allocation failed");
+    if (cudaMemset(h->thr, 0, 8 * sizeof(float)) != cudaSuccess) return bail(SDBE_ERR_CUDA, "memset");
+    *out = h;
+    return SDBE_OK;
+}
+
+int sdbe_destroy(sdbe_resampler *h) {
+    if (!h) return SDBE_OK;
+    DeviceGuard g(h->cfg.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return SDBE_OK;
+}
+
+int64_t sdbe_output_bytes(const sdbe_resampler *h, int32_t n_frames, uint32_t flags) {
+    if (!h || n_frames < 0) return -1;
+    const int64_t pkt = (flags & SDBE_OUT_FRAMED) ? kOutPkt : kOutPktData;
+    return 2 * batches_for(h, n_frames) * kChunks * pkt;
+}
+
+int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames, uint64_t b_zero,
+                 void *out, int64_t out_bytes, uint32_t flags, void *stream, sdbe_result *result) {
+    if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
+    if (n_frames < 0 || n_frames > h->cfg.max_frames)
+        return fail(h, SDBE_ERR_CAPACITY, "n_frames outside [0, max_frames]");
+    if (n_packets < 0 || (n_packets > 0 && !packets)) return fail(h, SDBE_ERR_ARG, "bad packets");
+    DeviceGuard g(h->cfg.device);
+    if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
+    cudaStream_t st = pick(h, stream);
+    const bool framed = (flags & SDBE_OUT_FRAMED) != 0;
+    const int64_t n_batches = batches_for(h, n_frames);
+    const int64_t n_out = n_batches * kChunks;
+    const int64_t pkt_stride = framed ? kOutPkt : kOutPktData;
+    const int64_t payload_off = framed ? 32 : 0;
+    const int64_t out_pol_stride = n_out * pkt_stride;
+    if (out_bytes < 2 * out_pol_stride) return fail(h, SDBE_ERR_CAPACITY, "output buffer too small");
+    if (n_out > 0 && !out) return fail(h, SDBE_ERR_ARG, "null output");
+    if (h->cfg.threshold_mode == SDBE_THRESH_FIXED && !h->thresholds_set && n_batches > 0)
+        return fail(h, SDBE_ERR_STATE, "fixed threshold mode needs sdbe_set_state first");
+
+    const uint8_t *src = static_cast<const uint8_t *>(packets);
+    if ((flags & SDBE_IN_HOST) && n_packets > 0) {
+        int rc = grow(h, &h->pkt_stage, &h->pkt_stage_bytes, n_packets * kPktBytes, "packet staging");
+        if (rc) return rc;
+        SDBE_CK(h, cudaMemcpyAsync(h->pkt_stage, packets, n_packets * kPktBytes, cudaMemcpyHostToDevice, st));
+        src = h->pkt_stage;
+    } else if (n_packets > 0 && (reinterpret_cast<uintptr_t>(packets) & 15u)) {
+        return fail(h, SDBE_ERR_ARG, "device packet buffer must be 16-byte aligned");
+    }
+    uint8_t *dev_out = static_cast<uint8_t *>(out);
+    if ((flags & SDBE_OUT_HOST) && n_out > 0) {
+        int rc = grow(h, &h->out_stage, &h->out_stage_bytes, 2 * out_pol_stride, "output staging");
+        if (rc) return rc;
+        dev_out = h->out_stage;
+    } else if (n_out > 0 && (reinterpret_cast<uintptr_t>(out) & 15u)) {
+        return fail(h, SDBE_ERR_ARG, "device output buffer must be 16-byte aligned");
+    }
+
+    const int map = h->cfg.channel_map;
+    if (n_frames > 0) {
+        SDBE_CK(h, cudaMemsetAsync(h->bitmap, 0, static_cast<size_t>(n_frames) * 256, st));
+        SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
+        SDBE_CK(h, launch_unpack(src, n_packets, b_zero, n_frames, map, h->spec, h->spec_pol_stride, h->carry,
+                                 h->bitmap, h->counts, h->counts + h->cfg.max_frames, st));
+        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, h->spec, h->spec_pol_stride, h->carry, st));
+        h->launches += n_packets > 0 ? 2 : 1;
+    }
+
+    int64_t b = 0;
+    if (n_batches > 0 && !h->thresholds_set) {
+        // First batch: floats + FP64 statistics, thresholds set once (.cu:953-986).
+        SDBE_CK(h, launch_swarm_c2r(h->spec, h->spec_pol_stride, 0, kBatchSnaps, 2, h->ts, h->ts_pol_stride, h->tw, st));
+        ResampleOut o{};
+        o.fout = h->fout;
+        o.fout_pol_stride = static_cast<int64_t>(kChunks) * kNC;
+        o.partials = h->partials;
+        SDBE_CK(h, launch_resample(1, h->ts, h->ts_pol_stride, h->skip, kChunks, 2, o, h->tw, st));
+        SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
+        SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, dev_out,
+                                          out_pol_stride, pkt_stride, payload_off, 0, st));
+        h->thresholds_set = true;
+        h->launches += 4;
+        b = 1;
+    }
+    for (; b < n_batches; b += h->wave) {
+        const int64_t nb = std::min<int64_t>(h->wave, n_batches - b);
+        size_t slot;
+        SDBE_CK(h, timed_begin(h, 0, 2 * nb * kBatchSnaps, st, &slot));
+        SDBE_CK(h, launch_swarm_c2r(h->spec, h->spec_pol_stride, b * kBatchSnaps, nb * kBatchSnaps, 2, h->ts,
+                                    h->ts_pol_stride, h->tw, st));
+        SDBE_CK(h, timed_end(h, slot, st));
+        SDBE_CK(h, timed_begin(h, 1, 2 * nb * kChunks, st, &slot));
+        ResampleOut o{};
+        o.out = dev_out;
+        o.out_pol_stride = out_pol_stride;
+        o.pkt_stride = pkt_stride;
+        o.payload_off = payload_off;
+        o.pkt0 = b * kChunks;
+        o.thr = h->thr;
+        SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
+        SDBE_CK(h, timed_end(h, slot, st));
+        h->launches += 2;
+    }
+    if (framed && n_out > 0) {
+        SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
+                                       h->station, h->bdc, h->rx, st));
+        h->launches += 1;
+        const uint64_t dfs = static_cast<uint64_t>(h->df) + static_cast<uint64_t>(n_out);
+        h->secs += static_cast<uint32_t>(dfs / 125000u);
+        h->df = static_cast<uint32_t>(dfs % 125000u);
+        h->psn += static_cast<uint64_t>(n_out);
+    }
+    const int64_t total = h->carry + static_cast<int64_t>(n_frames) * kSnapsPerFrame;
+    const int64_t new_carry = total - n_batches * kBatchSnaps;
+    if (n_batches > 0 && new_carry > 0) {
+        for (int pol = 0; pol < 2; ++pol) {
+            uint32_t *base = h->spec + pol * h->spec_pol_stride;
+            SDBE_CK(h, cudaMemcpyAsync(base, base + n_batches * kBatchSnaps * kGroups,
+                                       new_carry * kGroups * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    h->carry = new_carry;
+    if ((flags & SDBE_OUT_HOST) && n_out > 0)
+        SDBE_CK(h, cudaMemcpyAsync(out, dev_out, 2 * out_pol_stride, cudaMemcpyDeviceToHost, st));
+    const bool need_sync = result || (flags & (SDBE_SYNC | SDBE_IN_HOST | SDBE_OUT_HOST));
+    if (need_sync) SDBE_CK(h, cudaStreamSynchronize(st));
+    if (result) {
+        std::vector<int32_t> cnt(static_cast<size_t>(h->cfg.max_frames) + 1);
+        SDBE_CK(h, cudaMemcpy(cnt.data(), h->counts, cnt.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        int64_t acc = 0, incomplete = 0;
+        for (int32_t f = 0; f < n_frames; ++f) {
+            acc += cnt[f];
+            if (cnt[f] < kPktsPerFrame) ++incomplete;
+        }
+        result->n_batches = n_batches;
+        result->n_out_packets = n_out;
+        result->packets_accepted = acc;
+        result->packets_rejected = cnt[h->cfg.max_frames];
+        result->frames_incomplete = incomplete;
+        result->carry_snapshots = h->carry;
+    }
+    return SDBE_OK;
+}
+
+int sdbe_get_state(sdbe_resampler *h, sdbe_state *st) {
+    if (!h || !st) return fail(h, SDBE_ERR_ARG, "null argument");
+    DeviceGuard g(h->cfg.device);
+    float thr[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    SDBE_CK(h, cudaDeviceSynchronize());
+    if (h->thresholds_set) SDBE_CK(h, cudaMemcpy(thr, h->thr, sizeof(thr), cudaMemcpyDeviceToHost));
+    std::memset(st, 0, sizeof(*st));
+    st->threshold[0] = thr[4];
+    st->threshold[1] = thr[5];
+    st->offset[0] = thr[6];
+    st->offset[1] = thr[7];
+    st->thresholds_set = h->thresholds_set ? 1 : 0;
+    st->carry_snapshots = static_cast<int32_t>(h->carry);
+    st->secs_inre = h->secs;
+    st->df_num_insec = h->df;
+    st->edh_psn = h->psn;
+    st->ref_epoch = h->ref_epoch;
+    st->station_id = h->station;
+    st->bdc_sideband = h->bdc;
+    st->rx_sideband = h->rx;
+    return SDBE_OK;
+}
+
+int sdbe_set_state(sdbe_resampler *h, const sdbe_state *st) {
+    if (!h || !st) return fail(h, SDBE_ERR_ARG, "null argument");
+    if (st->df_num_insec >= 125000u) return fail(h, SDBE_ERR_ARG, "df_num_insec must be < 125000");
+    DeviceGuard g(h->cfg.device);
+    const bool p1 = h->cfg.pol1_uses_pol0_threshold != 0;
+    float thr[8] = {st->threshold[0], p1 ? st->threshold[0] : st->threshold[1],
+                    st->offset[0],    p1 ? st->offset[0] : st->offset[1],
+                    st->threshold[0], st->threshold[1], st->offset[0], st->offset[1]};
+    SDBE_CK(h, cudaDeviceSynchronize());
+    SDBE_CK(h, cudaMemcpy(h->thr, thr, sizeof(thr), cudaMemcpyHostToDevice));
+    h->thresholds_set = (st->threshold[0] != 0.f || st->threshold[1] != 0.f);
+    if (st->carry_snapshots == 0) h->carry = 0;
+    h->secs = st->secs_inre;
+    h->df = st->df_num_insec;
+    h->psn = st->edh_psn;
+    h->ref_epoch = st->ref_epoch;
+    h->station = st->station_id;
+    h->bdc = st->bdc_sideband;
+    h->rx = st->rx_sideband;
+    return SDBE_OK;
+}
+
+int sdbe_reset(sdbe_resampler *h) {
+    if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
+    h->thresholds_set = false;
+    h->carry = 0;
+    return SDBE_OK;
+}
+
+int sdbe_profile_enable(sdbe_resampler *h, int32_t enable) {
+    if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
+    h->prof = enable != 0;
+    return SDBE_OK;
+}
+
+int sdbe_profile_read(sdbe_resampler *h, sdbe_profile *out) {
+    if (!h || !out) return fail(h, SDBE_ERR_ARG, "null argument");
+    DeviceGuard g(h->cfg.device);
+    std::memset(out, 0, sizeof(*out));
+    for (size_t i = 0; i < h->n_timed; ++i) {
+        auto &t = h->timed[i];
+        SDBE_CK(h, cudaEventSynchronize(t.b));
+        float ms = 0.f;
+        SDBE_CK(h, cudaEventElapsedTime(&ms, t.a, t.b));
+        if (t.kind == 0) {
+            out->stage_a_launches += 1;
+            out->stage_a_snapshots += t.units;
+            out->stage_a_ms += ms;
+        } else {
+            out->stage_bc_launches += 1;
+            out->stage_bc_chunks += t.units;
+            out->stage_bc_ms += ms;
+        }
+    }
+    out->launches = h->launches;
+    h->n_timed = 0;
+    h->launches = 0;
+    return SDBE_OK;
+}
+
+int sdbe_last_error(const sdbe_resampler *h, char *buf, size_t n) {
+    if (!buf || n == 0) return SDBE_ERR_ARG;
+    const std::string &m = h ? h->err : thread_error();
+    const size_t k = std::min(n - 1, m.size());
+    std::memcpy(buf, m.data(), k);
+    buf[k] = '\0';
+    return SDBE_OK;
+}
+
+int sdbe_host_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return fail(nullptr, SDBE_ERR_ARG, "null argument");
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(nullptr, SDBE_ERR_NOMEM, "cudaMallocHost failed");
+    }
+    return SDBE_OK;
+}
+
+int sdbe_host_free(void *ptr) {
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) return fail(nullptr, SDBE_ERR_CUDA, "cudaFreeHost failed");
+    return SDBE_OK;
+}
+
+int sdbe_vdif_to_beng(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t n_frames, int32_t channel_map,
+                      int8_t *beng0, int8_t *beng1, void *stream) {
+    if (n_frames < 0 || n_packets < 0 || (n_frames > 0 && (!beng0 || !beng1)) || (n_packets > 0 && !packets))
+        return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = static_cast<size_t>(n_frames) * kSnapsPerFrame * kChannels * 2;
+    SDBE_CK(nullptr, cudaMemsetAsync(beng0, 0, bytes, st));
+    SDBE_CK(nullptr, cudaMemsetAsync(beng1, 0, bytes, st));
+    SDBE_CK(nullptr, launch_vdif_to_beng_ref(packets, n_packets, b_zero, n_frames, channel_map, beng0, beng1, st));
+    return SDBE_OK;
+}
+
+int sdbe_unpack(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t n_frames, int32_t channel_map,
+                uint32_t *spec, int64_t pol_stride_words, int64_t snap0, uint32_t *bitmap, int32_t *frame_counts,
+                int32_t *rejected, void *stream) {
+    if (n_frames < 0 || n_packets < 0 || !spec || !bitmap || !frame_counts || !rejected || snap0 < 0 ||
+        (n_packets > 0 && !packets))
+        return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    SDBE_CK(nullptr, launch_unpack(packets, n_packets, b_zero, n_frames, channel_map, spec, pol_stride_words, snap0,
+                                   bitmap, frame_counts, rejected, static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+int sdbe_fill_missing(const uint32_t *bitmap, int32_t n_frames, int32_t channel_map, uint32_t *spec,
+                      int64_t pol_stride_words, int64_t snap0, void *stream) {
+    if (n_frames < 0 || !bitmap || !spec || snap0 < 0) return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    SDBE_CK(nullptr, launch_fill_missing(bitmap, n_frames, channel_map, spec, pol_stride_words, snap0,
+                                         static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, void *stream) {
+    if (n_spectra < 0 || (n_spectra > 0 && (!beng || !out_c64))) return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    SDBE_CK(nullptr, launch_beng_to_complex(beng, n_spectra, out_c64, static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out, void *stream) {
+    if (!h || n_snapshots < 0 || (n_snapshots > 0 && (!spec || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    DeviceGuard g(h->cfg.device);
+    SDBE_CK(h, launch_swarm_c2r(spec, 0, 0, n_snapshots, 1, out, 0, h->tw, pick(h, stream)));
+    return SDBE_OK;
+}
+
+int sdbe_swarm_r2c(sdbe_resampler *h, const float *in, int64_t n_chunks, void *out_c64, void *stream) {
+    if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out_c64))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    DeviceGuard g(h->cfg.device);
+    SDBE_CK(h, launch_swarm_r2c(in, n_chunks, out_c64, h->tw, pick(h, stream)));
+    return SDBE_OK;
+}
+
+int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int32_t skip_chan, float *out,
+                   void *stream) {
+    if (!h || n_chunks < 0 || skip_chan < 0 || skip_chan > kMaxSkip || (n_chunks > 0 && (!in_c64 || !out)))
+        return fail(h, SDBE_ERR_ARG, "bad argument");
+    DeviceGuard g(h->cfg.device);
+    SDBE_CK(h, launch_r2dbe_c2r(in_c64, n_chunks, skip_chan, out, h->tw, pick(h, stream)));
+    return SDBE_OK;
+}
+
+int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, void *stream) {
+    if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    DeviceGuard g(h->cfg.device);
+    ResampleOut o{};
+    o.fout = out;
+    SDBE_CK(h, launch_resample(2, in, 0, h->skip, n_chunks, 1, o, h->tw, pick(h, stream)));
+    return SDBE_OK;
+}
+
+int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *stream) {
+    if (!in || !out_host || n < 2) return fail(nullptr, SDBE_ERR_ARG, "need n >= 2 and non-null pointers");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int blocks = stats_partial_blocks(n);
+    double *part = nullptr;
+    SDBE_CK(nullptr, cudaMallocAsync(&part, static_cast<size_t>(blocks) * 2 * sizeof(double), st));
+    std::vector<double> hp(static_cast<size_t>(blocks) * 2);
+    cudaError_t e = launch_stats_partial(in, n, part, blocks, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(part, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(nullptr, SDBE_ERR_CUDA, std::string("summary_stats: ") + cudaGetErrorString(e));
+    double s1 = 0.0, s2 = 0.0;
+    for (int b = 0; b < blocks; ++b) {
+        s1 += hp[2 * b];
+        s2 += hp[2 * b + 1];
+    }
+    const double nn = static_cast<double>(n);
+    const double mean = s1 / nn;
+    out_host[0] = mean;
+    out_host[1] = std::sqrt((s2 - s1 * mean) / (nn - 1.0));
+    return SDBE_OK;
+}
+
+int sdbe_quantize2bit(const float *in, uint32_t *out, int64_t n, float thresh, float offset, void *stream) {
+    if (n < 0 || (n % 16) != 0 || (n > 0 && (!in || !out))) return fail(nullptr, SDBE_ERR_ARG, "n must be a multiple of 16");
+    SDBE_CK(nullptr, launch_quantize_flat(in, out, n, thresh, offset, static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+int sdbe_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride_bytes, uint32_t secs0, uint32_t df0,
+                      uint64_t psn0, uint32_t ref_epoch, uint32_t station_id, uint32_t bdc_sideband,
+                      uint32_t rx_sideband, void *stream) {
+    if (n_pkts < 0 || (n_pkts > 0 && !frames) || df0 >= 125000u || (pol_stride_bytes & 15) ||
+        (reinterpret_cast<uintptr_t>(frames) & 15u))
+        return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    SDBE_CK(nullptr, launch_vdif_headers(frames, n_pkts, pol_stride_bytes, secs0, df0, psn0, ref_epoch, station_id,
+                                         bdc_sideband, rx_sideband, static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+int sdbe_reorder_mar2015(const uint32_t *spec_in, int32_t n_frames, uint32_t *spec_out, void *stream) {
+    if (n_frames < 2 || !spec_in || !spec_out) return fail(nullptr, SDBE_ERR_ARG, "need n_frames >= 2");
+    SDBE_CK(nullptr, launch_reorder_mar2015(spec_in, n_frames, spec_out, static_cast<cudaStream_t>(stream)));
+    return SDBE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,218 @@
+// Register-resident DFT codelets and shared-memory helpers for the
+// Stockham FFT passes of the resampling kernels.
+//
+// A pass of radix R over an N-point sequence held in shared memory
+// (Stockham autosort, natural order in and out):
+//   for butterfly j < N/R:  v[r] = x[j + r*N/R]
+//                           v[r] *= W_{Ns*R}^{(j mod Ns)*r}
+//                           v = DFT_R(v)
+//                           y[(j/Ns)*Ns*R + (j mod Ns) + r*Ns] = v[r]
+// with Ns the product of the radices of the earlier passes.  The first pass
+// therefore reads with stride N/R (coalesced straight from global memory)
+// and the last pass writes with stride N/R (coalesced straight to global).
+#pragma once
+
+#include "sdbe_internal.cuh"
+
+namespace sdbe {
+
+// Padded shared-memory index: one float2 of padding per 32 elements keeps
+// the stride-16/32 accesses of the passes free of bank conflicts.
+__device__ __forceinline__ int pad(int a) { return a + (a >> 5); }
+constexpr int padded_len(int n) { return n + (n >> 5) + 1; }
+
+// cos(2 pi m / 32) for integer m; constant-folds when m is a compile-time value.
+__device__ __forceinline__ float cos32(int m) {
+    m &= 31;
+    constexpr float t[9] = {1.0f, 0.98078528040323043f, 0.92387953251128674f,
+                            0.83146961230254524f, 0.70710678118654757f, 0.55557023301960229f,
+                            0.38268343236508984f, 0.19509032201612833f, 0.0f};
+    if (m <= 8) return t[m];
+    if (m <= 16) return -t[16 - m];
+    if (m <= 24) return -t[m - 16];
+    return t[32 - m];
+}
+__device__ __forceinline__ float sin32(int m) { return cos32(m - 8); }
+
+// a * W_32^m, W_32 = exp(-2 pi i / 32) (forward) or its conjugate (inverse).
+template <bool INV>
+__device__ __forceinline__ float2 mul_w32(float2 a, int m) {
+    m &= 31;
+    if (m == 0) return a;
+    if (m == 16) return make_float2(-a.x, -a.y);
+    if (m == 8) return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+    if (m == 24) return INV ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+    const float c = cos32(m);
+    const float s = INV ? sin32(m) : -sin32(m);
+    return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+__host__ __device__ constexpr int bitrev(int x, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((x >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+
+// In-register power-of-two DFT (R <= 32), natural order in and out:
+// bit-reversal by register renaming, then radix-2 decimation-in-time stages.
+template <int R, bool INV>
+__device__ __forceinline__ void dft_pow2(float2 *v) {
+    constexpr int B = ilog2c(R);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j = bitrev(i, B);
+        if (i < j) {
+            const float2 t = v[i];
+            v[i] = v[j];
+            v[j] = t;
+        }
+    }
+#pragma unroll
+    for (int half = 1; half < R; half <<= 1) {
+#pragma unroll
+        for (int i = 0; i < R; i += 2 * half) {
+#pragma unroll
+            for (int k = 0; k < half; ++k) {
+                const float2 b = mul_w32<INV>(v[i + k + half], k * (32 / (2 * half)));
+                const float2 a = v[i + k];
+                v[i + k] = cadd(a, b);
+                v[i + k + half] = csub(a, b);
+            }
+        }
+    }
+}
+
+// cos/sin(2 pi m / P) tables for the odd prime radices.
+template <int P>
+struct OddConst;
+template <>
+struct OddConst<11> {
+    __device__ static __forceinline__ float c(int m) {
+        constexpr float t[6] = {1.0f, 0.84125353283118121f, 0.41541501300188644f, -0.142314838273285f,
+                                -0.65486073394528499f, -0.95949297361449737f};
+        return t[m];
+    }
+    __device__ static __forceinline__ float s(int m) {
+        constexpr float t[6] = {0.0f, 0.54064081745559756f, 0.90963199535451833f, 0.9898214418809328f,
+                                0.75574957435425827f, 0.28173255684142967f};
+        return t[m];
+    }
+};
+template <>
+struct OddConst<13> {
+    __device__ static __forceinline__ float c(int m) {
+        constexpr float t[7] = {1.0f, 0.88545602565320991f, 0.56806474673115592f, 0.12053668025532301f,
+                                -0.35460488704253545f, -0.74851074817110119f, -0.97094181742605201f};
+        return t[m];
+    }
+    __device__ static __forceinline__ float s(int m) {
+        constexpr float t[7] = {0.0f, 0.46472317204376851f, 0.82298386589365635f, 0.99270887409805397f,
+                                0.93501624268541483f, 0.66312265824079519f, 0.23931566428755768f};
+        return t[m];
+    }
+};
+
+// Odd prime DFT by conjugate-pair symmetry: with s_j = v_j + v_{P-j},
+// d_j = v_j - v_{P-j}, A_k = v_0 + sum s_j cos(2 pi jk/P),
+// B_k = sum d_j sin(2 pi jk/P):  y_k = A_k -+ i B_k, y_{P-k} = A_k +- i B_k.
+template <int P, bool INV>
+__device__ __forceinline__ void dft_odd(float2 *v) {
+    constexpr int H = (P - 1) / 2;
+    float2 s[H + 1], d[H + 1];
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+        s[j] = cadd(v[j], v[P - j]);
+        d[j] = csub(v[j], v[P - j]);
+    }
+    float2 y0 = v[0];
+#pragma unroll
+    for (int j = 1; j <= H; ++j) y0 = cadd(y0, s[j]);
+    float2 out[P];
+    out[0] = y0;
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        float2 A = v[0];
+        float2 Bv = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 1; j <= H; ++j) {
+            int m = (j * k) % P;
+            float cs, sn;
+            if (m <= H) {
+                cs = OddConst<P>::c(m);
+                sn = OddConst<P>::s(m);
+            } else {
+                cs = OddConst<P>::c(P - m);
+                sn = -OddConst<P>::s(P - m);
+            }
+            A.x = fmaf(s[j].x, cs, A.x);
+            A.y = fmaf(s[j].y, cs, A.y);
+            Bv.x = fmaf(d[j].x, sn, Bv.x);
+            Bv.y = fmaf(d[j].y, sn, Bv.y);
+        }
+        // forward: y_k = A - i B = (A.x + B.y, A.y - B.x)
+        if (!INV) {
+            out[k] = make_float2(A.x + Bv.y, A.y - Bv.x);
+            out[P - k] = make_float2(A.x - Bv.y, A.y + Bv.x);
+        } else {
+            out[k] = make_float2(A.x - Bv.y, A.y + Bv.x);
+            out[P - k] = make_float2(A.x + Bv.y, A.y - Bv.x);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) v[k] = out[k];
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 *v) {
+    if constexpr (R == 11 || R == 13) {
+        dft_odd<R, INV>(v);
+    } else {
+        dft_pow2<R, INV>(v);
+    }
+}
+
+// Table twiddle W_N^e (forward) or its conjugate (inverse).
+template <bool INV>
+__device__ __forceinline__ float2 twiddle(const float2 *__restrict__ tab, int e) {
+    const float2 w = __ldg(tab + e);
+    return INV ? make_float2(w.x, -w.y) : w;
+}
+
+// ---- 2-bit requantization (quantize2bit, vdif_inout_gpu_thread.cu:577) ----
+__device__ __forceinline__ uint32_t code2(float x, float th, float off) {
+    const float v = x - off;
+    return ((static_cast<uint32_t>(fabsf(v) >= th) | 2u) ^ (3u * static_cast<uint32_t>(v < 0.f))) & 3u;
+}
+
+// ---- block reductions -------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums a and b over the block; result valid in thread 0.  scratch >= 2*32 doubles.
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *scratch) {
+    a = warp_sum(a);
+    b = warp_sum(b);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        scratch[warp] = a;
+        scratch[32 + warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sa = 0.0, sb = 0.0;
+        for (int w = 0; w < nw; ++w) {
+            sa += scratch[w];
+            sb += scratch[32 + w];
+        }
+        a = sa;
+        b = sb;
+    }
+}
+
+}  // namespace sdbe

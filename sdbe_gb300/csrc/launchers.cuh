@@ -1,0 +1,38 @@
+// Kernel launchers shared between the translation units of libsdbe.
+#pragma once
+
+#include "sdbe_internal.cuh"
+
+namespace sdbe {
+struct ResampleOut {
+    uint8_t *out;
+    int64_t out_pol_stride, pkt_stride, payload_off, pkt0;
+    const float *thr;
+    float *fout;
+    int64_t fout_pol_stride;
+    double *partials;
+};
+cudaError_t launch_unpack(const void *, int64_t, uint64_t, int, int, uint32_t *, int64_t, int64_t, uint32_t *,
+                          int32_t *, int32_t *, cudaStream_t);
+cudaError_t launch_fill_missing(const uint32_t *, int, int, uint32_t *, int64_t, int64_t, cudaStream_t);
+cudaError_t launch_vdif_to_beng_ref(const void *, int64_t, uint64_t, int, int, int8_t *, int8_t *, cudaStream_t);
+cudaError_t launch_reorder_mar2015(const uint32_t *, int, uint32_t *, cudaStream_t);
+cudaError_t launch_beng_to_complex(const int8_t *, int64_t, void *, cudaStream_t);
+cudaError_t build_twiddles(Twiddles &, float2 **);
+cudaError_t configure_fft_kernels();
+cudaError_t launch_swarm_c2r(const uint32_t *, int64_t, int64_t, int64_t, int, float *, int64_t, const Twiddles &,
+                             cudaStream_t);
+cudaError_t launch_resample(int, const float *, int64_t, int, int64_t, int, const ResampleOut &, const Twiddles &,
+                            cudaStream_t);
+cudaError_t launch_swarm_r2c(const float *, int64_t, void *, const Twiddles &, cudaStream_t);
+cudaError_t launch_r2dbe_c2r(const void *, int64_t, int, float *, const Twiddles &, cudaStream_t);
+cudaError_t launch_finalize_thresholds(const double *, int, int, float *, cudaStream_t);
+cudaError_t launch_quantize_chunks(const float *, int64_t, int64_t, const float *, uint8_t *, int64_t, int64_t,
+                                   int64_t, int64_t, cudaStream_t);
+cudaError_t launch_quantize_flat(const float *, uint32_t *, int64_t, float, float, cudaStream_t);
+int stats_partial_blocks(int64_t);
+cudaError_t launch_stats_partial(const float *, int64_t, double *, int, cudaStream_t);
+cudaError_t launch_vdif_headers(void *, int64_t, int64_t, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t,
+                                uint32_t, cudaStream_t);
+
+}  // namespace sdbe

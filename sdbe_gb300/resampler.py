@@ -1,0 +1,195 @@
+"""Python host side of the GB300 resampling stage (over the C ABI).
+
+``Resampler`` owns one ``sdbe_resampler`` handle, the GB300 counterpart of
+``aphids_resampler_t`` (software/aphids/vdif_inout_gpu_thread.cu:144-180):
+device buffers, twiddle tables, the one-off thresholds and the carried
+snapshots of a stream.  ``process`` is one pass of the GPU stage over a group
+of B-frames (``run_method``'s STATE_PROC body, .cu:874-1017).
+
+Buffers may be numpy arrays (host memory, copied in/out by the library),
+torch CUDA tensors, or raw device addresses (``int``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+
+
+def _is_device(buf) -> bool:
+    if isinstance(buf, np.ndarray):
+        return False
+    if isinstance(buf, int):
+        return True
+    return bool(getattr(buf, "is_cuda", False)) or hasattr(buf, "__cuda_array_interface__")
+
+
+def _addr(buf) -> int:
+    if buf is None:
+        return 0
+    if isinstance(buf, int):
+        return buf
+    if isinstance(buf, np.ndarray):
+        return buf.ctypes.data
+    if hasattr(buf, "data_ptr"):
+        return int(buf.data_ptr())
+    if hasattr(buf, "__cuda_array_interface__"):
+        return int(buf.__cuda_array_interface__["data"][0])
+    raise TypeError(f"unsupported buffer type {type(buf)!r}")
+
+
+def _nbytes(buf) -> int:
+    if isinstance(buf, np.ndarray):
+        return buf.nbytes
+    if hasattr(buf, "element_size"):
+        return int(buf.numel() * buf.element_size())
+    raise TypeError("pass out_bytes for raw device addresses")
+
+
+@dataclass
+class GroupResult:
+    n_batches: int
+    n_out_packets: int
+    packets_accepted: int
+    packets_rejected: int
+    frames_incomplete: int
+    carry_snapshots: int
+
+
+class Resampler:
+    """One resampling stream pair (both phased sums of a packet stream)."""
+
+    def __init__(self, trim_mhz: int = 150, device: int = 0, max_frames: int = 143,
+                 threshold_mode: int = N.THRESH_FIRST_BATCH, pol1_uses_pol0_threshold: bool = False,
+                 channel_map: int = N.MAP_APHIDS, wave_batches: int = 0):
+        self._lib = N.lib()
+        cfg = N.Config()
+        cfg.device = device
+        cfg.trim_mhz = trim_mhz
+        cfg.max_frames = max_frames
+        cfg.threshold_mode = threshold_mode
+        cfg.pol1_uses_pol0_threshold = int(bool(pol1_uses_pol0_threshold))
+        cfg.channel_map = channel_map
+        cfg.wave_batches = wave_batches
+        h = C.c_void_p()
+        N.check(self._lib.sdbe_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.trim_mhz = trim_mhz
+        self.device = device
+        self.max_frames = max_frames
+        self.skip_chan = int(trim_mhz * 1e6 / (4576e6 / 36608))
+
+    # -- lifecycle --------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sdbe_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- processing ---------------------------------------------------------
+    def output_bytes(self, n_frames: int, framed: bool = False) -> int:
+        return int(self._lib.sdbe_output_bytes(self._h, n_frames, N.OUT_FRAMED if framed else 0))
+
+    def process(self, packets, n_frames: int, b_zero: int, out=None, framed: bool = False,
+                stream=None, n_packets: int | None = None, out_bytes: int | None = None,
+                want_result: bool = True):
+        """Run the stage on ``n_frames`` B-frames starting at counter ``b_zero``.
+
+        Returns ``(out, GroupResult | None)``; ``out`` holds the payloads as
+        ``[2, n_out_packets, 8192]`` (or 8224-B VDIF frames when ``framed``).
+        """
+        if n_packets is None:
+            n_packets = int(packets.shape[0]) if hasattr(packets, "shape") else 0
+        flags = 0 if _is_device(packets) else N.IN_HOST
+        need = self.output_bytes(n_frames, framed)
+        if out is None:
+            pkt = N.OUT_PKT_BYTES if framed else N.OUT_PKT_DATA_BYTES
+            out = np.empty((2, need // (2 * pkt) if need else 0, pkt), np.uint8)
+        if not _is_device(out):
+            flags |= N.OUT_HOST
+        if framed:
+            flags |= N.OUT_FRAMED
+        cap = _nbytes(out) if out_bytes is None else out_bytes
+        res = N.Result() if want_result else None
+        st = C.c_void_p(stream) if isinstance(stream, int) else (
+            C.c_void_p(stream.cuda_stream) if stream is not None else None)
+        rc = self._lib.sdbe_process(self._h, _addr(packets), n_packets, n_frames, b_zero, _addr(out), cap,
+                                    flags, st, C.byref(res) if res is not None else None)
+        N.check(rc, self._h)
+        if res is None:
+            return out, None
+        return out, GroupResult(res.n_batches, res.n_out_packets, res.packets_accepted, res.packets_rejected,
+                                res.frames_incomplete, res.carry_snapshots)
+
+    # -- state ----------------------------------------------------------------
+    def get_state(self) -> N.State:
+        st = N.State()
+        N.check(self._lib.sdbe_get_state(self._h, C.byref(st)), self._h)
+        return st
+
+    def set_state(self, st: N.State):
+        N.check(self._lib.sdbe_set_state(self._h, C.byref(st)), self._h)
+
+    def set_thresholds(self, threshold, offset):
+        st = self.get_state()
+        st.threshold[0], st.threshold[1] = threshold
+        st.offset[0], st.offset[1] = offset
+        self.set_state(st)
+
+    def reset(self):
+        N.check(self._lib.sdbe_reset(self._h), self._h)
+
+    # -- profiling ------------------------------------------------------------
+    def profile(self, enable: bool = True):
+        N.check(self._lib.sdbe_profile_enable(self._h, int(bool(enable))), self._h)
+
+    def read_profile(self) -> N.Profile:
+        p = N.Profile()
+        N.check(self._lib.sdbe_profile_read(self._h, C.byref(p)), self._h)
+        return p
+
+    @property
+    def thresholds(self):
+        st = self.get_state()
+        return (st.threshold[0], st.threshold[1]), (st.offset[0], st.offset[1]), bool(st.thresholds_set)
+
+
+def host_buffer(nbytes: int) -> np.ndarray:
+    """Pinned host buffer (cudaMallocHost) as a uint8 numpy array; freed with the array's owner."""
+    p = C.c_void_p()
+    N.check(N.lib().sdbe_host_alloc(C.byref(p), nbytes))
+    arr = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(p.value))
+    return _PinnedArray(arr, p.value)
+
+
+class _PinnedArray(np.ndarray):
+    def __new__(cls, arr, ptr):
+        obj = arr.view(cls)
+        obj._pinned_ptr = ptr
+        return obj
+
+    def __array_finalize__(self, obj):
+        self._pinned_ptr = None  # views never own the allocation
+
+    def free(self):
+        if getattr(self, "_pinned_ptr", None):
+            N.lib().sdbe_host_free(self._pinned_ptr)
+            self._pinned_ptr = None

@@ -1,0 +1,79 @@
+"""CPU checks of the C ABI: the library builds, loads and exports every symbol
+declared in include/sdbe.h, and the Python binding agrees with the header."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "sdbe.h")
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sdbe_[a-z0-9_]+)\s*\(", text)))
+
+
+def _header_defines():
+    out = {}
+    for name, val in re.findall(r"#define\s+(SDBE_[A-Z0-9_]+)\s+(-?\d+)u?\b", open(HEADER).read()):
+        out[name] = int(val)
+    return out
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    from sdbe_gb300 import _native
+
+    return _native
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = C.CDLL(built.LIB_PATH)
+    names = _declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(built):
+    assert set(_declared_functions()) == set(built.SIGNATURES)
+
+
+def test_struct_layouts(built):
+    assert C.sizeof(built.Config) == 16 * 4
+    assert C.sizeof(built.State) == 4 * 2 * 2 + 4 * 4 + 8 + 4 * 4 + 6 * 4
+    assert C.sizeof(built.Result) == 6 * 8
+
+
+def test_constants_match_header(built):
+    d = _header_defines()
+    assert d["SDBE_IN_PKT_BYTES"] == built.IN_PKT_BYTES
+    assert d["SDBE_OUT_PKT_BYTES"] == built.OUT_PKT_BYTES
+    assert d["SDBE_OUT_PKT_DATA_BYTES"] == built.OUT_PKT_DATA_BYTES
+    assert d["SDBE_BATCH_SNAPSHOTS"] == built.BATCH_SNAPSHOTS
+    assert d["SDBE_OK"] == built.OK and d["SDBE_ERR_CAPACITY"] == built.ERR_CAPACITY
+    assert d["SDBE_IN_HOST"] == built.IN_HOST and d["SDBE_OUT_FRAMED"] == built.OUT_FRAMED
+
+
+def test_error_paths_without_gpu(built):
+    """Argument checks run before any CUDA call and report through sdbe_last_error."""
+    lib = built.lib()
+    h = C.c_void_p()
+    assert lib.sdbe_create(None, C.byref(h)) == built.ERR_ARG
+    cfg = built.Config()
+    cfg.max_frames = 0
+    assert lib.sdbe_create(C.byref(cfg), C.byref(h)) == built.ERR_ARG
+    assert "max_frames" in built.last_error()
+    cfg.max_frames = 143
+    cfg.trim_mhz = 241
+    assert lib.sdbe_create(C.byref(cfg), C.byref(h)) == built.ERR_ARG
+    assert lib.sdbe_quantize2bit(None, None, 17, 1.0, 0.0, None) == built.ERR_ARG
+    assert lib.sdbe_reorder_mar2015(None, 1, None, None) == built.ERR_ARG
+    assert lib.sdbe_process(None, None, 0, 0, 0, None, 0, 0, None, None) == built.ERR_ARG

@@ -1,0 +1,229 @@
+"""End-to-end parity of sdbe_process (the drop-in GPU stage) against the oracle.
+
+Bar: 2-bit code agreement >= 99.9% against the FP64 oracle (FP32 path);
+unpack, carry, framing and header fields bit-exact; error codes for bad calls.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import codes_of, dev, empty, host
+from oracle import sdbe_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+AGREE_MIN = 0.999
+
+
+@pytest.fixture(scope="module")
+def S():
+    import __graft_entry__ as g
+
+    g.build()
+    from sdbe_gb300 import synth
+
+    return synth
+
+
+def _agreement(a, b):
+    return float(np.mean(codes_of(a) == codes_of(b)))
+
+
+@pytest.fixture(scope="module")
+def cfg1(S):
+    spec = S.config1()
+    p = S.generate(spec)
+    return spec, p
+
+
+def test_process_config1_vs_oracle(S, cfg1):
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=150, max_frames=8) as rs:
+        out, res = rs.process(p, 8, spec.b_start)
+        (th0, th1), (off0, off1), ok = rs.thresholds
+    assert res.n_batches == 7 and res.n_out_packets == 7 * 128 and res.carry_snapshots == 1024 - 7 * 143
+    assert res.packets_accepted == p.shape[0] and res.packets_rejected == 0 and res.frames_incomplete == 0
+    st = O.StreamState()
+    ref = O.process_group(p, spec.b_start, 8, 150, state=st)
+    assert out.shape == ref.shape
+    for pol in range(2):
+        agree = _agreement(out[pol], ref[pol])
+        assert agree >= AGREE_MIN, (pol, agree)
+    assert ok
+    assert abs(th0 - st.threshold[0]) <= 1e-5 * st.threshold[0]
+    assert abs(th1 - st.threshold[1]) <= 1e-5 * st.threshold[1]
+    assert abs(off0 - st.offset[0]) <= 1e-5 * st.threshold[0]
+
+
+def test_device_path_equals_host_path(S, cfg1):
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=150, max_frames=8) as a, Resampler(trim_mhz=150, max_frames=8) as b:
+        out_h, _ = a.process(p, 8, spec.b_start)
+        d_out = empty(b.output_bytes(8))
+        b.process(dev(p), 8, spec.b_start, out=d_out)
+        np.testing.assert_array_equal(host(d_out).reshape(out_h.shape), out_h)
+
+
+def test_carry_across_calls_is_exact(S, cfg1):
+    """Four calls of 2 B-frames give the same bytes as one call of 8."""
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=150, max_frames=8) as one, Resampler(trim_mhz=150, max_frames=8) as many:
+        ref, _ = one.process(p, 8, spec.b_start)
+        parts = []
+        for k in range(4):
+            o, r = many.process(p[k * 4096:(k + 1) * 4096], 2, spec.b_start + 2 * k)
+            parts.append(o)
+        got = np.concatenate(parts, axis=1)
+        assert r.carry_snapshots == 1024 - 7 * 143
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_framed_output_headers_and_payload(S, cfg1):
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=102, max_frames=8) as rs, Resampler(trim_mhz=102, max_frames=8) as rs2:
+        st = rs.get_state()
+        st.secs_inre, st.df_num_insec, st.edh_psn, st.ref_epoch = 500, 124900, 1, 30
+        st.bdc_sideband, st.rx_sideband = 1, 1
+        rs.set_state(st)
+        framed, res = rs.process(p, 8, spec.b_start, framed=True)
+        plain, _ = rs2.process(p, 8, spec.b_start)
+        st2 = rs.get_state()
+    n = res.n_out_packets
+    assert framed.shape == (2, n, 8224)
+    np.testing.assert_array_equal(framed[:, :, 32:], plain)
+    for pol in range(2):
+        ref = O.vdif_out_header_words(n, pol, secs=500, df=124900, psn=1, ref_epoch=30, bdc_sideband=1,
+                                      rx_sideband=1)
+        np.testing.assert_array_equal(framed[pol, :, :32].copy().view("<u4"), ref)
+    assert st2.edh_psn == 1 + n and st2.df_num_insec == (124900 + n) % 125000
+    assert st2.secs_inre == 500 + (124900 + n) // 125000
+
+
+def test_impaired_stream_zero_fill_and_counts(S):
+    from sdbe_gb300 import Resampler
+
+    spec = S.config1(stream=3)
+    spec.n_frames = 4
+    spec.drop_frac, spec.reorder_frac, spec.reorder_max = 0.01, 0.005, 64
+    p = S.generate(spec)
+    w = p.view("<u4").reshape(p.shape[0], -1)
+    w[5, 0] |= np.uint32(1 << 31)
+    with Resampler(trim_mhz=150, max_frames=4) as rs:
+        out, res = rs.process(p, 4, spec.b_start)
+    assert res.packets_rejected == 1
+    assert res.packets_accepted == p.shape[0] - 1
+    assert res.frames_incomplete == 4
+    ref = O.process_group(p, spec.b_start, 4, 150)
+    for pol in range(2):
+        assert _agreement(out[pol], ref[pol]) >= AGREE_MIN
+
+
+def test_pol1_uses_pol0_threshold_flag(S, cfg1):
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    q = p[:2 * 2048]
+    with Resampler(trim_mhz=150, max_frames=2, pol1_uses_pol0_threshold=True) as rs:
+        out, _ = rs.process(q, 2, spec.b_start)
+    ref = O.process_group(q, spec.b_start, 2, 150, pol1_uses_pol0_threshold=True)
+    assert _agreement(out[1], ref[1]) >= AGREE_MIN
+    ref_own = O.process_group(q, spec.b_start, 2, 150)
+    assert not np.array_equal(ref[1], ref_own[1])
+
+
+def test_fixed_threshold_mode(S, cfg1):
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300._native import THRESH_FIXED, SdbeError
+
+    spec, p = cfg1
+    q = p[:2 * 2048]
+    with Resampler(trim_mhz=150, max_frames=2, threshold_mode=THRESH_FIXED) as rs:
+        with pytest.raises(SdbeError):
+            rs.process(q, 2, spec.b_start)
+        rs.set_thresholds((5.0e6, 6.0e6), (1.0e4, -2.0e4))
+        out, _ = rs.process(q, 2, spec.b_start)
+    st = O.StreamState()
+    st.threshold, st.offset = [5.0e6, 6.0e6], [1.0e4, -2.0e4]
+    ref = O.process_group(q, spec.b_start, 2, 150, state=st)
+    for pol in range(2):
+        assert _agreement(out[pol], ref[pol]) >= AGREE_MIN
+
+
+def test_no_batch_all_carried_then_emitted(S, cfg1):
+    from sdbe_gb300 import Resampler
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=150, max_frames=8) as rs:
+        out, res = rs.process(p[:2048], 1, spec.b_start)
+        assert res.n_batches == 0 and out.shape[1] == 0 and res.carry_snapshots == 128
+        out2, res2 = rs.process(p[2048:4096], 1, spec.b_start + 1)
+        assert res2.n_batches == 1 and res2.carry_snapshots == 256 - 143
+    ref = O.process_group(p[:4096], spec.b_start, 2, 150)
+    assert _agreement(out2[0], ref[0]) >= AGREE_MIN
+
+
+def test_empty_group_reads_zero(S):
+    """No packets at all: every sample is zero, output is the all-zero code pattern."""
+    from sdbe_gb300 import Resampler
+
+    with Resampler(trim_mhz=150, max_frames=2, threshold_mode=1) as rs:
+        rs.set_thresholds((1.0, 1.0), (0.0, 0.0))
+        out, res = rs.process(np.zeros((0, 1056), np.uint8), 2, 0)
+    assert res.n_batches == 1 and res.packets_accepted == 0 and res.frames_incomplete == 2
+    assert (codes_of(out) == 2).all()   # 0 - offset 0 >= 0 and < th -> code 2
+
+
+def test_bad_calls_raise(S, cfg1):
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300._native import ERR_CAPACITY, SdbeError
+
+    spec, p = cfg1
+    with Resampler(trim_mhz=150, max_frames=2) as rs:
+        with pytest.raises(SdbeError) as e:
+            rs.process(p, 8, spec.b_start)
+        assert e.value.code == ERR_CAPACITY
+        small = np.empty((2, 10, 8192), np.uint8)
+        with pytest.raises(SdbeError) as e:
+            rs.process(p[:4096], 2, spec.b_start, out=small)
+        assert e.value.code == ERR_CAPACITY
+
+
+def test_full_size_512_frames_properties(S):
+    """512-frame stream (the bench workload): sampled batches match the oracle,
+    the run is deterministic, and the code histogram is the 2-bit Gaussian one."""
+    from sdbe_gb300 import Resampler
+
+    spec = S.config2()
+    p = S.generate(spec)
+    with Resampler(trim_mhz=150, max_frames=512) as rs:
+        d_p = dev(p)
+        d_out = empty(rs.output_bytes(512))
+        _, res = rs.process(d_p, 512, spec.b_start, out=d_out)
+        (th0, th1), (off0, off1), _ = rs.thresholds
+        first = host(d_out).copy()
+        rs.reset()
+        rs.process(d_p, 512, spec.b_start, out=d_out)
+        second = host(d_out)
+    assert res.n_batches == 458 and res.packets_accepted == 512 * 2048
+    assert np.array_equal(first, second)
+    out = first.reshape(2, 458 * 128, 8192)
+    hist = np.bincount(codes_of(out[0, :128 * 8]), minlength=4) / (128 * 8 * 32768)
+    assert abs(hist[0] - 0.1587) < 0.01 and abs(hist[3] - 0.1587) < 0.01
+    for b in (0, 229, 457):
+        s0, s1 = b * 143, (b + 1) * 143
+        f0, f1 = s0 // 128, (s1 - 1) // 128 + 1
+        sel = p[f0 * 2048:f1 * 2048]
+        beng = O.vdif_to_beng(sel, spec.b_start + f0, f1 - f0)
+        for pol, (th, off) in enumerate(((th0, off0), (th1, off1))):
+            spec_c = O.beng_to_complex(beng[pol].reshape(-1, 16384, 2))[s0 - f0 * 128:s1 - f0 * 128]
+            y = O.r2dbe_c2r(O.swarm_r2c(O.swarm_c2r(spec_c).reshape(-1)), 1200)
+            ref = O.pack2bit(O.quantize2bit_codes(y, th, off, np.float32)).view(np.uint8)
+            got = out[pol, b * 128:(b + 1) * 128]
+            assert _agreement(got, ref) >= AGREE_MIN, (b, pol)
