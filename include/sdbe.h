@@ -215,6 +215,22 @@ int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, f
  * out[0] = mean (quantizeOffset), out[1] = sqrt(M2/(n-1)) (quantizeThreshold). */
 int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *stream);
 
+/* Allocation-free variant of sdbe_summary_stats.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc: a thread that shares
+ * the device with asynchronous packet/payload copies (a cudaMalloc or
+ * cudaFree can synchronize the whole device and stall them), or a process
+ * held to a fixed, pre-reserved memory budget.  Its scratch is a fixed
+ * 131,088-byte device array (8192 FP64 partial pairs + the result) that every
+ * device loading the library holds until exit; n may be at most
+ * SDBE_NOALLOC_MAX_SAMPLES (8192 partials x 16384 samples), larger n returns
+ * SDBE_ERR_CAPACITY.  The first call on a device looks up the array's device
+ * address with that device current; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race.  Nothing accumulates in it across calls,
+ * so it needs no clearing.  Allocates nothing, device or host. */
+#define SDBE_NOALLOC_MAX_SAMPLES 134217728LL
+int sdbe_summary_stats_noalloc(const float *in, int64_t n, double *out_host, void *stream);
+
 /* quantize2bit (.cu:565-583): n floats -> n/16 words (n multiple of 16). */
 int sdbe_quantize2bit(const float *in, uint32_t *out, int64_t n, float thresh, float offset,
                       void *stream);

@@ -27,6 +27,7 @@ SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED = 0, 1
 MAP_APHIDS, MAP_MAR2015 = 0, 1
 IN_HOST, OUT_HOST, OUT_FRAMED, SYNC = 1, 2, 4, 8
+NOALLOC_MAX_SAMPLES = 134217728
 
 
 class Config(C.Structure):
@@ -85,6 +86,7 @@ SIGNATURES = {
     "sdbe_r2dbe_c2r": (C.c_int, [vp, vp, i64, i32, vp, vp]),
     "sdbe_resample_chunks": (C.c_int, [vp, vp, i64, vp, vp]),
     "sdbe_summary_stats": (C.c_int, [vp, i64, C.POINTER(C.c_double), vp]),
+    "sdbe_summary_stats_noalloc": (C.c_int, [vp, i64, C.POINTER(C.c_double), vp]),
     "sdbe_quantize2bit": (C.c_int, [vp, vp, i64, f32, f32, vp]),
     "sdbe_vdif_headers": (C.c_int, [vp, i64, i64, u32, u32, u64, u32, u32, u32, u32, vp]),
     "sdbe_reorder_mar2015": (C.c_int, [vp, i32, vp, vp]),
