@@ -172,6 +172,74 @@ __device__ __forceinline__ void dft(float2 *v) {
     }
 }
 
+// ---- compile-time twiddle constants ---------------------------------------
+// sin/cos of 2*pi*num/den in double at compile time: exact integer reduction
+// to a quadrant, then Taylor series on |x| <= pi/4 (error < 1e-16).
+constexpr double kPi = 3.141592653589793238462643383279502884;
+__host__ __device__ constexpr double cx_sin_small(double x) {
+    double x2 = x * x, term = x, sum = x;
+    for (int k = 1; k < 14; ++k) {
+        term *= -x2 / ((2.0 * k) * (2.0 * k + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+__host__ __device__ constexpr double cx_cos_small(double x) {
+    double x2 = x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 14; ++k) {
+        term *= -x2 / ((2.0 * k - 1.0) * (2.0 * k));
+        sum += term;
+    }
+    return sum;
+}
+// Returns {cos, sin} of 2*pi*num/den.
+struct CS {
+    double c, s;
+};
+__host__ __device__ constexpr CS cx_cossin_2pi(long long num, long long den) {
+    long long m = num % den;
+    if (m < 0) m += den;
+    // 8m/den in [0, 8): octant index q = round(4m/den) in [0, 4], remainder t in [-1/2, 1/2]
+    const long long q4 = (8 * m + den) / (2 * den);       // nearest quarter-turn
+    const double t = (4.0 * static_cast<double>(m) - static_cast<double>(q4) * static_cast<double>(den)) /
+                     static_cast<double>(den);          // fraction of a quarter-turn
+    const double x = t * (kPi / 2.0);
+    const double sx = cx_sin_small(x), cxv = cx_cos_small(x);
+    switch (q4 & 3) {
+        case 0: return CS{cxv, sx};
+        case 1: return CS{-sx, cxv};
+        case 2: return CS{-cxv, -sx};
+        default: return CS{sx, -cxv};
+    }
+}
+// W_N^E = exp(-2 pi i E/N) rounded to float, usable as device constants.
+template <long long N, long long E>
+struct TwC {
+    static constexpr CS v = cx_cossin_2pi(E, N);
+    static constexpr float c = static_cast<float>(v.c);
+    static constexpr float s = static_cast<float>(-v.s);
+};
+// a * W_N^E (or a * conj(W_N^E) when CONJ) with E a compile-time value.
+template <long long N, long long E, bool CONJ>
+__device__ __forceinline__ float2 mul_tc(float2 a) {
+    constexpr float c = TwC<N, E>::c;
+    constexpr float s = CONJ ? -TwC<N, E>::s : TwC<N, E>::s;
+    if constexpr (E % N == 0) {
+        return a;
+    } else {
+        return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+// Padded index of the small shared-memory twiddle tables.
+__device__ __forceinline__ int tp(int m) { return m + (m >> 4); }
+constexpr int tp_len(int n) { return n + ((n - 1) >> 4) + 1; }
+
+// W_N^e from the two-level tables H[a] = W_N^{128 a}, L[b] = W_N^b.
+__device__ __forceinline__ float2 tw2(const float2 *H, const float2 *L, int e) {
+    return cmul(H[tp(e >> 7)], L[tp(e & 127)]);
+}
+
 // Table twiddle W_N^e (forward) or its conjugate (inverse).
 template <bool INV>
 __device__ __forceinline__ float2 twiddle(const float2 *__restrict__ tab, int e) {

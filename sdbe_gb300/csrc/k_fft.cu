@@ -1,16 +1,19 @@
-// Resampling FFT kernels, one CTA per transform, data resident in shared memory.
+// Resampling FFT kernels: one transform per CTA at a time, the whole transform
+// resident in shared memory, persistent grids (one CTA per SM looping over
+// transforms, twiddle tables loaded into shared memory once per CTA).
 //
 // Reference: the three cuFFT plans of vdif_inout_gpu_thread.cu:271-333 run by
 // SwarmC2R / SwarmR2C / R2dbeC2R (:589-709) on each 143-snapshot batch.
 //   stage A  C2R 32768 per snapshot  = 16384-point complex inverse FFT plus
 //            Hermitian pre-processing, fed straight from the packed 2-bit
-//            spectrum (beng_int8_to_cufftComplex and the Nyquist memset fused).
+//            spectrum (beng_int8_to_cufftComplex and the Nyquist memset fused);
+//            the next snapshot's 8 KB are prefetched with cp.async.
 //   stage BC R2C 36608 per chunk = 18304-point complex FFT + post-processing,
 //            bins [skip, skip+16384] selected in registers, C2R 32768 through
 //            a 16384-point inverse FFT, then quantize2bit in the epilogue.
 // All scaling is cuFFT's unnormalised convention.
-#include <vector>
 #include <cmath>
+#include <vector>
 
 #include "fft_core.cuh"
 #include "launchers.cuh"
@@ -19,24 +22,60 @@
 namespace sdbe {
 
 constexpr int kNTA = 512;   // stage A threads: 512 radix-32 butterflies per pass
-constexpr int kNTB = 576;   // stage BC threads: balances the 16/8/11/13 passes of 18304
+constexpr int kNTB = 512;   // stage BC threads: 4 warps per SM sub-partition -> 128 registers
 constexpr int kPadA = padded_len(kMA);
 constexpr int kPadB = padded_len(kMB);
-constexpr size_t kSmemA = kGroups * sizeof(uint32_t) + kPadA * sizeof(float2);
-constexpr size_t kSmemB = kPadB * sizeof(float2);
+
+// Shared-memory twiddle tables (float2, padded with tp()).
+constexpr int kT1024 = tp_len(1024);   // W_1024^m            (16384-point pass 2)
+constexpr int kT128 = tp_len(128);     // two-level halves
+constexpr int kT208 = tp_len(208);     // W_208^m             (18304-point radix-13 pass)
+constexpr int kT2288 = tp_len(2288);   // W_2288^m            (18304-point radix-11 pass)
+constexpr int kH18304 = tp_len(143);   // W_18304^{128 a}
+constexpr int kTwA = kT1024 + 2 * kT128;                              // stage A tables
+constexpr int kTwB = kTwA + kT208 + kT2288 + kH18304 + kT128;          // stage BC tables
+constexpr size_t kSmemA = 2 * kGroups * sizeof(uint32_t) + (kPadA + kTwA) * sizeof(float2);
+constexpr size_t kSmemB = (kPadB + kTwB) * sizeof(float2);
+
+// ---- table loading --------------------------------------------------------
+struct TabsA {  // inverse-16384 tables
+    float2 *t1024, *h16384, *l16384;
+};
+struct TabsB {  // forward-18304 tables
+    float2 *t208, *t2288, *h18304, *l18304;
+};
+
+__device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
+    for (int m = threadIdx.x; m < 1024; m += blockDim.x) t.t1024[tp(m)] = __ldg(tw.w16384 + 16 * m);
+    for (int m = threadIdx.x; m < 128; m += blockDim.x) {
+        t.h16384[tp(m)] = __ldg(tw.w16384 + 128 * m);
+        t.l16384[tp(m)] = __ldg(tw.w16384 + m);
+    }
+}
+
+__device__ __forceinline__ void load_tabs_b(TabsB t, const Twiddles &tw) {
+    for (int m = threadIdx.x; m < 2288; m += blockDim.x) t.t2288[tp(m)] = __ldg(tw.w18304 + 8 * m);
+    for (int m = threadIdx.x; m < 208; m += blockDim.x) t.t208[tp(m)] = __ldg(tw.w18304 + 88 * m);
+    for (int m = threadIdx.x; m < 143; m += blockDim.x) t.h18304[tp(m)] = __ldg(tw.w18304 + 128 * m);
+    for (int m = threadIdx.x; m < 128; m += blockDim.x) t.l18304[tp(m)] = __ldg(tw.w18304 + m);
+}
+
+__device__ __forceinline__ TabsB tabs_b_at(float2 *tb) {
+    float2 *p = tb + kTwA;
+    return TabsB{p, p + kT208, p + kT208 + kT2288, p + kT208 + kT2288 + kH18304};
+}
 
 // ---------------------------------------------------------------------------
-// Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(k) gives input
-// k (it may read `sm`; the first barrier separates those reads from the
-// writes), epi(jj, u) receives outputs z[jj + 1024 r], r < 16.  blockDim.x is
-// a multiple of 32 and >= 512.
+// Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(r) gives
+// input element tid + 512 r of this thread (it may read `sm`: a barrier
+// separates those reads from the writes); epi(jj, u) receives outputs
+// z[jj + 1024 r], r < 16.  blockDim.x is a multiple of 32 and >= 512.
 template <class In, class Epi>
-__device__ __forceinline__ void ifft16384(float2 *sm, const float2 *__restrict__ w16384, In zin, Epi epi) {
+__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi) {
     const int tid = threadIdx.x;
     float2 v[32];
     if (tid < 512) {
-#pragma unroll
-        for (int r = 0; r < 32; ++r) v[r] = zin(tid + 512 * r);
+        zin(v);
         dft<32, true>(v);
     }
     __syncthreads();
@@ -48,9 +87,19 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const float2 *__restrict__
     if (tid < 512) {
 #pragma unroll
         for (int r = 0; r < 32; ++r) v[r] = sm[pad(tid + 512 * r)];
+        // W_1024^{jm r} = A[r/8] * S[r%8]
         const int jm = tid & 31;
+        float2 S[8], A[4];
 #pragma unroll
-        for (int r = 1; r < 32; ++r) v[r] = cmul(v[r], twiddle<true>(w16384, jm * r * 16));
+        for (int s = 1; s < 8; ++s) S[s] = T.t1024[tp(jm * s)];
+#pragma unroll
+        for (int a = 1; a < 4; ++a) A[a] = T.t1024[tp(jm * 8 * a)];
+#pragma unroll
+        for (int r = 1; r < 32; ++r) {
+            const int a = r >> 3, s = r & 7;
+            const float2 w = a == 0 ? S[s] : (s == 0 ? A[a] : cmul(A[a], S[s]));
+            v[r] = cmulc(v[r], w);
+        }
         dft<32, true>(v);
     }
     __syncthreads();
@@ -64,90 +113,124 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const float2 *__restrict__
         float2 u[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) u[r] = sm[pad(jj + 1024 * r)];
+        // W_16384^{jj r} = A[r/4] * S[r%4]
+        float2 S[4], A[4];
 #pragma unroll
-        for (int r = 1; r < 16; ++r) u[r] = cmul(u[r], twiddle<true>(w16384, jj * r));
+        for (int s = 1; s < 4; ++s) S[s] = tw2(T.h16384, T.l16384, jj * s);
+#pragma unroll
+        for (int a = 1; a < 4; ++a) A[a] = tw2(T.h16384, T.l16384, jj * 4 * a);
+#pragma unroll
+        for (int r = 1; r < 16; ++r) {
+            const int a = r >> 2, s = r & 3;
+            const float2 w = a == 0 ? S[s] : (s == 0 ? A[a] : cmul(A[a], S[s]));
+            u[r] = cmulc(u[r], w);
+        }
         dft<16, true>(u);
         epi(jj, u);
     }
 }
 
-// In-place Stockham pass in shared memory: every thread first holds all of
-// its butterflies in registers, then all threads write after a barrier.
-template <int R, int NS, int N, int NT, bool INV>
-__device__ __forceinline__ void smem_pass(float2 *sm, const float2 *__restrict__ tw) {
-    constexpr int NB = N / R;
-    constexpr int ITERS = (NB + NT - 1) / NT;
-    constexpr int TS = N / (NS * R);
-    float2 v[ITERS][R];
-#pragma unroll
-    for (int it = 0; it < ITERS; ++it) {
-        const int j = threadIdx.x + it * NT;
-        if (j < NB) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) v[it][r] = sm[pad(j + NB * r)];
-            const int jm = j % NS;
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[it][r] = cmul(v[it][r], twiddle<INV>(tw, jm * r * TS));
-            dft<R, INV>(v[it]);
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < ITERS; ++it) {
-        const int j = threadIdx.x + it * NT;
-        if (j < NB) {
-            const int base = (j / NS) * NS * R + (j % NS);
-#pragma unroll
-            for (int r = 0; r < R; ++r) sm[pad(base + NS * r)] = v[it][r];
-        }
-    }
-    __syncthreads();
-}
-
-// Forward 18304-point FFT of the complex sequence z[m] = x[2m] + i x[2m+1]
-// read from global memory; result Z in natural order in `sm`.
-// Radices 16 (from global) x 8 x 11 x 13.
-__device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *__restrict__ z,
-                                                     const float2 *__restrict__ w18304) {
+// Forward 18304-point FFT of z[m] = x[2m] + i x[2m+1] read from global memory;
+// result Z in natural order in `sm`.  In-place decimation in time, radices
+// 16 (from global) x 13 x 11 x 8: the first pass reads z[j + 1144 r] (coalesced)
+// and writes its 16 outputs to slots 16*rho(j) + r, rho = digit reversal of j
+// over (8, 11, 13); every later butterfly reads and writes the same slots
+// g*Ns*R + k + Ns*r with twiddles W_{Ns*R}^{k r}, so passes need no staging.
+__device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *__restrict__ z, const TabsB &T) {
     constexpr int NB1 = kMB / 16;  // 1144
-    for (int j = threadIdx.x; j < NB1; j += kNTB) {
+    for (int j = threadIdx.x; j < NB1; j += blockDim.x) {
         float2 v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = __ldcs(z + j + NB1 * r);
         dft<16, false>(v);
+        const int rho = (j / 88) + 13 * (((j >> 3) % 11) + 11 * (j & 7));
 #pragma unroll
-        for (int r = 0; r < 16; ++r) sm[pad(16 * j + r)] = v[r];
+        for (int r = 0; r < 16; ++r) sm[pad(16 * rho + r)] = v[r];
     }
     __syncthreads();
-    smem_pass<8, 16, kMB, kNTB, false>(sm, w18304);
-    smem_pass<11, 128, kMB, kNTB, false>(sm, w18304);
-    smem_pass<13, 1408, kMB, kNTB, false>(sm, w18304);
+    // radix 13, Ns = 16: twiddles W_208^{k r}
+    for (int b = threadIdx.x; b < kMB / 13; b += blockDim.x) {
+        const int k = b & 15, base = (b >> 4) * 208 + k;
+        float2 v[13];
+#pragma unroll
+        for (int r = 0; r < 13; ++r) v[r] = sm[pad(base + 16 * r)];
+#pragma unroll
+        for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], T.t208[tp(k * r)]);
+        dft<13, false>(v);
+#pragma unroll
+        for (int r = 0; r < 13; ++r) sm[pad(base + 16 * r)] = v[r];
+    }
+    __syncthreads();
+    // radix 11, Ns = 208: twiddles W_2288^{k r}
+    for (int b = threadIdx.x; b < kMB / 11; b += blockDim.x) {
+        const int k = b % 208, base = (b / 208) * 2288 + k;
+        float2 v[11];
+#pragma unroll
+        for (int r = 0; r < 11; ++r) v[r] = sm[pad(base + 208 * r)];
+#pragma unroll
+        for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], T.t2288[tp(k * r)]);
+        dft<11, false>(v);
+#pragma unroll
+        for (int r = 0; r < 11; ++r) sm[pad(base + 208 * r)] = v[r];
+    }
+    __syncthreads();
+    // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
+    for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
+        float2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = sm[pad(k + 2288 * r)];
+        float2 S[4];
+#pragma unroll
+        for (int q = 1; q < 4; ++q) S[q] = tw2(T.h18304, T.l18304, k * q);
+        const float2 A1 = tw2(T.h18304, T.l18304, 4 * k);
+#pragma unroll
+        for (int r = 1; r < 8; ++r) {
+            const float2 w = r < 4 ? S[r] : (r == 4 ? A1 : cmul(A1, S[r - 4]));
+            v[r] = cmul(v[r], w);
+        }
+        dft<8, false>(v);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) sm[pad(k + 2288 * r)] = v[r];
+    }
+    __syncthreads();
 }
 
 // Unnormalised R2C bin q (0 <= q <= 18304) of the 36608 real samples from the
-// half-length complex transform Z in `sm`:
-//   X[q] = (Z[q] + conj Z[M-q])/2 - i W^q (Z[q] - conj Z[M-q])/2,  W = e^{-2 pi i/36608}.
-__device__ __forceinline__ float2 r2c_bin(const float2 *sm, const float2 *__restrict__ w36608, int q) {
+// half-length complex transform Z in `sm`, given w = e^{-2 pi i q/36608}:
+//   X[q] = (Z[q] + conj Z[M-q])/2 - i w (Z[q] - conj Z[M-q])/2.
+__device__ __forceinline__ float2 r2c_bin(const float2 *sm, int q, float2 w) {
     const int qa = q == kMB ? 0 : q;
     const int qb = q == 0 ? 0 : kMB - q;
     const float2 za = sm[pad(qa)];
     const float2 zb = conjf2(sm[pad(qb)]);
     const float2 s = cadd(za, zb), d = csub(za, zb);
-    const float2 wd = cmul(__ldg(w36608 + q), d);
+    const float2 wd = cmul(w, d);
     return make_float2(0.5f * (s.x + wd.y), 0.5f * (s.y - wd.x));
 }
 
-// Hermitian pre-processing of a C2R of length 32768 from bins Y[0..16384]:
-//   Z[k] = (Y[k] + conj Y[M-k]) + i e^{+2 pi i k/32768} (Y[k] - conj Y[M-k]),
+// Hermitian pre-processing of a C2R of length 32768 from bins Y[0..16384],
+// given we = e^{+2 pi i k/32768}:
+//   Z[k] = (Y[k] + conj Y[M-k]) + i we (Y[k] - conj Y[M-k]),
 // imaginary parts of Y[0] and Y[16384] ignored (as cuFFT / numpy do).
-__device__ __forceinline__ float2 c2r_pre(float2 y, float2 ym, int k, const float2 *__restrict__ w32768) {
+__device__ __forceinline__ float2 c2r_pre(float2 y, float2 ym, int k, float2 we) {
     if (k == 0) {
         y.y = 0.f;
         ym.y = 0.f;
     }
     const float2 e = make_float2(y.x + ym.x, y.y - ym.y);
-    const float2 o = cmul(make_float2(y.x - ym.x, y.y + ym.y), twiddle<true>(w32768, k));
+    const float2 o = cmul(make_float2(y.x - ym.x, y.y + ym.y), we);
     return make_float2(e.x - o.y, e.y + o.x);
+}
+
+// e^{+2 pi i (tid + 512 r)/32768} for r = 0..31 from one table value.
+template <int R>
+__device__ __forceinline__ float2 c2r_tw(float2 base) {
+    return mul_tc<64, R, true>(base);
+}
+
+template <int... R, class F>
+__device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
+    (f(std::integral_constant<int, R>{}), ...);
 }
 
 // Packed nibble -> (real, imag) = codes - 2.
@@ -156,132 +239,191 @@ __device__ __forceinline__ float2 nib_value(const uint32_t *sp, int k) {
     return make_float2(static_cast<float>(nib >> 2) - 2.0f, static_cast<float>(nib & 3u) - 2.0f);
 }
 
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
-// Stage A: grid (n_snaps, 2 pols).  Packed spectrum of snapshot s of pol p at
-// spec + p*spec_pol_stride + (snap0 + s)*2048; time series to
+// Stage A (persistent): items = n_snaps x n_pols.  Packed spectrum of snapshot
+// s of pol p at spec + p*spec_pol_stride + (snap0 + s)*2048; time series to
 // out + p*out_pol_stride + s*32768.
 __global__ void __launch_bounds__(kNTA, 1)
-    k_swarm_c2r(const uint32_t *__restrict__ spec, int64_t spec_pol_stride, int64_t snap0,
-                float *__restrict__ out, int64_t out_pol_stride, Twiddles tw) {
+    k_swarm_c2r(const uint32_t *__restrict__ spec, int64_t spec_pol_stride, int64_t snap0, int64_t n_snaps,
+                int n_pols, float *__restrict__ out, int64_t out_pol_stride, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *sp = reinterpret_cast<uint32_t *>(smem_raw);
-    float2 *sm = reinterpret_cast<float2 *>(smem_raw + kGroups * sizeof(uint32_t));
-    const int pol = blockIdx.y;
-    const int64_t s = blockIdx.x;
-    const uint4 *src = reinterpret_cast<const uint4 *>(spec + pol * spec_pol_stride + (snap0 + s) * kGroups);
-    reinterpret_cast<uint4 *>(sp)[threadIdx.x] = __ldg(src + threadIdx.x);  // 512 x 16 B = 8 KB
-    __syncthreads();
-    float2 *dst = reinterpret_cast<float2 *>(out + pol * out_pol_stride + s * kNA);
-    const float2 *w32768 = tw.w32768;
-    auto zin = [&](int k) -> float2 {
-        const float2 a = nib_value(sp, k);
-        const float2 b = k == 0 ? make_float2(0.f, 0.f) : nib_value(sp, kMA - k);  // X[16384] = 0
-        return c2r_pre(a, b, k, w32768);
+    uint32_t *sp = reinterpret_cast<uint32_t *>(smem_raw);  // [2][2048] double buffer
+    float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
+    TabsA T{sm + kPadA, sm + kPadA + kT1024, sm + kPadA + kT1024 + kT128};
+    load_tabs_a(T, tw);
+    const int64_t n_items = n_snaps * n_pols;
+    auto src_of = [&](int64_t item) {
+        const int64_t pol = item / n_snaps, s = item % n_snaps;
+        return reinterpret_cast<const uint4 *>(spec + pol * spec_pol_stride + (snap0 + s) * kGroups);
     };
-    auto epi = [&](int jj, const float2 *u) {
+    int64_t item = blockIdx.x;
+    if (item < n_items) cp_async16(sp + 4 * threadIdx.x, src_of(item) + threadIdx.x);
+    cp_async_commit();
+    const float2 wbase = conjf2(__ldg(tw.w32768 + threadIdx.x));  // e^{+2 pi i tid/32768}
+    for (int buf = 0; item < n_items; item += gridDim.x, buf ^= 1) {
+        const int64_t next = item + gridDim.x;
+        if (next < n_items) cp_async16(sp + (buf ^ 1) * kGroups + 4 * threadIdx.x, src_of(next) + threadIdx.x);
+        cp_async_commit();
+        cp_async_wait_1();
+        __syncthreads();  // this item's spectrum landed; tables loaded
+        const uint32_t *cur = sp + buf * kGroups;
+        const int64_t pol = item / n_snaps, s = item % n_snaps;
+        float2 *dst = reinterpret_cast<float2 *>(out + pol * out_pol_stride + s * kNA);
+        auto zin = [&](float2 *v) {
+            const int tid = threadIdx.x;
+            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int k = tid + 512 * r;
+                const float2 a = nib_value(cur, k);
+                const float2 b = k == 0 ? make_float2(0.f, 0.f) : nib_value(cur, kMA - k);  // X[16384] = 0
+                v[r] = c2r_pre(a, b, k, c2r_tw<r>(wbase));
+            });
+        };
+        auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) dst[jj + 1024 * r] = u[r];
-    };
-    ifft16384(sm, tw.w16384, zin, epi);
+            for (int r = 0; r < 16; ++r) __stcs(dst + jj + 1024 * r, u[r]);
+        };
+        ifft16384(sm, T, zin, epi);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Stage BC: grid (n_chunks, 2 pols).  Chunk c of pol p: 36608 floats at
-// in + p*in_pol_stride + c*36608.
+// Stage BC (persistent): items = n_chunks x n_pols.  Chunk c of pol p: 36608
+// floats at in + p*in_pol_stride + c*36608.
 //   MODE 0: quantize with thr[p] / thr[2+p] into the u32 payload at
 //           out + p*out_pol_stride + (pkt0 + c)*pkt_stride + payload_off.
 //   MODE 1: floats to fout + p*fout_pol_stride + c*32768 and per-chunk
 //           (n, mean, M2) in FP64 to partials[(p*n_chunks + c)*3].
 //   MODE 2: floats only.
-
 template <int MODE>
 __global__ void __launch_bounds__(kNTB, 1)
-    k_resample(const float *__restrict__ in, int64_t in_pol_stride, int skip, int n_chunks, ResampleOut o,
-               Twiddles tw) {
+    k_resample(const float *__restrict__ in, int64_t in_pol_stride, int skip, int n_chunks, int n_pols,
+               ResampleOut o, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
+    float2 *tb = sm + kPadB;
+    TabsA TA{tb, tb + kT1024, tb + kT1024 + kT128};
+    TabsB TB = tabs_b_at(tb);
     __shared__ double red[64];
-    const int pol = blockIdx.y;
-    const int64_t c = blockIdx.x;
-    const float2 *z = reinterpret_cast<const float2 *>(in + pol * in_pol_stride + c * kNB);
-    fft18304_from_global(sm, z, tw.w18304);
-
-    const float2 *w36608 = tw.w36608, *w32768 = tw.w32768;
-    auto zin = [&](int jj) -> float2 {
-        const float2 y = r2c_bin(sm, w36608, skip + jj);
-        const float2 ym = r2c_bin(sm, w36608, skip + kMA - jj);
-        return c2r_pre(y, ym, jj, w32768);
-    };
-    if constexpr (MODE == 0) {
-        uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride + (o.pkt0 + c) * o.pkt_stride +
-                                                       o.payload_off);
-        const float th = o.thr[pol], off = o.thr[2 + pol];
-        auto epi = [&](int jj, const float2 *u) {
-#pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                uint32_t q = (code2(u[r].x, th, off) | (code2(u[r].y, th, off) << 2)) << (4 * (jj & 7));
-                q |= __shfl_xor_sync(0xffffffffu, q, 1);
-                q |= __shfl_xor_sync(0xffffffffu, q, 2);
-                q |= __shfl_xor_sync(0xffffffffu, q, 4);
-                if ((jj & 7) == 0) words[(jj >> 3) + 128 * r] = q;
-            }
+    load_tabs_a(TA, tw);
+    load_tabs_b(TB, tw);
+    const int tid = threadIdx.x;
+    // per-thread bases of the pre/post-processing twiddles
+    const float2 wc = conjf2(__ldg(tw.w32768 + tid));
+    const float2 wq = __ldg(tw.w36608 + skip + tid);
+    const float2 wqm = __ldg(tw.w36608 + skip + kMA - tid);
+    const int64_t n_items = static_cast<int64_t>(n_chunks) * n_pols;
+    for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const int pol = static_cast<int>(item / n_chunks);
+        const int64_t c = item % n_chunks;
+        __syncthreads();  // tables loaded / previous item's last smem reads done
+        const float2 *z = reinterpret_cast<const float2 *>(in + pol * in_pol_stride + c * kNB);
+        fft18304_from_global(sm, z, TB);
+        auto zin = [&](float2 *v) {
+            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int jj = tid + 512 * r;
+                // e^{-2 pi i q/36608}, q = skip + jj and skip + 16384 - jj
+                const float2 y = r2c_bin(sm, skip + jj, mul_tc<143, 2 * r, false>(wq));
+                const float2 ym = r2c_bin(sm, skip + kMA - jj, mul_tc<143, 2 * r, true>(wqm));
+                v[r] = c2r_pre(y, ym, jj, c2r_tw<r>(wc));
+            });
         };
-        ifft16384(sm, tw.w16384, zin, epi);
-    } else {
-        float2 *fo = reinterpret_cast<float2 *>(o.fout + pol * o.fout_pol_stride + c * kNC);
-        double s1 = 0.0, s2 = 0.0;
-        auto epi = [&](int jj, const float2 *u) {
+        if constexpr (MODE == 0) {
+            uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
+                                                           (o.pkt0 + c) * o.pkt_stride + o.payload_off);
+            const float th = o.thr[pol], off = o.thr[2 + pol];
+            auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                fo[jj + 1024 * r] = u[r];
-                if constexpr (MODE == 1) {
-                    const double a = u[r].x, b = u[r].y;
-                    s1 += a + b;
-                    s2 += a * a + b * b;
+                for (int r = 0; r < 16; ++r) {
+                    uint32_t q = (code2(u[r].x, th, off) | (code2(u[r].y, th, off) << 2)) << (4 * (jj & 7));
+                    q |= __shfl_xor_sync(0xffffffffu, q, 1);
+                    q |= __shfl_xor_sync(0xffffffffu, q, 2);
+                    q |= __shfl_xor_sync(0xffffffffu, q, 4);
+                    if ((jj & 7) == 0) words[(jj >> 3) + 128 * r] = q;
                 }
-            }
-        };
-        ifft16384(sm, tw.w16384, zin, epi);
-        if constexpr (MODE == 1) {
-            block_sum2(s1, s2, red);
-            if (threadIdx.x == 0) {
-                const double n = static_cast<double>(kNC);
-                const double mean = s1 / n;
-                double *pp = o.partials + (static_cast<int64_t>(pol) * n_chunks + c) * 3;
-                pp[0] = n;
-                pp[1] = mean;
-                pp[2] = s2 - s1 * mean;
+            };
+            ifft16384(sm, TA, zin, epi);
+        } else {
+            float2 *fo = reinterpret_cast<float2 *>(o.fout + pol * o.fout_pol_stride + c * kNC);
+            double s1 = 0.0, s2 = 0.0;
+            auto epi = [&](int jj, const float2 *u) {
+#pragma unroll
+                for (int r = 0; r < 16; ++r) {
+                    fo[jj + 1024 * r] = u[r];
+                    if constexpr (MODE == 1) {
+                        const double a = u[r].x, b = u[r].y;
+                        s1 += a + b;
+                        s2 += a * a + b * b;
+                    }
+                }
+            };
+            ifft16384(sm, TA, zin, epi);
+            if constexpr (MODE == 1) {
+                block_sum2(s1, s2, red);
+                if (tid == 0) {
+                    const double n = static_cast<double>(kNC);
+                    const double mean = s1 / n;
+                    double *pp = o.partials + (static_cast<int64_t>(pol) * n_chunks + c) * 3;
+                    pp[0] = n;
+                    pp[1] = mean;
+                    pp[2] = s2 - s1 * mean;
+                }
             }
         }
     }
 }
 
-// SwarmR2C alone: complex64 [n][18305] spectra.  grid (n_chunks).
+// SwarmR2C alone: complex64 [n][18305] spectra (persistent over chunks).
 __global__ void __launch_bounds__(kNTB, 1)
-    k_swarm_r2c(const float *__restrict__ in, float2 *__restrict__ out, Twiddles tw) {
+    k_swarm_r2c(const float *__restrict__ in, int64_t n_chunks, float2 *__restrict__ out, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
-    const int64_t c = blockIdx.x;
-    fft18304_from_global(sm, reinterpret_cast<const float2 *>(in + c * kNB), tw.w18304);
-    float2 *dst = out + c * (kMB + 1);
-    for (int q = threadIdx.x; q <= kMB; q += kNTB) dst[q] = r2c_bin(sm, tw.w36608, q);
+    float2 *tb = sm + kPadB;
+    TabsB TB = tabs_b_at(tb);
+    load_tabs_b(TB, tw);
+    for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        __syncthreads();
+        fft18304_from_global(sm, reinterpret_cast<const float2 *>(in + c * kNB), TB);
+        float2 *dst = out + c * (kMB + 1);
+        for (int q = threadIdx.x; q <= kMB; q += kNTB) dst[q] = r2c_bin(sm, q, __ldg(tw.w36608 + q));
+    }
 }
 
 // R2dbeC2R alone: complex64 [n][18305] from bin skip -> float [n][32768].
 __global__ void __launch_bounds__(kNTB, 1)
-    k_r2dbe_c2r(const float2 *__restrict__ in, int skip, float *__restrict__ out, Twiddles tw) {
+    k_r2dbe_c2r(const float2 *__restrict__ in, int64_t n_chunks, int skip, float *__restrict__ out, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
-    const int64_t c = blockIdx.x;
-    const float2 *y = in + c * (kMB + 1) + skip;
-    const float2 *w32768 = tw.w32768;
-    auto zin = [&](int k) -> float2 { return c2r_pre(__ldg(y + k), __ldg(y + kMA - k), k, w32768); };
-    float2 *dst = reinterpret_cast<float2 *>(out + c * kNC);
-    auto epi = [&](int jj, const float2 *u) {
+    float2 *tb = sm + kPadB;
+    TabsA TA{tb, tb + kT1024, tb + kT1024 + kT128};
+    load_tabs_a(TA, tw);
+    const int tid = threadIdx.x;
+    const float2 wc = conjf2(__ldg(tw.w32768 + tid));
+    for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        __syncthreads();
+        const float2 *y = in + c * (kMB + 1) + skip;
+        auto zin = [&](float2 *v) {
+            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int k = tid + 512 * r;
+                v[r] = c2r_pre(__ldg(y + k), __ldg(y + kMA - k), k, c2r_tw<r>(wc));
+            });
+        };
+        float2 *dst = reinterpret_cast<float2 *>(out + c * kNC);
+        auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) dst[jj + 1024 * r] = u[r];
-    };
-    ifft16384(sm, tw.w16384, zin, epi);
+            for (int r = 0; r < 16; ++r) dst[jj + 1024 * r] = u[r];
+        };
+        ifft16384(sm, TA, zin, epi);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -427,40 +569,51 @@ cudaError_t configure_fft_kernels() {
     return cudaSuccess;
 }
 
+// Persistent grid size: one CTA per SM, at most `items`.
+static unsigned persistent_grid(int64_t items) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 1;
+    }
+    return static_cast<unsigned>(items < sms ? items : sms);
+}
+
 // ---- launchers ----------------------------------------------------------------
 cudaError_t launch_swarm_c2r(const uint32_t *spec, int64_t spec_pol_stride, int64_t snap0, int64_t n_snaps, int n_pols,
                              float *out, int64_t out_pol_stride, const Twiddles &tw, cudaStream_t st) {
     if (n_snaps <= 0) return cudaSuccess;
-    dim3 grid(static_cast<unsigned>(n_snaps), n_pols);
-    k_swarm_c2r<<<grid, kNTA, kSmemA, st>>>(spec, spec_pol_stride, snap0, out, out_pol_stride, tw);
+    k_swarm_c2r<<<persistent_grid(n_snaps * n_pols), kNTA, kSmemA, st>>>(spec, spec_pol_stride, snap0, n_snaps, n_pols,
+                                                                          out, out_pol_stride, tw);
     return cudaGetLastError();
 }
 
 cudaError_t launch_resample(int mode, const float *in, int64_t in_pol_stride, int skip, int64_t n_chunks, int n_pols,
                             const ResampleOut &o, const Twiddles &tw, cudaStream_t st) {
     if (n_chunks <= 0) return cudaSuccess;
-    dim3 grid(static_cast<unsigned>(n_chunks), n_pols);
+    const unsigned grid = persistent_grid(n_chunks * n_pols);
     const int nc = static_cast<int>(n_chunks);
     if (mode == 0)
-        k_resample<0><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, o, tw);
+        k_resample<0><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
     else if (mode == 1)
-        k_resample<1><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, o, tw);
+        k_resample<1><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
     else
-        k_resample<2><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, o, tw);
+        k_resample<2><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
     return cudaGetLastError();
 }
 
 cudaError_t launch_swarm_r2c(const float *in, int64_t n_chunks, void *out, const Twiddles &tw, cudaStream_t st) {
     if (n_chunks <= 0) return cudaSuccess;
-    k_swarm_r2c<<<static_cast<unsigned>(n_chunks), kNTB, kSmemB, st>>>(in, static_cast<float2 *>(out), tw);
+    k_swarm_r2c<<<persistent_grid(n_chunks), kNTB, kSmemB, st>>>(in, n_chunks, static_cast<float2 *>(out), tw);
     return cudaGetLastError();
 }
 
 cudaError_t launch_r2dbe_c2r(const void *in, int64_t n_chunks, int skip, float *out, const Twiddles &tw,
                              cudaStream_t st) {
     if (n_chunks <= 0) return cudaSuccess;
-    k_r2dbe_c2r<<<static_cast<unsigned>(n_chunks), kNTB, kSmemB, st>>>(static_cast<const float2 *>(in), skip, out,
-                                                                        tw);
+    k_r2dbe_c2r<<<persistent_grid(n_chunks), kNTB, kSmemB, st>>>(static_cast<const float2 *>(in), n_chunks, skip, out,
+                                                                  tw);
     return cudaGetLastError();
 }
 
