@@ -64,6 +64,8 @@ extern "C" {
 #define SDBE_OUT_HOST 2u           /* output goes to host memory (copied out)            */
 #define SDBE_OUT_FRAMED 4u         /* write 8224-B VDIF frames with headers              */
 #define SDBE_SYNC 8u               /* synchronize the stream before returning            */
+#define SDBE_ASYNC 16u             /* with host buffers: return without waiting; the
+                                      buffers must stay valid until sdbe_sync          */
 
 typedef struct sdbe_config {
     int32_t device;            /* CUDA device ordinal (resampler->deviceId, .cu:147)        */
@@ -128,7 +130,12 @@ int64_t sdbe_output_bytes(const sdbe_resampler *h, int32_t n_frames, uint32_t fl
  *   out       : host (SDBE_OUT_HOST) or device; out_bytes = its capacity
  *   result    : optional; filling it synchronizes the stream
  * With SDBE_OUT_FRAMED the headers come from the handle's header counters,
- * which advance by the packets written. */
+ * which advance by the packets written.
+ * Host buffers go through two device staging slots on separate copy streams:
+ * the payloads of each FFT wave leave for the host while the next wave
+ * computes, and with SDBE_ASYNC the next call's packet upload overlaps this
+ * call's compute (the overlap the reference gets from its separate ingest,
+ * GPU and output threads).  Host buffers should be pinned (sdbe_host_alloc). */
 int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames,
                  uint64_t b_zero, void *out, int64_t out_bytes, uint32_t flags, void *stream,
                  sdbe_result *result);
@@ -136,6 +143,9 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
 /* State of the stream.  get/set synchronize the device first (work may be in
  * flight on any stream).  set: thresholds/offsets (marked set if any
  * threshold != 0), header counters; clears the carry when carry_snapshots == 0. */
+/* Wait for all work the handle issued (its streams and the last stream passed
+ * to sdbe_process). */
+int sdbe_sync(sdbe_resampler *h);
 int sdbe_get_state(sdbe_resampler *h, sdbe_state *st);
 int sdbe_set_state(sdbe_resampler *h, const sdbe_state *st);
 /* Forget thresholds and carry (a new stream).  Host-side only: the next

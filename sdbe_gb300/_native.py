@@ -26,7 +26,7 @@ FRAMES_PER_GROUP = 143
 SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED = 0, 1
 MAP_APHIDS, MAP_MAR2015 = 0, 1
-IN_HOST, OUT_HOST, OUT_FRAMED, SYNC = 1, 2, 4, 8
+IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC = 1, 2, 4, 8, 16
 NOALLOC_MAX_SAMPLES = 134217728
 
 
@@ -72,6 +72,7 @@ SIGNATURES = {
     "sdbe_get_state": (C.c_int, [vp, C.POINTER(State)]),
     "sdbe_set_state": (C.c_int, [vp, C.POINTER(State)]),
     "sdbe_reset": (C.c_int, [vp]),
+    "sdbe_sync": (C.c_int, [vp]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

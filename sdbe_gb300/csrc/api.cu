@@ -37,10 +37,18 @@ struct sdbe_resampler {
     float *fout = nullptr;        // [2][128*32768] first-batch floats
     double *partials = nullptr;   // [2][128][3]
     float *thr = nullptr;         // device [8], see k_finalize_thresholds
-    uint8_t *pkt_stage = nullptr;
-    int64_t pkt_stage_bytes = 0;
-    uint8_t *out_stage = nullptr;
-    int64_t out_stage_bytes = 0;
+    // host I/O: two staging slots so one call's copies overlap another's compute
+    cudaStream_t copy_in = nullptr, copy_out = nullptr, last_stream = nullptr;
+    struct Stage {
+        uint8_t *pkt = nullptr;
+        int64_t pkt_bytes = 0;
+        uint8_t *out = nullptr;
+        int64_t out_bytes = 0;
+        cudaEvent_t pkt_ready = nullptr, pkt_free = nullptr, out_free = nullptr;
+    };
+    Stage stage[2];
+    int stage_idx = 0;
+    cudaEvent_t wave_ev = nullptr;
     bool thresholds_set = false;
     int64_t carry = 0;
     uint32_t secs = 0, df = 0, ref_epoch = 0, station = (uint32_t('S') << 8) | uint32_t('m'), bdc = 0, rx = 0;
@@ -119,8 +127,16 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->fout);
     cudaFree(h->partials);
     cudaFree(h->thr);
-    cudaFree(h->pkt_stage);
-    cudaFree(h->out_stage);
+    for (auto &sg : h->stage) {
+        cudaFree(sg.pkt);
+        cudaFree(sg.out);
+        if (sg.pkt_ready) cudaEventDestroy(sg.pkt_ready);
+        if (sg.pkt_free) cudaEventDestroy(sg.pkt_free);
+        if (sg.out_free) cudaEventDestroy(sg.out_free);
+    }
+    if (h->wave_ev) cudaEventDestroy(h->wave_ev);
+    if (h->copy_in) cudaStreamDestroy(h->copy_in);
+    if (h->copy_out) cudaStreamDestroy(h->copy_out);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -134,6 +150,7 @@ int64_t batches_for(const sdbe_resampler *h, int32_t n_frames) {
 
 int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what) {
     if (*cap >= need) return SDBE_OK;
+    if (*buf && cudaDeviceSynchronize() != cudaSuccess) return fail(h, SDBE_ERR_CUDA, "synchronize before regrow");
     cudaFree(*buf);
     *buf = nullptr;
     *cap = 0;
@@ -171,7 +188,7 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     sdbe_resampler *h = new sdbe_resampler();
     h->cfg = *cfg;
     h->skip = skip;
-    h->wave = cfg->wave_batches > 0 ? cfg->wave_batches : 4;
+    h->wave = cfg->wave_batches > 0 ? cfg->wave_batches : 16;
     h->max_snaps = static_cast<int64_t>(cfg->max_frames) * kSnapsPerFrame + kBatchSnaps;
     h->spec_pol_stride = h->max_snaps * kGroups;
     h->ts_pol_stride = static_cast<int64_t>(h->wave) * kBatchSnaps * kNA;
@@ -182,8 +199,16 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
         return fail(nullptr, code, m);
     };
     if (configure_fft_kernels() != cudaSuccess) return bail(SDBE_ERR_CUDA, "kernel attribute setup failed");
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_out, cudaStreamNonBlocking) != cudaSuccess)
         return bail(SDBE_ERR_CUDA, "stream creation failed");
+    bool ev_ok = cudaEventCreateWithFlags(&h->wave_ev, cudaEventDisableTiming) == cudaSuccess;
+    for (auto &sg : h->stage)
+        ev_ok = ev_ok && cudaEventCreateWithFlags(&sg.pkt_ready, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&sg.pkt_free, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&sg.out_free, cudaEventDisableTiming) == cudaSuccess;
+    if (!ev_ok) return bail(SDBE_ERR_CUDA, "event creation failed");
     if (build_twiddles(h->tw, &h->tw_storage) != cudaSuccess) return bail(SDBE_ERR_NOMEM, "twiddle tables");
     bool ok = cudaMalloc(&h->spec, 2 * h->spec_pol_stride * sizeof(uint32_t)) == cudaSuccess &&
               cudaMalloc(&h->bitmap, static_cast<size_t>(cfg->max_frames) * 256) == cudaSuccess &&
@@ -201,7 +226,7 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
 int sdbe_destroy(sdbe_resampler *h) {
     if (!h) return SDBE_OK;
     DeviceGuard g(h->cfg.device);
-    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaDeviceSynchronize();
     free_all(h);
     delete h;
     return SDBE_OK;
@@ -233,23 +258,44 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     if (h->cfg.threshold_mode == SDBE_THRESH_FIXED && !h->thresholds_set && n_batches > 0)
         return fail(h, SDBE_ERR_STATE, "fixed threshold mode needs sdbe_set_state first");
 
+    const bool host_in = (flags & SDBE_IN_HOST) && n_packets > 0;
+    const bool host_out = (flags & SDBE_OUT_HOST) && n_out > 0;
+    sdbe_resampler::Stage &sg = h->stage[h->stage_idx];
+    if (host_in || host_out) h->stage_idx ^= 1;
     const uint8_t *src = static_cast<const uint8_t *>(packets);
-    if ((flags & SDBE_IN_HOST) && n_packets > 0) {
-        int rc = grow(h, &h->pkt_stage, &h->pkt_stage_bytes, n_packets * kPktBytes, "packet staging");
+    if (host_in) {
+        int rc = grow(h, &sg.pkt, &sg.pkt_bytes, n_packets * kPktBytes, "packet staging");
         if (rc) return rc;
-        SDBE_CK(h, cudaMemcpyAsync(h->pkt_stage, packets, n_packets * kPktBytes, cudaMemcpyHostToDevice, st));
-        src = h->pkt_stage;
+        // the slot's previous packets must have been unpacked before they are overwritten
+        SDBE_CK(h, cudaStreamWaitEvent(h->copy_in, sg.pkt_free, 0));
+        SDBE_CK(h, cudaMemcpyAsync(sg.pkt, packets, n_packets * kPktBytes, cudaMemcpyHostToDevice, h->copy_in));
+        SDBE_CK(h, cudaEventRecord(sg.pkt_ready, h->copy_in));
+        SDBE_CK(h, cudaStreamWaitEvent(st, sg.pkt_ready, 0));
+        src = sg.pkt;
     } else if (n_packets > 0 && (reinterpret_cast<uintptr_t>(packets) & 15u)) {
         return fail(h, SDBE_ERR_ARG, "device packet buffer must be 16-byte aligned");
     }
     uint8_t *dev_out = static_cast<uint8_t *>(out);
-    if ((flags & SDBE_OUT_HOST) && n_out > 0) {
-        int rc = grow(h, &h->out_stage, &h->out_stage_bytes, 2 * out_pol_stride, "output staging");
+    if (host_out) {
+        int rc = grow(h, &sg.out, &sg.out_bytes, 2 * out_pol_stride, "output staging");
         if (rc) return rc;
-        dev_out = h->out_stage;
+        // the slot's previous payloads must have left for the host before they are overwritten
+        SDBE_CK(h, cudaStreamWaitEvent(st, sg.out_free, 0));
+        dev_out = sg.out;
     } else if (n_out > 0 && (reinterpret_cast<uintptr_t>(out) & 15u)) {
         return fail(h, SDBE_ERR_ARG, "device output buffer must be 16-byte aligned");
     }
+    // Payload packets [lo, hi) of both pols are final: send them to the host
+    // on the copy stream while the next wave computes.
+    auto ship = [&](int64_t lo, int64_t hi) -> int {
+        if (!host_out || hi <= lo) return SDBE_OK;
+        SDBE_CK(h, cudaEventRecord(h->wave_ev, st));
+        SDBE_CK(h, cudaStreamWaitEvent(h->copy_out, h->wave_ev, 0));
+        SDBE_CK(h, cudaMemcpy2DAsync(static_cast<uint8_t *>(out) + lo * pkt_stride, out_pol_stride,
+                                     dev_out + lo * pkt_stride, out_pol_stride, (hi - lo) * pkt_stride, 2,
+                                     cudaMemcpyDeviceToHost, h->copy_out));
+        return SDBE_OK;
+    };
 
     const int map = h->cfg.channel_map;
     if (n_frames > 0) {
@@ -257,8 +303,18 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
         SDBE_CK(h, launch_unpack(src, n_packets, b_zero, n_frames, map, h->spec, h->spec_pol_stride, h->carry,
                                  h->bitmap, h->counts, h->counts + h->cfg.max_frames, st));
+        if (host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
         SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, h->spec, h->spec_pol_stride, h->carry, st));
         h->launches += n_packets > 0 ? 2 : 1;
+    }
+    if (framed && n_out > 0) {  // headers first, so every shipped wave is complete
+        SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
+                                       h->station, h->bdc, h->rx, st));
+        h->launches += 1;
+        const uint64_t dfs = static_cast<uint64_t>(h->df) + static_cast<uint64_t>(n_out);
+        h->secs += static_cast<uint32_t>(dfs / 125000u);
+        h->df = static_cast<uint32_t>(dfs % 125000u);
+        h->psn += static_cast<uint64_t>(n_out);
     }
 
     int64_t b = 0;
@@ -276,6 +332,7 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         h->thresholds_set = true;
         h->launches += 4;
         b = 1;
+        if (int rc = ship(0, kChunks)) return rc;
     }
     for (; b < n_batches; b += h->wave) {
         const int64_t nb = std::min<int64_t>(h->wave, n_batches - b);
@@ -295,16 +352,9 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
         SDBE_CK(h, timed_end(h, slot, st));
         h->launches += 2;
+        if (int rc = ship(b * kChunks, (b + nb) * kChunks)) return rc;
     }
-    if (framed && n_out > 0) {
-        SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
-                                       h->station, h->bdc, h->rx, st));
-        h->launches += 1;
-        const uint64_t dfs = static_cast<uint64_t>(h->df) + static_cast<uint64_t>(n_out);
-        h->secs += static_cast<uint32_t>(dfs / 125000u);
-        h->df = static_cast<uint32_t>(dfs % 125000u);
-        h->psn += static_cast<uint64_t>(n_out);
-    }
+    if (host_out) SDBE_CK(h, cudaEventRecord(sg.out_free, h->copy_out));
     const int64_t total = h->carry + static_cast<int64_t>(n_frames) * kSnapsPerFrame;
     const int64_t new_carry = total - n_batches * kBatchSnaps;
     if (n_batches > 0 && new_carry > 0) {
@@ -315,10 +365,13 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         }
     }
     h->carry = new_carry;
-    if ((flags & SDBE_OUT_HOST) && n_out > 0)
-        SDBE_CK(h, cudaMemcpyAsync(out, dev_out, 2 * out_pol_stride, cudaMemcpyDeviceToHost, st));
-    const bool need_sync = result || (flags & (SDBE_SYNC | SDBE_IN_HOST | SDBE_OUT_HOST));
-    if (need_sync) SDBE_CK(h, cudaStreamSynchronize(st));
+    h->last_stream = st;
+    const bool need_sync =
+        result || (!(flags & SDBE_ASYNC) && (flags & (SDBE_SYNC | SDBE_IN_HOST | SDBE_OUT_HOST)));
+    if (need_sync) {
+        SDBE_CK(h, cudaStreamSynchronize(st));
+        if (host_out) SDBE_CK(h, cudaStreamSynchronize(h->copy_out));
+    }
     if (result) {
         std::vector<int32_t> cnt(static_cast<size_t>(h->cfg.max_frames) + 1);
         SDBE_CK(h, cudaMemcpy(cnt.data(), h->counts, cnt.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
@@ -334,6 +387,16 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         result->frames_incomplete = incomplete;
         result->carry_snapshots = h->carry;
     }
+    return SDBE_OK;
+}
+
+int sdbe_sync(sdbe_resampler *h) {
+    if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
+    DeviceGuard g(h->cfg.device);
+    SDBE_CK(h, cudaStreamSynchronize(h->copy_in));
+    if (h->last_stream) SDBE_CK(h, cudaStreamSynchronize(h->last_stream));
+    SDBE_CK(h, cudaStreamSynchronize(h->stream));
+    SDBE_CK(h, cudaStreamSynchronize(h->copy_out));
     return SDBE_OK;
 }
 

@@ -110,11 +110,14 @@ class Resampler:
 
     def process(self, packets, n_frames: int, b_zero: int, out=None, framed: bool = False,
                 stream=None, n_packets: int | None = None, out_bytes: int | None = None,
-                want_result: bool = True):
+                want_result: bool = True, asynchronous: bool = False):
         """Run the stage on ``n_frames`` B-frames starting at counter ``b_zero``.
 
         Returns ``(out, GroupResult | None)``; ``out`` holds the payloads as
         ``[2, n_out_packets, 8192]`` (or 8224-B VDIF frames when ``framed``).
+        With ``asynchronous`` (and no result requested) the call returns once
+        the work is queued; ``sync()`` waits for it, and host buffers must stay
+        alive until then.
         """
         if n_packets is None:
             n_packets = int(packets.shape[0]) if hasattr(packets, "shape") else 0
@@ -127,6 +130,8 @@ class Resampler:
             flags |= N.OUT_HOST
         if framed:
             flags |= N.OUT_FRAMED
+        if asynchronous:
+            flags |= N.ASYNC
         cap = _nbytes(out) if out_bytes is None else out_bytes
         res = N.Result() if want_result else None
         st = C.c_void_p(stream) if isinstance(stream, int) else (
@@ -156,6 +161,9 @@ class Resampler:
 
     def reset(self):
         N.check(self._lib.sdbe_reset(self._h), self._h)
+
+    def sync(self):
+        N.check(self._lib.sdbe_sync(self._h), self._h)
 
     # -- profiling ------------------------------------------------------------
     def profile(self, enable: bool = True):
