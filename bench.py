@@ -106,7 +106,7 @@ def _load_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(sample_frames=4, workers=None):
+def cpu_baseline(sample_frames=96, workers=None):
     """The oracle's FP32 path (numpy unpack + scipy.fft) on a bounded sample."""
     from oracle import sdbe_oracle as O
     from sdbe_gb300 import synth
@@ -259,12 +259,12 @@ def run_ours(args):
         dom_bytes, dom_ms = (bc_bytes, bc_ms) if dominant == "stage_bc" else (a_bytes, a_ms)
         achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
         traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            try:
-                traffic = json.load(open(tpath)).get(dominant)
-            except ValueError:
-                traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.txt")
+        if os.path.exists(tpath) and args.wave in (0, 16):  # captured for wave-16 launches
+            for ln in open(tpath):
+                parts = ln.split()
+                if len(parts) == 2 and parts[0] == dominant:
+                    traffic = int(parts[1])
         # FP32 work per launch (nominal 2.5 N log2 N per real transform)
         a_flop = 2.5 * 32768 * 15
         bc_flop = 2.5 * 36608 * np.log2(36608) + 2.5 * 32768 * 15
