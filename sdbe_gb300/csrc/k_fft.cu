@@ -79,14 +79,19 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
         dft<32, true>(v);
     }
     __syncthreads();
+    // padded addresses as base + compile-time offsets: pad(32 t + r) = 33 t + r,
+    // pad(t + 512 r) = pad(t) + 528 r, pad(b + 32 r) = pad(b) + 33 r (b % 32 + r < 32 not
+    // needed: b is a multiple of 1024 plus a lane), pad(j + 1024 r) = pad(j) + 1056 r.
     if (tid < 512) {
+        float2 *dst = sm + 33 * tid;
 #pragma unroll
-        for (int r = 0; r < 32; ++r) sm[pad(32 * tid + r)] = v[r];
+        for (int r = 0; r < 32; ++r) dst[r] = v[r];
     }
     __syncthreads();
     if (tid < 512) {
+        const float2 *src = sm + pad(tid);
 #pragma unroll
-        for (int r = 0; r < 32; ++r) v[r] = sm[pad(tid + 512 * r)];
+        for (int r = 0; r < 32; ++r) v[r] = src[528 * r];
         // W_1024^{jm r} = A[r/8] * S[r%8]
         const int jm = tid & 31;
         float2 S[8], A[4];
@@ -104,15 +109,16 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
     __syncthreads();
     if (tid < 512) {
-        const int base = (tid >> 5) * 1024 + (tid & 31);
+        float2 *dst = sm + (tid >> 5) * 1056 + (tid & 31);
 #pragma unroll
-        for (int r = 0; r < 32; ++r) sm[pad(base + 32 * r)] = v[r];
+        for (int r = 0; r < 32; ++r) dst[33 * r] = v[r];
     }
     __syncthreads();
     for (int jj = tid; jj < 1024; jj += blockDim.x) {
         float2 u[16];
+        const float2 *src = sm + pad(jj);
 #pragma unroll
-        for (int r = 0; r < 16; ++r) u[r] = sm[pad(jj + 1024 * r)];
+        for (int r = 0; r < 16; ++r) u[r] = src[1056 * r];
         // W_16384^{jj r} = A[r/4] * S[r%4]
         float2 S[4], A[4];
 #pragma unroll
@@ -233,10 +239,36 @@ __device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
     (f(std::integral_constant<int, R>{}), ...);
 }
 
-// Packed nibble -> (real, imag) = codes - 2.
+// Packed nibble k -> (real, imag) = codes - 2.  A 2-bit code c placed in the
+// mantissa of 1.5 * 2^23 gives the float 12582912 + c exactly; subtracting
+// 12582914 leaves c - 2 (one logic op and one add, no int-to-float convert).
 __device__ __forceinline__ float2 nib_value(const uint32_t *sp, int k) {
-    const uint32_t nib = (sp[k >> 3] >> ((k & 7) * 4)) & 0xFu;
-    return make_float2(static_cast<float>(nib >> 2) - 2.0f, static_cast<float>(nib & 3u) - 2.0f);
+    const uint32_t w = sp[k >> 3] >> ((k & 7) * 4);
+    const float re = __uint_as_float(0x4B400000u | ((w >> 2) & 3u)) - 12582914.0f;
+    const float im = __uint_as_float(0x4B400000u | (w & 3u)) - 12582914.0f;
+    return make_float2(re, im);
+}
+
+// Hermitian pair of a length-32768 C2R input: from Y[k], Y[M-k] (M = 16384)
+// and we = e^{+2 pi i k/32768},
+//   Z[k]   = (Y[k] + conj Y[M-k]) + i we (Y[k] - conj Y[M-k]) =: e + i t
+//   Z[M-k] = conj(e) + i conj(t),
+// so one complex multiply serves both.
+__device__ __forceinline__ void c2r_pair(float2 y, float2 ym, float2 we, float2 &zk, float2 &zmk) {
+    const float2 e = make_float2(y.x + ym.x, y.y - ym.y);
+    const float2 t = cmul(make_float2(y.x - ym.x, y.y + ym.y), we);
+    zk = make_float2(e.x - t.y, e.y + t.x);
+    zmk = make_float2(e.x + t.y, t.x - e.y);
+}
+
+// Hermitian pair of a length-36608 R2C output: from Z[q], Z[M'-q] (M' = 18304)
+// and w = e^{-2 pi i q/36608}, with s = Z[q] + conj Z[M'-q], t = w (Z[q] - conj Z[M'-q]):
+//   X[q] = (s - i t)/2,   X[M'-q] = (conj(s) - i conj(t))/2.
+__device__ __forceinline__ void r2c_pair(float2 za, float2 zb, float2 w, float2 &xq, float2 &xmq) {
+    const float2 s = make_float2(za.x + zb.x, za.y - zb.y);
+    const float2 t = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
+    xq = make_float2(0.5f * (s.x + t.y), 0.5f * (s.y - t.x));
+    xmq = make_float2(0.5f * (s.x - t.y), -0.5f * (s.y + t.x));
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -266,7 +298,6 @@ __global__ void __launch_bounds__(kNTA, 1)
     int64_t item = blockIdx.x;
     if (item < n_items) cp_async16(sp + 4 * threadIdx.x, src_of(item) + threadIdx.x);
     cp_async_commit();
-    const float2 wbase = conjf2(__ldg(tw.w32768 + threadIdx.x));  // e^{+2 pi i tid/32768}
     for (int buf = 0; item < n_items; item += gridDim.x, buf ^= 1) {
         const int64_t next = item + gridDim.x;
         if (next < n_items) cp_async16(sp + (buf ^ 1) * kGroups + 4 * threadIdx.x, src_of(next) + threadIdx.x);
@@ -276,15 +307,25 @@ __global__ void __launch_bounds__(kNTA, 1)
         const uint32_t *cur = sp + buf * kGroups;
         const int64_t pol = item / n_snaps, s = item % n_snaps;
         float2 *dst = reinterpret_cast<float2 *>(out + pol * out_pol_stride + s * kNA);
+        // Hermitian pairing: Z[k], Z[M-k] for k = 0..8192 from X[k], X[M-k];
+        // X[16384] (Nyquist) = 0 and the imaginary part of X[0] are dropped.
+        for (int k = threadIdx.x; k <= kMA / 2; k += kNTA) {
+            float2 a = nib_value(cur, k);
+            float2 b = make_float2(0.f, 0.f);
+            if (k == 0)
+                a.y = 0.f;
+            else
+                b = nib_value(cur, kMA - k);
+            float2 zk, zmk;
+            c2r_pair(a, b, conjf2(__ldg(tw.w32768 + k)), zk, zmk);
+            sm[pad(k)] = zk;
+            if (k != 0 && k != kMA / 2) sm[pad(kMA - k)] = zmk;
+        }
+        __syncthreads();
         auto zin = [&](float2 *v) {
-            const int tid = threadIdx.x;
-            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
-                constexpr int r = decltype(rc)::value;
-                const int k = tid + 512 * r;
-                const float2 a = nib_value(cur, k);
-                const float2 b = k == 0 ? make_float2(0.f, 0.f) : nib_value(cur, kMA - k);  // X[16384] = 0
-                v[r] = c2r_pre(a, b, k, c2r_tw<r>(wbase));
-            });
+            const float2 *src = sm + pad(threadIdx.x);
+#pragma unroll
+            for (int r = 0; r < 32; ++r) v[r] = src[528 * r];
         };
         auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
@@ -315,10 +356,6 @@ __global__ void __launch_bounds__(kNTB, 1)
     load_tabs_a(TA, tw);
     load_tabs_b(TB, tw);
     const int tid = threadIdx.x;
-    // per-thread bases of the pre/post-processing twiddles
-    const float2 wc = conjf2(__ldg(tw.w32768 + tid));
-    const float2 wq = __ldg(tw.w36608 + skip + tid);
-    const float2 wqm = __ldg(tw.w36608 + skip + kMA - tid);
     const int64_t n_items = static_cast<int64_t>(n_chunks) * n_pols;
     for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
         const int pol = static_cast<int>(item / n_chunks);
@@ -326,15 +363,38 @@ __global__ void __launch_bounds__(kNTB, 1)
         __syncthreads();  // tables loaded / previous item's last smem reads done
         const float2 *z = reinterpret_cast<const float2 *>(in + pol * in_pol_stride + c * kNB);
         fft18304_from_global(sm, z, TB);
+        // R2C post-processing in place: X[q], X[M'-q] from Z[q], Z[M'-q];
+        // X[0] and X[18304] (both real) from Z[0], X[18304] in the spare slot.
+        for (int q = tid; q <= kMB / 2; q += kNTB) {
+            if (q == 0) {
+                const float2 z0 = sm[0];
+                sm[0] = make_float2(z0.x + z0.y, 0.f);
+                sm[pad(kMB)] = make_float2(z0.x - z0.y, 0.f);
+            } else {
+                float2 xq, xmq;
+                r2c_pair(sm[pad(q)], sm[pad(kMB - q)], __ldg(tw.w36608 + q), xq, xmq);
+                sm[pad(q)] = xq;
+                if (q != kMB / 2) sm[pad(kMB - q)] = xmq;
+            }
+        }
+        __syncthreads();
+        // C2R pre-processing in place on the window Y[j] = X[skip + j], j = 0..16384:
+        // Z'[j] is stored in the slot of Y[j].
+        for (int j = tid; j <= kMA / 2; j += kNTB) {
+            float2 y = sm[pad(skip + j)], ym = sm[pad(skip + kMA - j)];
+            if (j == 0) {
+                y.y = 0.f;
+                ym.y = 0.f;
+            }
+            float2 zk, zmk;
+            c2r_pair(y, ym, conjf2(__ldg(tw.w32768 + j)), zk, zmk);
+            sm[pad(skip + j)] = zk;
+            if (j != 0 && j != kMA / 2) sm[pad(skip + kMA - j)] = zmk;
+        }
+        __syncthreads();
         auto zin = [&](float2 *v) {
-            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
-                constexpr int r = decltype(rc)::value;
-                const int jj = tid + 512 * r;
-                // e^{-2 pi i q/36608}, q = skip + jj and skip + 16384 - jj
-                const float2 y = r2c_bin(sm, skip + jj, mul_tc<143, 2 * r, false>(wq));
-                const float2 ym = r2c_bin(sm, skip + kMA - jj, mul_tc<143, 2 * r, true>(wqm));
-                v[r] = c2r_pre(y, ym, jj, c2r_tw<r>(wc));
-            });
+#pragma unroll
+            for (int r = 0; r < 32; ++r) v[r] = sm[pad(skip + tid + 512 * r)];
         };
         if constexpr (MODE == 0) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
@@ -430,32 +490,54 @@ __global__ void __launch_bounds__(kNTB, 1)
 // Threshold from the per-chunk partials: Chan's merge in FP64, in chunk order
 // (deterministic).  thr_state: [0..1] effective threshold, [2..3] effective
 // offset, [4..5] own threshold, [6..7] own offset.
+struct Moments {
+    double n, mean, m2;
+};
+
+// Chan et al. pairwise merge of (n, mean, M2).
+__device__ __forceinline__ Moments merge_moments(Moments a, Moments b) {
+    const double n = a.n + b.n;
+    if (n == 0.0) return a;
+    const double delta = b.mean - a.mean;
+    return Moments{n, a.mean + delta * b.n / n, a.m2 + b.m2 + delta * delta * a.n * b.n / n};
+}
+
+// Threshold from the per-chunk partials, FP64, one warp per pol: each lane
+// merges its chunks in order, then a fixed butterfly tree merges the lanes
+// (deterministic).  thr_state: [0..1] effective threshold, [2..3] effective
+// offset, [4..5] own threshold, [6..7] own offset.
 __global__ void k_finalize_thresholds(const double *__restrict__ partials, int n_chunks, int pol1_uses_pol0,
                                       float *__restrict__ thr_state) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    float th[2], off[2];
-    for (int pol = 0; pol < 2; ++pol) {
-        double n = 0.0, mean = 0.0, m2 = 0.0;
-        for (int c = 0; c < n_chunks; ++c) {
+    __shared__ float th_s[2], off_s[2];
+    const int pol = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (pol < 2) {
+        Moments m{0.0, 0.0, 0.0};
+        for (int c = lane; c < n_chunks; c += 32) {
             const double *pp = partials + (static_cast<int64_t>(pol) * n_chunks + c) * 3;
-            const double nb = pp[0], mb = pp[1], m2b = pp[2];
-            const double nn = n + nb;
-            const double delta = mb - mean;
-            mean += delta * nb / nn;
-            m2 += m2b + delta * delta * n * nb / nn;
-            n = nn;
+            m = merge_moments(m, Moments{pp[0], pp[1], pp[2]});
         }
-        th[pol] = static_cast<float>(sqrt(m2 / (n - 1.0)));
-        off[pol] = static_cast<float>(mean);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            Moments other{__shfl_xor_sync(0xffffffffu, m.n, o), __shfl_xor_sync(0xffffffffu, m.mean, o),
+                          __shfl_xor_sync(0xffffffffu, m.m2, o)};
+            m = (lane & o) ? merge_moments(other, m) : merge_moments(m, other);
+        }
+        if (lane == 0) {
+            th_s[pol] = static_cast<float>(sqrt(m.m2 / (m.n - 1.0)));
+            off_s[pol] = static_cast<float>(m.mean);
+        }
     }
-    thr_state[4] = th[0];
-    thr_state[5] = th[1];
-    thr_state[6] = off[0];
-    thr_state[7] = off[1];
-    thr_state[0] = th[0];
-    thr_state[1] = pol1_uses_pol0 ? th[0] : th[1];
-    thr_state[2] = off[0];
-    thr_state[3] = pol1_uses_pol0 ? off[0] : off[1];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        thr_state[4] = th_s[0];
+        thr_state[5] = th_s[1];
+        thr_state[6] = off_s[0];
+        thr_state[7] = off_s[1];
+        thr_state[0] = th_s[0];
+        thr_state[1] = pol1_uses_pol0 ? th_s[0] : th_s[1];
+        thr_state[2] = off_s[0];
+        thr_state[3] = pol1_uses_pol0 ? off_s[0] : off_s[1];
+    }
 }
 
 // quantize2bit over float chunks: each thread packs 16 samples into one word.
@@ -619,7 +701,7 @@ cudaError_t launch_r2dbe_c2r(const void *in, int64_t n_chunks, int skip, float *
 
 cudaError_t launch_finalize_thresholds(const double *partials, int n_chunks, int pol1_uses_pol0, float *thr_state,
                                        cudaStream_t st) {
-    k_finalize_thresholds<<<1, 32, 0, st>>>(partials, n_chunks, pol1_uses_pol0, thr_state);
+    k_finalize_thresholds<<<1, 64, 0, st>>>(partials, n_chunks, pol1_uses_pol0, thr_state);
     return cudaGetLastError();
 }
 
