@@ -327,6 +327,7 @@ class StreamState:
         self.threshold = [0.0, 0.0]
         self.offset = [0.0, 0.0]
         self.carry = [np.zeros((0, BENG_CHANNELS), np.complex128) for _ in range(2)]
+        self.raw = [None, None]   # Mar-2015 format: last unpacked B-frame, held for the next call
 
 
 def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
@@ -351,6 +352,13 @@ def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
     spec_dtype = np.complex64 if precision == "f32" else np.complex128
     outs, floats = [], []
     for pol, beng in enumerate((beng0, beng1)):
+        if channel_map == "mar2015":
+            # Mar-2015 SDBE: output frame f needs input frames f and f+1
+            # (reorder.py:284-293), so the last input frame waits for the next call.
+            if state.raw[pol] is not None:
+                beng = np.concatenate([state.raw[pol], beng], axis=0)
+            state.raw[pol] = beng[-1:].copy() if beng.shape[0] else state.raw[pol]
+            beng = reorder_mar2015(beng) if beng.shape[0] >= 2 else beng[:0]
         spec = beng_to_complex(beng.reshape(-1, BENG_CHANNELS_, 2), spec_dtype)
         spec = np.concatenate([state.carry[pol].astype(spec_dtype), spec], axis=0)
         n_batches = spec.shape[0] // BATCH_SNAPSHOTS

@@ -51,6 +51,11 @@ struct sdbe_resampler {
     cudaEvent_t wave_ev = nullptr;
     bool thresholds_set = false;
     int64_t carry = 0;
+    // Mar-2015 format: unpacked frames land here first; the last one is held
+    // for the next call because output frame f needs input frame f+1.
+    uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]
+    int64_t raw_pol_stride = 0;   // words
+    int raw_carry = 0;            // 0 or 1 frame held
     uint32_t secs = 0, df = 0, ref_epoch = 0, station = (uint32_t('S') << 8) | uint32_t('m'), bdc = 0, rx = 0;
     uint64_t psn = 1;
     std::string err;
@@ -127,6 +132,7 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->fout);
     cudaFree(h->partials);
     cudaFree(h->thr);
+    cudaFree(h->raw);
     for (auto &sg : h->stage) {
         cudaFree(sg.pkt);
         cudaFree(sg.out);
@@ -144,8 +150,15 @@ cudaStream_t pick(sdbe_resampler *h, void *stream) {
     return stream ? static_cast<cudaStream_t>(stream) : h->stream;
 }
 
+// B-frames of spectra a call adds to the snapshot stream.
+int64_t frames_out(const sdbe_resampler *h, int32_t n_frames) {
+    if (h->cfg.channel_map != SDBE_MAP_MAR2015) return n_frames;
+    const int64_t n_in = h->raw_carry + static_cast<int64_t>(n_frames);
+    return n_in >= 2 ? n_in - 1 : 0;
+}
+
 int64_t batches_for(const sdbe_resampler *h, int32_t n_frames) {
-    return (h->carry + static_cast<int64_t>(n_frames) * kSnapsPerFrame) / kBatchSnaps;
+    return (h->carry + frames_out(h, n_frames) * kSnapsPerFrame) / kBatchSnaps;
 }
 
 int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what) {
@@ -217,6 +230,10 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
               cudaMalloc(&h->fout, 2 * static_cast<size_t>(kChunks) * kNC * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&h->partials, 2 * kChunks * 3 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&h->thr, 8 * sizeof(float)) == cudaSuccess;
+    if (ok && cfg->channel_map == SDBE_MAP_MAR2015) {
+        h->raw_pol_stride = (static_cast<int64_t>(cfg->max_frames) + 1) * kSnapsPerFrame * kGroups;
+        ok = cudaMalloc(&h->raw, 2 * h->raw_pol_stride * sizeof(uint32_t)) == cudaSuccess;
+    }
     if (!ok) return bail(SDBE_ERR_NOMEM, "device buffer allocation failed");
     if (cudaMemset(h->thr, 0, 8 * sizeof(float)) != cudaSuccess) return bail(SDBE_ERR_CUDA, "memset");
     *out = h;
@@ -298,14 +315,38 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     };
 
     const int map = h->cfg.channel_map;
+    const bool mar = map == SDBE_MAP_MAR2015;
+    const int64_t n_frames_out = frames_out(h, n_frames);
     if (n_frames > 0) {
+        // Mar-2015: unpack after the held frame in `raw`; otherwise straight
+        // into the snapshot stream after the carried snapshots.
+        uint32_t *dst = mar ? h->raw : h->spec;
+        const int64_t dst_stride = mar ? h->raw_pol_stride : h->spec_pol_stride;
+        const int64_t snap0 = mar ? static_cast<int64_t>(h->raw_carry) * kSnapsPerFrame : h->carry;
         SDBE_CK(h, cudaMemsetAsync(h->bitmap, 0, static_cast<size_t>(n_frames) * 256, st));
         SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
-        SDBE_CK(h, launch_unpack(src, n_packets, b_zero, n_frames, map, h->spec, h->spec_pol_stride, h->carry,
-                                 h->bitmap, h->counts, h->counts + h->cfg.max_frames, st));
+        SDBE_CK(h, launch_unpack(src, n_packets, b_zero, n_frames, map, dst, dst_stride, snap0, h->bitmap, h->counts,
+                                 h->counts + h->cfg.max_frames, st));
         if (host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
-        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, h->spec, h->spec_pol_stride, h->carry, st));
+        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, dst, dst_stride, snap0, st));
         h->launches += n_packets > 0 ? 2 : 1;
+        if (mar) {
+            const int n_in = h->raw_carry + n_frames;
+            for (int pol = 0; pol < 2 && n_in >= 2; ++pol) {
+                SDBE_CK(h, launch_reorder_mar2015(h->raw + pol * h->raw_pol_stride, n_in,
+                                                  h->spec + pol * h->spec_pol_stride + h->carry * kGroups, st));
+                h->launches += 1;
+            }
+            if (n_in >= 2) {  // hold the newest frame
+                for (int pol = 0; pol < 2; ++pol) {
+                    uint32_t *base = h->raw + pol * h->raw_pol_stride;
+                    SDBE_CK(h, cudaMemcpyAsync(base, base + static_cast<int64_t>(n_in - 1) * kSnapsPerFrame * kGroups,
+                                               static_cast<size_t>(kSnapsPerFrame) * kGroups * sizeof(uint32_t),
+                                               cudaMemcpyDeviceToDevice, st));
+                }
+            }
+            h->raw_carry = 1;
+        }
     }
     if (framed && n_out > 0) {  // headers first, so every shipped wave is complete
         SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
@@ -355,7 +396,7 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         if (int rc = ship(b * kChunks, (b + nb) * kChunks)) return rc;
     }
     if (host_out) SDBE_CK(h, cudaEventRecord(sg.out_free, h->copy_out));
-    const int64_t total = h->carry + static_cast<int64_t>(n_frames) * kSnapsPerFrame;
+    const int64_t total = h->carry + n_frames_out * kSnapsPerFrame;
     const int64_t new_carry = total - n_batches * kBatchSnaps;
     if (n_batches > 0 && new_carry > 0) {
         for (int pol = 0; pol < 2; ++pol) {
@@ -449,6 +490,7 @@ int sdbe_reset(sdbe_resampler *h) {
     if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
     h->thresholds_set = false;
     h->carry = 0;
+    h->raw_carry = 0;
     return SDBE_OK;
 }
 

@@ -249,3 +249,26 @@ def test_async_pipelined_calls_match_sync(S, cfg1):
         rs.sync()
     for k in range(2):
         np.testing.assert_array_equal(np.asarray(outs[k]).reshape(refs[k].shape), refs[k])
+
+
+def test_mar2015_format_stream_vs_oracle(S):
+    """Mar-2015 channel map + cross-frame snapshot reorder, streamed over two calls."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300._native import MAP_MAR2015
+
+    spec = S.config1(stream=4)
+    spec.n_frames = 5
+    spec.channel_map = 1
+    p = S.generate(spec)
+    st = O.StreamState()
+    with Resampler(trim_mhz=150, max_frames=3, channel_map=MAP_MAR2015) as rs:
+        outs, refs = [], []
+        for lo, nf in ((0, 3), (3, 2)):
+            q = p[lo * 2048:(lo + nf) * 2048]
+            o, res = rs.process(q, nf, spec.b_start + lo)
+            outs.append(o)
+            refs.append(O.process_group(q, spec.b_start + lo, nf, 150, state=st, channel_map="mar2015"))
+    got, ref = np.concatenate(outs, axis=1), np.concatenate(refs, axis=1)
+    assert got.shape == ref.shape == (2, 3 * 128, 8192)
+    for pol in range(2):
+        assert _agreement(got[pol], ref[pol]) >= AGREE_MIN

@@ -1,0 +1,65 @@
+"""Precision of the FP32 path against the FP64 oracle (the precision-form config).
+
+Measures, on sampled 143-snapshot batches of the 3-tone stream, the relative
+RMS error of the resampled series before requantization and the 2-bit code
+agreement (GPU: FP32 series + FP32 compare with its own FP64-accumulated
+thresholds; oracle: FP64 series, FP64 thresholds).  Results are written to
+``gpurun_out/precision_fp32.json`` when that directory exists.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_util import dev, empty, host, ptr, rel_rms, zeros
+from oracle import sdbe_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 3e-6        # FP32 chain of three transforms vs FP64, relative RMS
+AGREE_MIN = 0.999
+
+
+def test_fp32_path_rms_and_code_agreement():
+    import __graft_entry__ as g
+
+    g.build()
+    from sdbe_gb300 import Resampler, synth
+    from sdbe_gb300 import _native as N
+
+    spec = synth.config2(n_frames=4)
+    p = synth.generate(spec)
+    nf = 4
+    snaps = nf * 128
+    words = empty(2 * snaps * 2048 * 4, "int32")
+    bitmap, counts, rej = zeros(nf * 256), zeros(nf * 4, "int32"), zeros(4, "int32")
+    lib = N.lib()
+    N.check(lib.sdbe_unpack(ptr(dev(p)), p.shape[0], spec.b_start, nf, 0, ptr(words), snaps * 2048, 0, ptr(bitmap),
+                            ptr(counts), ptr(rej), None))
+    beng = O.vdif_to_beng(p, spec.b_start, nf)
+    results = []
+    with Resampler(trim_mhz=150, max_frames=nf) as rs:
+        for b in (0, 2):
+            ts = empty(143 * 32768 * 4, "float32")
+            y = empty(128 * 32768 * 4, "float32")
+            src = int(words.data_ptr()) + b * 143 * 2048 * 4   # pol 0
+            N.check(lib.sdbe_swarm_c2r(rs.handle, src, 143, ptr(ts), None), rs.handle)
+            N.check(lib.sdbe_resample_chunks(rs.handle, ptr(ts), 128, ptr(y), None), rs.handle)
+            got = host(y).reshape(128, 32768).astype(np.float64)
+            sp = O.beng_to_complex(beng[0].reshape(-1, 16384, 2))[b * 143:(b + 1) * 143]
+            ref = O.r2dbe_c2r(O.swarm_r2c(O.swarm_c2r(sp).reshape(-1)), rs.skip_chan)
+            err = rel_rms(got, ref)
+            off_g, th_g = O.summary_stats(got)
+            off_r, th_r = O.summary_stats(ref)
+            cg = O.quantize2bit_codes(got.astype(np.float32), th_g, off_g, np.float32)
+            cr = O.quantize2bit_codes(ref, th_r, off_r)
+            agree = float(np.mean(cg == cr))
+            results.append({"batch": b, "rel_rms": err, "max_abs_rel": float(np.abs(got - ref).max() / ref.std()),
+                            "code_agreement": agree, "threshold_rel_diff": abs(th_g - th_r) / th_r})
+    for r in results:
+        assert r["rel_rms"] < RMS_TOL, r
+        assert r["code_agreement"] >= AGREE_MIN, r
+    if os.path.isdir("gpurun_out"):
+        with open(os.path.join("gpurun_out", "precision_fp32.json"), "w") as f:
+            json.dump({"path": "fp32", "samples_per_batch": 128 * 32768, "batches": results}, f, indent=1)

@@ -118,3 +118,17 @@ def test_streams_shard_over_ranks_gloo(tmp_path):
     r1 = np.load(tmp_path / "r1.npy")
     assert r0[1] == r1[1] == 7
     assert sorted(list(r0[2:]) + list(r1[2:])) == list(range(7))
+
+
+def test_oracle_mar2015_stream_split_equals_single(synth):
+    """Mar-2015 mode holds one frame back; splitting the stream changes nothing."""
+    spec = synth.config1()
+    spec.n_frames = 5
+    spec.channel_map = 1
+    p = synth.generate(spec)
+    one = O.process_group(p, spec.b_start, 5, 150, channel_map="mar2015")
+    st = O.StreamState()
+    a = O.process_group(p[:3 * 2048], spec.b_start, 3, 150, state=st, channel_map="mar2015")
+    b = O.process_group(p[3 * 2048:], spec.b_start + 3, 2, 150, state=st, channel_map="mar2015")
+    assert one.shape[1] == (4 * 128 // 143) * 128
+    assert np.array_equal(np.concatenate([a, b], axis=1), one)
