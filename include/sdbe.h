@@ -66,6 +66,8 @@ extern "C" {
 #define SDBE_SYNC 8u               /* synchronize the stream before returning            */
 #define SDBE_ASYNC 16u             /* with host buffers: return without waiting; the
                                       buffers must stay valid until sdbe_sync          */
+#define SDBE_OUT_ALIGNED 32u       /* time-aligned 8224-B VDIF frames (implies FRAMED):
+                                      the output thread's skip + leftover carry         */
 
 typedef struct sdbe_config {
     int32_t device;            /* CUDA device ordinal (resampler->deviceId, .cu:147)        */
@@ -143,6 +145,27 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
 /* State of the stream.  get/set synchronize the device first (work may be in
  * flight on any stream).  set: thresholds/offsets (marked set if any
  * threshold != 0), header counters; clears the carry when carry_snapshots == 0. */
+/* Output time alignment (vdif_out_net_thread.c:199-317, template from
+ * fill_vdif_header_template, vdif_in_databuf.c:193-220).  A template holds
+ * the first output second, data frame and the picoseconds the stream starts
+ * early.  sdbe_align_start arms it for the next SDBE_OUT_ALIGNED call, which
+ * starts on the next second boundary if its block would cross one, skips
+ * floor(floor((ps + 3715791) * 4096e6 / 1e12) / 16) payload words and sets psn
+ * to 1.  Every aligned call frames whole 8192-B packets of the word stream
+ * (previous call's leftover words, then this call's) and carries the rest, so
+ * its packet count is floor((leftover + words) / 2048) per pol
+ * (sdbe_result.n_out_packets). */
+typedef struct sdbe_time_template {
+    uint32_t secs_inre;
+    uint32_t df_num_insec;
+    uint64_t ps_early;         /* edh_psn field of the reference template */
+    uint32_t ref_epoch;
+    uint32_t reserved;
+} sdbe_time_template;
+/* Template from the first B-engine timestamp (t0_sec, t0_clk at 286 MHz). */
+int sdbe_header_template(int32_t t0_sec, int32_t t0_clk, uint32_t ref_epoch, sdbe_time_template *out);
+int sdbe_align_start(sdbe_resampler *h, const sdbe_time_template *t);
+
 /* Wait for all work the handle issued (its streams and the last stream passed
  * to sdbe_process). */
 int sdbe_sync(sdbe_resampler *h);

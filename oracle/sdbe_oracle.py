@@ -423,3 +423,99 @@ def frame_vdif(payloads, pol: int, **hdr):
     payloads = np.asarray(payloads, dtype=np.uint8).reshape(-1, OUT_PKT_DATA_BYTES)
     words = vdif_out_header_words(payloads.shape[0], pol, **hdr)
     return np.concatenate([words.view(np.uint8).reshape(-1, 32), payloads], axis=1)
+
+
+# ------------------------------------------------------ time alignment ------
+SWARM_CLK_PER_SEC = 286000000          # beng_reform.c:25
+SWARM_BFRAME_CLK = 262144              # beng_reform.c:27
+SWARM_ZERO_DELAY_OFFSET_PICOSECONDS = 3715791   # vdif_out_databuf.h:11
+OUT_WORDS_PER_PKT = OUT_PKT_DATA_BYTES // 4
+
+
+def beng_timestamp_increment(sec, clk):
+    """One B-frame later (``beng_reform.c:56-62``; wraps only when clk > 286e6)."""
+    clk += SWARM_BFRAME_CLK
+    if clk > SWARM_CLK_PER_SEC:
+        sec += 1
+        clk = clk % SWARM_CLK_PER_SEC
+    return sec, clk
+
+
+def beng_timestamp_decrement(sec, clk):
+    """One B-frame earlier (``beng_reform.c:64-70``)."""
+    clk -= SWARM_BFRAME_CLK
+    if clk < 0:
+        sec -= 1
+        clk = clk + SWARM_CLK_PER_SEC
+    return sec, clk
+
+
+def header_template(t0_sec, t0_clk, ref_epoch=0):
+    """Output timestamp template from the first B-engine timestamp.
+
+    ``get_beng_t0`` moves T0 one B-frame earlier (SWARM_TIMESTAMP_OFF_BY_BENG =
+    -1, ``beng_reform.c:112-126``); ``fill_vdif_header_template`` moves it one
+    frame later again and sets secs, the next whole 8-us data frame and the
+    picoseconds between the two (``vdif_in_databuf.c:193-220``).  Returns
+    ``(secs, df, ps_early, ref_epoch)``.
+    """
+    s, c = beng_timestamp_decrement(t0_sec, t0_clk)
+    s, c = beng_timestamp_increment(s, c)
+    frame_full = VDIF_OUT_FRAMES_PER_SECOND * 1.0 * (float(c) / float(SWARM_CLK_PER_SEC))
+    frame_ceil = float(np.ceil(frame_full))
+    frac = frame_ceil - frame_full
+    return s, int(frame_ceil), int(np.floor(frac * (1e12 / VDIF_OUT_FRAMES_PER_SECOND))), ref_epoch
+
+
+class AlignState:
+    """Output-thread state (``vdif_out_net_thread.c:72-80,199-317``)."""
+
+    def __init__(self, template=None, station=(ord("S") << 8) | ord("m"), bdc=0, rx=0):
+        self.pending = template is not None
+        self.template = template
+        self.leftover = [np.zeros(0, np.uint32), np.zeros(0, np.uint32)]
+        self.secs = self.df = self.psn = self.ref_epoch = 0
+        self.station, self.bdc, self.rx = station, bdc, rx
+
+
+def align_frames(payload, st: AlignState):
+    """Time-aligned 8224-B frames from one block of payloads ``[2, n, 8192]``.
+
+    On the first block after a template: start on the next second boundary
+    when the block would cross one (skip frames), skip
+    ``floor(floor((ps + 3715791) * 4096e6/1e12) / 16)`` 32-bit words, psn from 1
+    (``:206-237``).  Every block: the aligned word stream is the previous
+    block's leftover words followed by this block's words; whole 8192-B
+    packets are framed with secs/df/psn advancing per packet and the rest is
+    carried (``:251-317``).  The reference's first block reads its skipped
+    frames past the end of the block; here the skip is taken from the front.
+    """
+    words = [np.ascontiguousarray(payload[p]).reshape(-1).view("<u4") for p in range(2)]
+    n_words = words[0].size
+    skip = 0
+    if st.pending:
+        secs, df, ps, ref_epoch = st.template
+        skip_frames = 0
+        n_usable = n_words // OUT_WORDS_PER_PKT
+        if df > VDIF_OUT_FRAMES_PER_SECOND - n_usable:
+            skip_frames = VDIF_OUT_FRAMES_PER_SECOND - df
+            df = 0
+            secs += 1
+        skip_ps = ps + SWARM_ZERO_DELAY_OFFSET_PICOSECONDS
+        skip_samples = int(np.floor(float(skip_ps) * R2DBE_RATE / 1e12))
+        skip = int(np.floor(skip_samples / (8.0 / 2) / 4)) + skip_frames * OUT_WORDS_PER_PKT
+        st.secs, st.df, st.ref_epoch, st.psn = secs, df, ref_epoch, 1
+        st.pending = False
+    streams = [np.concatenate([st.leftover[p], words[p][skip:]]) for p in range(2)]
+    n_pkts = streams[0].size // OUT_WORDS_PER_PKT
+    frames = []
+    for p in range(2):
+        body = streams[p][:n_pkts * OUT_WORDS_PER_PKT].view(np.uint8).reshape(n_pkts, OUT_PKT_DATA_BYTES)
+        st.leftover[p] = streams[p][n_pkts * OUT_WORDS_PER_PKT:].copy()
+        frames.append(frame_vdif(body, p, secs=st.secs, df=st.df, psn=st.psn, ref_epoch=st.ref_epoch,
+                                 station=st.station, bdc_sideband=st.bdc, rx_sideband=st.rx))
+    dfs = st.df + n_pkts
+    st.secs += dfs // VDIF_OUT_FRAMES_PER_SECOND
+    st.df = dfs % VDIF_OUT_FRAMES_PER_SECOND
+    st.psn += n_pkts
+    return np.stack(frames)

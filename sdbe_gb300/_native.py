@@ -26,7 +26,7 @@ FRAMES_PER_GROUP = 143
 SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED = 0, 1
 MAP_APHIDS, MAP_MAR2015 = 0, 1
-IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC = 1, 2, 4, 8, 16
+IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED = 1, 2, 4, 8, 16, 32
 NOALLOC_MAX_SAMPLES = 134217728
 
 
@@ -54,6 +54,11 @@ class Profile(C.Structure):
                 ("stage_bc_ms", C.c_double), ("reserved", C.c_int64 * 4)]
 
 
+class TimeTemplate(C.Structure):
+    _fields_ = [("secs_inre", C.c_uint32), ("df_num_insec", C.c_uint32), ("ps_early", C.c_uint64),
+                ("ref_epoch", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("sigma", C.c_double), ("level", C.c_double), ("n_tones", C.c_int32),
                 ("tone_channel", C.c_int32 * 8), ("tone_amp", C.c_double * 8), ("tone_phase", C.c_double * 8),
@@ -73,6 +78,8 @@ SIGNATURES = {
     "sdbe_set_state": (C.c_int, [vp, C.POINTER(State)]),
     "sdbe_reset": (C.c_int, [vp]),
     "sdbe_sync": (C.c_int, [vp]),
+    "sdbe_header_template": (C.c_int, [i32, i32, u32, C.POINTER(TimeTemplate)]),
+    "sdbe_align_start": (C.c_int, [vp, C.POINTER(TimeTemplate)]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

@@ -49,6 +49,15 @@ struct sdbe_resampler {
     Stage stage[2];
     int stage_idx = 0;
     cudaEvent_t wave_ev = nullptr;
+    // output time alignment (SDBE_OUT_ALIGNED)
+    bool align_pending = false;
+    sdbe_time_template tmpl{};
+    int64_t skip_pending = 0;      // payload words still to drop
+    uint32_t *left[2] = {nullptr, nullptr};  // [2 pols][2048] leftover words, double-buffered
+    int left_idx = 0;
+    int64_t n_left = 0;
+    uint8_t *pay = nullptr;        // plain payload stream before alignment
+    int64_t pay_bytes = 0;
     bool thresholds_set = false;
     int64_t carry = 0;
     // Mar-2015 format: unpacked frames land here first; the last one is held
@@ -133,6 +142,9 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->partials);
     cudaFree(h->thr);
     cudaFree(h->raw);
+    cudaFree(h->left[0]);
+    cudaFree(h->left[1]);
+    cudaFree(h->pay);
     for (auto &sg : h->stage) {
         cudaFree(sg.pkt);
         cudaFree(sg.out);
@@ -230,6 +242,8 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
               cudaMalloc(&h->fout, 2 * static_cast<size_t>(kChunks) * kNC * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&h->partials, 2 * kChunks * 3 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&h->thr, 8 * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMalloc(&h->left[0], 2 * kOutWords * sizeof(uint32_t)) == cudaSuccess &&
+         cudaMalloc(&h->left[1], 2 * kOutWords * sizeof(uint32_t)) == cudaSuccess;
     if (ok && cfg->channel_map == SDBE_MAP_MAR2015) {
         h->raw_pol_stride = (static_cast<int64_t>(cfg->max_frames) + 1) * kSnapsPerFrame * kGroups;
         ok = cudaMalloc(&h->raw, 2 * h->raw_pol_stride * sizeof(uint32_t)) == cudaSuccess;
@@ -251,8 +265,10 @@ int sdbe_destroy(sdbe_resampler *h) {
 
 int64_t sdbe_output_bytes(const sdbe_resampler *h, int32_t n_frames, uint32_t flags) {
     if (!h || n_frames < 0) return -1;
+    const int64_t n_out = batches_for(h, n_frames) * kChunks;
+    if (flags & SDBE_OUT_ALIGNED) return 2 * ((h->n_left + n_out * kOutWords) / kOutWords) * kOutPkt;
     const int64_t pkt = (flags & SDBE_OUT_FRAMED) ? kOutPkt : kOutPktData;
-    return 2 * batches_for(h, n_frames) * kChunks * pkt;
+    return 2 * n_out * pkt;
 }
 
 int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames, uint64_t b_zero,
@@ -264,9 +280,45 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     DeviceGuard g(h->cfg.device);
     if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
     cudaStream_t st = pick(h, stream);
-    const bool framed = (flags & SDBE_OUT_FRAMED) != 0;
+    const bool aligned = (flags & SDBE_OUT_ALIGNED) != 0;
+    const bool framed = (flags & (SDBE_OUT_FRAMED | SDBE_OUT_ALIGNED)) != 0;
     const int64_t n_batches = batches_for(h, n_frames);
-    const int64_t n_out = n_batches * kChunks;
+    const int64_t n_pay = n_batches * kChunks;  // payload packets per pol the FFTs produce
+    // Time alignment (vdif_out_net_thread.c:199-317): first block after a
+    // template starts on the next second boundary if it would cross one and
+    // skips the sub-packet offset; every block frames whole packets of
+    // [leftover | payload] and carries the rest.
+    uint32_t a_secs = h->secs, a_df = h->df;
+    uint64_t a_psn = h->psn;
+    uint32_t a_epoch = h->ref_epoch;
+    int64_t a_skip_total = h->skip_pending, a_skip = 0, a_new_left = 0, a_skip_after = 0;
+    int64_t n_out = n_pay;
+    if (aligned) {
+        if (h->align_pending) {
+            a_secs = h->tmpl.secs_inre;
+            a_df = h->tmpl.df_num_insec;
+            int64_t skip_frames = 0;
+            if (static_cast<int64_t>(a_df) > 125000 - n_pay) {
+                skip_frames = 125000 - static_cast<int64_t>(a_df);
+                a_df = 0;
+                a_secs += 1;
+            }
+            const double skip_ps = static_cast<double>(h->tmpl.ps_early + 3715791ull);
+            const double skip_samples = std::floor(skip_ps * 4096e6 / 1e12);
+            a_skip_total += static_cast<int64_t>(std::floor(skip_samples / (8.0 / 2.0) / 4.0)) + skip_frames * kOutWords;
+            a_psn = 1;
+            a_epoch = h->tmpl.ref_epoch;
+        }
+        const int64_t stream_len = h->n_left + n_pay * kOutWords - a_skip_total;
+        if (stream_len < 0) {
+            n_out = 0;
+            a_skip_after = -stream_len;
+        } else {
+            a_skip = a_skip_total;
+            n_out = stream_len / kOutWords;
+            a_new_left = stream_len - n_out * kOutWords;
+        }
+    }
     const int64_t pkt_stride = framed ? kOutPkt : kOutPktData;
     const int64_t payload_off = framed ? 32 : 0;
     const int64_t out_pol_stride = n_out * pkt_stride;
@@ -301,6 +353,18 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         dev_out = sg.out;
     } else if (n_out > 0 && (reinterpret_cast<uintptr_t>(out) & 15u)) {
         return fail(h, SDBE_ERR_ARG, "device output buffer must be 16-byte aligned");
+    }
+    // Where the FFT waves write: the output itself, or the plain payload
+    // stream that the alignment step frames afterwards.
+    uint8_t *tgt = dev_out;
+    int64_t tgt_pol_stride = out_pol_stride, tgt_pkt_stride = pkt_stride, tgt_off = payload_off;
+    if (aligned && n_pay > 0) {
+        int rc = grow(h, &h->pay, &h->pay_bytes, 2 * n_pay * kOutPktData, "payload stream");
+        if (rc) return rc;
+        tgt = h->pay;
+        tgt_pol_stride = n_pay * kOutPktData;
+        tgt_pkt_stride = kOutPktData;
+        tgt_off = 0;
     }
     // Payload packets [lo, hi) of both pols are final: send them to the host
     // on the copy stream while the next wave computes.
@@ -348,7 +412,7 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
             h->raw_carry = 1;
         }
     }
-    if (framed && n_out > 0) {  // headers first, so every shipped wave is complete
+    if (framed && !aligned && n_out > 0) {  // headers first, so every shipped wave is complete
         SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
                                        h->station, h->bdc, h->rx, st));
         h->launches += 1;
@@ -368,12 +432,13 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         o.partials = h->partials;
         SDBE_CK(h, launch_resample(1, h->ts, h->ts_pol_stride, h->skip, kChunks, 2, o, h->tw, st));
         SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
-        SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, dev_out,
-                                          out_pol_stride, pkt_stride, payload_off, 0, st));
+        SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, tgt,
+                                          tgt_pol_stride, tgt_pkt_stride, tgt_off, 0, st));
         h->thresholds_set = true;
         h->launches += 4;
         b = 1;
-        if (int rc = ship(0, kChunks)) return rc;
+        if (!aligned)
+            if (int rc = ship(0, kChunks)) return rc;
     }
     for (; b < n_batches; b += h->wave) {
         const int64_t nb = std::min<int64_t>(h->wave, n_batches - b);
@@ -384,16 +449,46 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         SDBE_CK(h, timed_end(h, slot, st));
         SDBE_CK(h, timed_begin(h, 1, 2 * nb * kChunks, st, &slot));
         ResampleOut o{};
-        o.out = dev_out;
-        o.out_pol_stride = out_pol_stride;
-        o.pkt_stride = pkt_stride;
-        o.payload_off = payload_off;
+        o.out = tgt;
+        o.out_pol_stride = tgt_pol_stride;
+        o.pkt_stride = tgt_pkt_stride;
+        o.payload_off = tgt_off;
         o.pkt0 = b * kChunks;
         o.thr = h->thr;
         SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
         SDBE_CK(h, timed_end(h, slot, st));
         h->launches += 2;
-        if (int rc = ship(b * kChunks, (b + nb) * kChunks)) return rc;
+        if (!aligned)
+            if (int rc = ship(b * kChunks, (b + nb) * kChunks)) return rc;
+    }
+    if (aligned) {
+        const uint32_t *pay_w = reinterpret_cast<const uint32_t *>(h->pay);
+        const int64_t pay_ws = n_pay * kOutWords;
+        uint32_t *cur = h->left[h->left_idx], *nxt = h->left[h->left_idx ^ 1];
+        if (n_out > 0) {
+            SDBE_CK(h, launch_align_frames(pay_w, pay_ws, cur, kOutWords, h->n_left, a_skip, n_out, dev_out,
+                                           out_pol_stride, st));
+            SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, a_secs, a_df, a_psn, a_epoch, h->station,
+                                           h->bdc, h->rx, st));
+            h->launches += 2;
+        }
+        if (a_skip_after == 0) {
+            SDBE_CK(h, launch_save_leftover(pay_w, pay_ws, cur, kOutWords, h->n_left, a_skip, n_out * kOutWords,
+                                            a_new_left, nxt, st));
+            h->launches += a_new_left > 0 ? 1 : 0;
+            h->left_idx ^= 1;
+            h->n_left = a_new_left;
+        } else {
+            h->n_left = 0;
+        }
+        h->skip_pending = a_skip_after;
+        h->align_pending = false;
+        const uint64_t dfs = static_cast<uint64_t>(a_df) + static_cast<uint64_t>(n_out);
+        h->secs = a_secs + static_cast<uint32_t>(dfs / 125000u);
+        h->df = static_cast<uint32_t>(dfs % 125000u);
+        h->psn = a_psn + static_cast<uint64_t>(n_out);
+        h->ref_epoch = a_epoch;
+        if (int rc = ship(0, n_out)) return rc;
     }
     if (host_out) SDBE_CK(h, cudaEventRecord(sg.out_free, h->copy_out));
     const int64_t total = h->carry + n_frames_out * kSnapsPerFrame;
@@ -428,6 +523,42 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         result->frames_incomplete = incomplete;
         result->carry_snapshots = h->carry;
     }
+    return SDBE_OK;
+}
+
+int sdbe_header_template(int32_t t0_sec, int32_t t0_clk, uint32_t ref_epoch, sdbe_time_template *out) {
+    if (!out) return fail(nullptr, SDBE_ERR_ARG, "null argument");
+    constexpr int32_t kClkPerSec = 286000000, kBframeClk = 262144;  // beng_reform.c:25-27
+    // get_beng_t0: one B-frame earlier (beng_reform.c:112-126)
+    int32_t sec = t0_sec, clk = t0_clk - kBframeClk;
+    if (clk < 0) {
+        sec -= 1;
+        clk += kClkPerSec;
+    }
+    // fill_vdif_header_template: one B-frame later (beng_reform.c:56-62)
+    clk += kBframeClk;
+    if (clk > kClkPerSec) {
+        sec += 1;
+        clk %= kClkPerSec;
+    }
+    const double frame_full = (125000 * 1.0) * (static_cast<double>(clk) / static_cast<double>(kClkPerSec));
+    const double frame_ceil = std::ceil(frame_full);
+    const double frac = frame_ceil - frame_full;
+    out->secs_inre = static_cast<uint32_t>(sec);
+    out->df_num_insec = static_cast<uint32_t>(frame_ceil);
+    out->ps_early = static_cast<uint64_t>(std::floor(frac * (1e12 / 125000)));
+    out->ref_epoch = ref_epoch;
+    out->reserved = 0;
+    return SDBE_OK;
+}
+
+int sdbe_align_start(sdbe_resampler *h, const sdbe_time_template *t) {
+    if (!h || !t) return fail(h, SDBE_ERR_ARG, "null argument");
+    if (t->df_num_insec > 125000u) return fail(h, SDBE_ERR_ARG, "df_num_insec must be <= 125000");
+    h->tmpl = *t;
+    h->align_pending = true;
+    h->skip_pending = 0;
+    h->n_left = 0;
     return SDBE_OK;
 }
 
@@ -491,6 +622,8 @@ int sdbe_reset(sdbe_resampler *h) {
     h->thresholds_set = false;
     h->carry = 0;
     h->raw_carry = 0;
+    h->n_left = 0;
+    h->skip_pending = 0;
     return SDBE_OK;
 }
 

@@ -36,6 +36,58 @@ __global__ void k_vdif_headers(uint8_t *__restrict__ frames, int64_t n_pkts, int
     dst[1] = b;
 }
 
+// Time-aligned payloads: output word o of pol p is word o + skip of the
+// stream [left (n_left words) | pay]; 4 words per thread, one 16-B store.
+// grid (ceil(n_pkts*512/256), 2).
+__global__ void k_align_frames(const uint32_t *__restrict__ pay, int64_t pay_pol_stride, const uint32_t *__restrict__ left,
+                               int64_t left_pol_stride, int64_t n_left, int64_t skip, int64_t n_pkts,
+                               uint8_t *__restrict__ frames, int64_t frame_pol_stride) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= n_pkts * (kOutWords / 4)) return;
+    const int pol = blockIdx.y;
+    const int64_t o = 4 * t;
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t s = o + i + skip;
+        w[i] = s < n_left ? left[pol * left_pol_stride + s] : __ldg(pay + pol * pay_pol_stride + (s - n_left));
+    }
+    const int64_t pkt = o / kOutWords, word = o % kOutWords;
+    uint4 *dst = reinterpret_cast<uint4 *>(frames + pol * frame_pol_stride + pkt * kOutPkt + 32 + 4 * word);
+    *dst = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// Words [from, from + count) of the same stream -> the next leftover buffer.
+__global__ void k_save_leftover(const uint32_t *__restrict__ pay, int64_t pay_pol_stride,
+                                const uint32_t *__restrict__ left, int64_t left_pol_stride, int64_t n_left, int64_t skip,
+                                int64_t from, int64_t count, uint32_t *__restrict__ next) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int pol = blockIdx.y;
+    const int64_t s = from + i + skip;
+    next[pol * left_pol_stride + i] = s < n_left ? left[pol * left_pol_stride + s] : pay[pol * pay_pol_stride + (s - n_left)];
+}
+
+cudaError_t launch_align_frames(const uint32_t *pay, int64_t pay_pol_stride, const uint32_t *left, int64_t left_pol_stride,
+                                int64_t n_left, int64_t skip, int64_t n_pkts, void *frames, int64_t frame_pol_stride,
+                                cudaStream_t st) {
+    if (n_pkts <= 0) return cudaSuccess;
+    const int64_t threads = n_pkts * (kOutWords / 4);
+    dim3 grid(static_cast<unsigned>((threads + 255) / 256), 2);
+    k_align_frames<<<grid, 256, 0, st>>>(pay, pay_pol_stride, left, left_pol_stride, n_left, skip, n_pkts,
+                                         static_cast<uint8_t *>(frames), frame_pol_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_save_leftover(const uint32_t *pay, int64_t pay_pol_stride, const uint32_t *left,
+                                 int64_t left_pol_stride, int64_t n_left, int64_t skip, int64_t from, int64_t count,
+                                 uint32_t *next, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    dim3 grid(static_cast<unsigned>((count + 255) / 256), 2);
+    k_save_leftover<<<grid, 256, 0, st>>>(pay, pay_pol_stride, left, left_pol_stride, n_left, skip, from, count, next);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride, uint32_t secs0, uint32_t df0,
                                 uint64_t psn0, uint32_t ref_epoch, uint32_t station, uint32_t bdc, uint32_t rx,
                                 cudaStream_t st) {

@@ -32,6 +32,10 @@ cudaError_t launch_quantize_chunks(const float *, int64_t, int64_t, const float 
 cudaError_t launch_quantize_flat(const float *, uint32_t *, int64_t, float, float, cudaStream_t);
 int stats_partial_blocks(int64_t);
 cudaError_t launch_stats_partial(const float *, int64_t, double *, int, cudaStream_t);
+cudaError_t launch_align_frames(const uint32_t *, int64_t, const uint32_t *, int64_t, int64_t, int64_t, int64_t, void *,
+                                int64_t, cudaStream_t);
+cudaError_t launch_save_leftover(const uint32_t *, int64_t, const uint32_t *, int64_t, int64_t, int64_t, int64_t, int64_t,
+                                 uint32_t *, cudaStream_t);
 cudaError_t launch_vdif_headers(void *, int64_t, int64_t, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t,
                                 uint32_t, cudaStream_t);
 

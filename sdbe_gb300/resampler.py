@@ -105,12 +105,13 @@ class Resampler:
         return self._h
 
     # -- processing ---------------------------------------------------------
-    def output_bytes(self, n_frames: int, framed: bool = False) -> int:
-        return int(self._lib.sdbe_output_bytes(self._h, n_frames, N.OUT_FRAMED if framed else 0))
+    def output_bytes(self, n_frames: int, framed: bool = False, aligned: bool = False) -> int:
+        flags = (N.OUT_FRAMED if framed else 0) | (N.OUT_ALIGNED if aligned else 0)
+        return int(self._lib.sdbe_output_bytes(self._h, n_frames, flags))
 
     def process(self, packets, n_frames: int, b_zero: int, out=None, framed: bool = False,
                 stream=None, n_packets: int | None = None, out_bytes: int | None = None,
-                want_result: bool = True, asynchronous: bool = False):
+                want_result: bool = True, asynchronous: bool = False, aligned: bool = False):
         """Run the stage on ``n_frames`` B-frames starting at counter ``b_zero``.
 
         Returns ``(out, GroupResult | None)``; ``out`` holds the payloads as
@@ -122,7 +123,8 @@ class Resampler:
         if n_packets is None:
             n_packets = int(packets.shape[0]) if hasattr(packets, "shape") else 0
         flags = 0 if _is_device(packets) else N.IN_HOST
-        need = self.output_bytes(n_frames, framed)
+        framed = framed or aligned
+        need = self.output_bytes(n_frames, framed, aligned)
         if out is None:
             pkt = N.OUT_PKT_BYTES if framed else N.OUT_PKT_DATA_BYTES
             out = np.empty((2, need // (2 * pkt) if need else 0, pkt), np.uint8)
@@ -130,6 +132,8 @@ class Resampler:
             flags |= N.OUT_HOST
         if framed:
             flags |= N.OUT_FRAMED
+        if aligned:
+            flags |= N.OUT_ALIGNED
         if asynchronous:
             flags |= N.ASYNC
         cap = _nbytes(out) if out_bytes is None else out_bytes
@@ -139,6 +143,10 @@ class Resampler:
         rc = self._lib.sdbe_process(self._h, _addr(packets), n_packets, n_frames, b_zero, _addr(out), cap,
                                     flags, st, C.byref(res) if res is not None else None)
         N.check(rc, self._h)
+        if aligned and res is not None and isinstance(out, np.ndarray):
+            # packed [2][P][8224] in the first 2*P*8224 bytes
+            n = res.n_out_packets
+            out = out.reshape(-1)[:2 * n * N.OUT_PKT_BYTES].reshape(2, n, N.OUT_PKT_BYTES)
         if res is None:
             return out, None
         return out, GroupResult(res.n_batches, res.n_out_packets, res.packets_accepted, res.packets_rejected,
@@ -161,6 +169,13 @@ class Resampler:
 
     def reset(self):
         N.check(self._lib.sdbe_reset(self._h), self._h)
+
+    def align_start(self, t0_sec: int, t0_clk: int, ref_epoch: int = 0):
+        """Arm output time alignment from the first B-engine timestamp."""
+        t = N.TimeTemplate()
+        N.check(self._lib.sdbe_header_template(t0_sec, t0_clk, ref_epoch, C.byref(t)))
+        N.check(self._lib.sdbe_align_start(self._h, C.byref(t)), self._h)
+        return (t.secs_inre, t.df_num_insec, t.ps_early, t.ref_epoch)
 
     def sync(self):
         N.check(self._lib.sdbe_sync(self._h), self._h)

@@ -77,3 +77,19 @@ def test_error_paths_without_gpu(built):
     assert lib.sdbe_quantize2bit(None, None, 17, 1.0, 0.0, None) == built.ERR_ARG
     assert lib.sdbe_reorder_mar2015(None, 1, None, None) == built.ERR_ARG
     assert lib.sdbe_process(None, None, 0, 0, 0, None, 0, 0, None, None) == built.ERR_ARG
+
+
+def test_header_template_matches_oracle(built):
+    """sdbe_header_template (host-only) == fill_vdif_header_template restated."""
+    from oracle import sdbe_oracle as O
+
+    lib = built.lib()
+    cases = [(1000, 0), (1000, 1), (1000, 262143), (1000, 262144), (1000, 262145), (7, 285999999),
+             (7, 285737856), (12345, 143000000), (12345, 2288 * 1000 + 17)]
+    rng = __import__("numpy").random.default_rng(9)
+    cases += [(int(s), int(c)) for s, c in zip(rng.integers(0, 2**20, 50), rng.integers(0, 286000000, 50))]
+    for sec, clk in cases:
+        t = built.TimeTemplate()
+        assert lib.sdbe_header_template(sec, clk, 30, C.byref(t)) == built.OK
+        ref = O.header_template(sec, clk, 30)
+        assert (t.secs_inre, t.df_num_insec, t.ps_early, t.ref_epoch) == ref, (sec, clk)

@@ -272,3 +272,24 @@ def test_mar2015_format_stream_vs_oracle(S):
     assert got.shape == ref.shape == (2, 3 * 128, 8192)
     for pol in range(2):
         assert _agreement(got[pol], ref[pol]) >= AGREE_MIN
+
+
+def test_time_aligned_frames_over_calls(S):
+    """Aligned frames == the output thread's skip + leftover carry applied to the plain payloads."""
+    from sdbe_gb300 import Resampler
+
+    spec = S.config1(stream=5)
+    spec.n_frames = 6
+    p = S.generate(spec)
+    calls = ((0, 2), (2, 1), (3, 3))
+    with Resampler(trim_mhz=150, max_frames=3) as plain_rs, Resampler(trim_mhz=150, max_frames=3) as rs:
+        tmpl = rs.align_start(1_234_567, 285_800_000, ref_epoch=30)
+        st = O.AlignState(template=tmpl)
+        for lo, nf in calls:
+            q = p[lo * 2048:(lo + nf) * 2048]
+            plain, _ = plain_rs.process(q, nf, spec.b_start + lo)
+            got, res = rs.process(q, nf, spec.b_start + lo, aligned=True)
+            ref = O.align_frames(plain, st)
+            assert got.shape == ref.shape, (got.shape, ref.shape)
+            np.testing.assert_array_equal(got, ref)
+    assert tmpl[1] > 125000 - 128   # the first block would cross a second: frames skipped
