@@ -166,6 +166,41 @@ typedef struct sdbe_time_template {
 int sdbe_header_template(int32_t t0_sec, int32_t t0_clk, uint32_t ref_epoch, sdbe_time_template *out);
 int sdbe_align_start(sdbe_resampler *h, const sdbe_time_template *t);
 
+/* Group assembly: packets as received from the network, restating the
+ * ingest thread (vdif_in_net_thread.c:255-500, vdif_in_databuf.c:96-167).
+ * Each batch is sorted invalid-first then by B-counter; the first valid b of
+ * the stream fixes groups of 143 B-frames starting at b_first + 1; a ring of
+ * 4 open groups takes packets (at most 2048 per frame, 292864 per group); a
+ * packet more than 2 groups ahead of the oldest open group ships that group
+ * incomplete (missing packets read as zero); a complete group ships at once;
+ * packets before the oldest group, more than 4*143 frames beyond the ring,
+ * or flagged invalid are counted and dropped.  Every shipped group runs the
+ * stage and writes one vdif_out_data_group_t ([2][16384][8192]) to out, in
+ * ship order, or with SDBE_OUT_FRAMED [2][16384] 8224-B VDIF frames whose
+ * headers continue the handle's counters; *n_groups returns how many.  packets must be host memory (the
+ * policy reads the headers); out is host (SDBE_OUT_HOST) or device memory
+ * with room for out_groups groups (otherwise SDBE_ERR_CAPACITY before any
+ * change of state, with *n_groups set to the number the batch ships).  Not
+ * available with the Mar-2015 channel map. */
+typedef struct sdbe_ingest_stats {
+    int64_t packets;           /* received                                      */
+    int64_t invalid;           /* invalid flag                                  */
+    int64_t before_start;      /* b before the oldest open group (skipped)      */
+    int64_t too_far_ahead;     /* b more than 4*143 frames beyond the ring      */
+    int64_t used;              /* offered to a group                            */
+    int64_t overflow;          /* offered but over the frame/group limits       */
+    int64_t groups_shipped;
+    int64_t groups_incomplete; /* shipped with fewer than 292864 packets        */
+    int64_t b_first;           /* -1 until the first valid packet               */
+    int64_t reserved[3];
+} sdbe_ingest_stats;
+int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void *out, int64_t out_groups,
+                uint32_t flags, int32_t *n_groups);
+/* Ship every open group that holds packets (end of stream; the reference
+ * drops them instead). */
+int sdbe_ingest_flush(sdbe_resampler *h, void *out, int64_t out_groups, uint32_t flags, int32_t *n_groups);
+int sdbe_ingest_get_stats(const sdbe_resampler *h, sdbe_ingest_stats *st);
+
 /* Wait for all work the handle issued (its streams and the last stream passed
  * to sdbe_process). */
 int sdbe_sync(sdbe_resampler *h);

@@ -519,3 +519,110 @@ def align_frames(payload, st: AlignState):
     st.df = dfs % VDIF_OUT_FRAMES_PER_SECOND
     st.psn += n_pkts
     return np.stack(frames)
+
+
+# ------------------------------------------------------- group assembly -----
+BENG_GROUPS_IN_BUFFER = 4              # vdif_in_databuf.h:146
+MAX_INDEX_LOOK_AHEAD = 2               # vdif_in_net_thread.c:136
+GROUP_PACKETS = BENG_FRAMES_PER_GROUP * VDIF_PER_BENG   # 292864
+
+
+class IngestState:
+    """Ingest-thread state: b_first, the oldest open group and per-group counts."""
+
+    def __init__(self):
+        self.b_first = -1
+        self.ref = 0                       # index of the oldest open group
+        self.count = {}                    # group -> packets inserted
+        self.fcount = {}                   # group -> per-frame packets inserted
+        self.stats = dict(packets=0, invalid=0, before_start=0, too_far_ahead=0, used=0, overflow=0,
+                          groups_shipped=0, groups_incomplete=0)
+
+    def start(self, g):
+        return self.b_first + 1 + BENG_FRAMES_PER_GROUP * g
+
+
+def ingest_policy(packets, st: IngestState, flush=False):
+    """Which packets join which group, and when groups ship.
+
+    Restates the ingest loop of ``vdif_in_net_thread.c:255-500``: each received
+    batch is sorted invalid-first then by b (``compar_beng``, ``:48-68``); the
+    first valid b of the stream fixes the groups at b_first+1+143k (``:317-337``);
+    per packet ``get_beng_group_index_offset`` (``vdif_in_databuf.c:96-124``)
+    returns invalid / before start / too far ahead (beyond the 4th group by
+    more than 4*143 frames) or the group offset; an offset above
+    MAX_INDEX_LOOK_AHEAD ships the oldest group incomplete and the packet is
+    examined again (``:393-401``); otherwise it is inserted
+    (``insert_vdif_in_beng_group_buffer``, ``vdif_in_databuf.c:126-156``: at most
+    2048 packets per frame and 292864 per group) and a complete oldest group
+    ships (``check_beng_group_complete``, ``:158-167``).  Returns the accept
+    mask (original packet order) and the groups shipped, in order.  Only the
+    first 24 bytes of a row are read: ``[n, 1056]`` packets or ``[n, k >= 24]``
+    header rows.  ``flush`` then ships every group still holding packets.
+    """
+    pk = np.asarray(packets, dtype=np.uint8)
+    pk = pk.reshape(-1, IN_PKT_BYTES) if pk.ndim == 1 else pk
+    w = np.ascontiguousarray(pk[:, :24]).view("<u4")   # header rows suffice
+    invalid = ((w[:, 0] >> 31) & 1).astype(np.int64)
+    b = ((w[:, 4].astype(np.uint64) << np.uint64(8)) | (w[:, 5].astype(np.uint64) >> np.uint64(24))).astype(np.int64)
+    n = pk.shape[0]
+    st.stats["packets"] += n
+    key = np.where(invalid != 0, -(2**62), b)
+    order = np.argsort(key, kind="stable")
+    accept = np.zeros(n, bool)
+    ships = []
+
+    def ship():
+        g = st.ref
+        ships.append(g)
+        st.stats["groups_shipped"] += 1
+        if st.count.get(g, 0) < GROUP_PACKETS:
+            st.stats["groups_incomplete"] += 1
+        st.count.pop(g, None)
+        st.fcount.pop(g, None)
+        st.ref += 1
+
+    if st.b_first < 0:
+        valid = order[invalid[order] == 0]
+        if valid.size == 0:
+            st.stats["invalid"] += n
+            return accept, ships
+        st.b_first = int(b[valid[0]])
+        st.ref = 0
+    for i in order:
+        bi = int(b[i])
+        while True:
+            if invalid[i]:
+                st.stats["invalid"] += 1
+                break
+            lo = st.start(st.ref)
+            if bi < lo:
+                st.stats["before_start"] += 1
+                break
+            off = (bi - lo) // BENG_FRAMES_PER_GROUP
+            if off >= BENG_GROUPS_IN_BUFFER:
+                lu_last = st.start(st.ref + BENG_GROUPS_IN_BUFFER) - 1
+                if bi > lu_last + BENG_GROUPS_IN_BUFFER * BENG_FRAMES_PER_GROUP:
+                    st.stats["too_far_ahead"] += 1
+                    break
+                off = BENG_GROUPS_IN_BUFFER
+            if off > MAX_INDEX_LOOK_AHEAD:
+                ship()
+                continue
+            g = st.ref + off
+            frame = bi - st.start(g)
+            fc = st.fcount.setdefault(g, np.zeros(BENG_FRAMES_PER_GROUP, np.int64))
+            st.stats["used"] += 1
+            if fc[frame] < VDIF_PER_BENG and st.count.get(g, 0) < GROUP_PACKETS:
+                fc[frame] += 1
+                st.count[g] = st.count.get(g, 0) + 1
+                accept[i] = True
+            else:
+                st.stats["overflow"] += 1
+            if st.count.get(st.ref, 0) == GROUP_PACKETS:
+                ship()
+            break
+    if flush:
+        while st.count:
+            ship()
+    return accept, ships

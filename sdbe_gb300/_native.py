@@ -59,6 +59,12 @@ class TimeTemplate(C.Structure):
                 ("ref_epoch", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class IngestStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("packets", "invalid", "before_start", "too_far_ahead", "used", "overflow",
+                                         "groups_shipped", "groups_incomplete", "b_first")] + [
+        ("reserved", C.c_int64 * 3)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("sigma", C.c_double), ("level", C.c_double), ("n_tones", C.c_int32),
                 ("tone_channel", C.c_int32 * 8), ("tone_amp", C.c_double * 8), ("tone_phase", C.c_double * 8),
@@ -80,6 +86,9 @@ SIGNATURES = {
     "sdbe_sync": (C.c_int, [vp]),
     "sdbe_header_template": (C.c_int, [i32, i32, u32, C.POINTER(TimeTemplate)]),
     "sdbe_align_start": (C.c_int, [vp, C.POINTER(TimeTemplate)]),
+    "sdbe_ingest": (C.c_int, [vp, vp, i64, vp, i64, u32, C.POINTER(i32)]),
+    "sdbe_ingest_flush": (C.c_int, [vp, vp, i64, u32, C.POINTER(i32)]),
+    "sdbe_ingest_get_stats": (C.c_int, [vp, C.POINTER(IngestStats)]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

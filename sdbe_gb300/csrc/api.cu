@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "handle.cuh"
 #include "launchers.cuh"
 #include "sdbe_internal.cuh"
 
@@ -20,67 +21,7 @@ const std::string &thread_error() { return g_thread_error; }
 
 using namespace sdbe;
 
-struct sdbe_resampler {
-    sdbe_config cfg{};
-    int skip = 0;
-    int wave = 4;
-    cudaStream_t stream = nullptr;
-    Twiddles tw{};
-    float2 *tw_storage = nullptr;
-    int64_t max_snaps = 0;
-    uint32_t *spec = nullptr;     // [2][max_snaps][2048] packed spectra
-    int64_t spec_pol_stride = 0;  // words
-    uint32_t *bitmap = nullptr;   // [max_frames][64]
-    int32_t *counts = nullptr;    // [max_frames] per-frame packets, then [1] rejected
-    float *ts = nullptr;          // [2][wave*143*32768] stage-A time series
-    int64_t ts_pol_stride = 0;
-    float *fout = nullptr;        // [2][128*32768] first-batch floats
-    double *partials = nullptr;   // [2][128][3]
-    float *thr = nullptr;         // device [8], see k_finalize_thresholds
-    // host I/O: two staging slots so one call's copies overlap another's compute
-    cudaStream_t copy_in = nullptr, copy_out = nullptr, last_stream = nullptr;
-    struct Stage {
-        uint8_t *pkt = nullptr;
-        int64_t pkt_bytes = 0;
-        uint8_t *out = nullptr;
-        int64_t out_bytes = 0;
-        cudaEvent_t pkt_ready = nullptr, pkt_free = nullptr, out_free = nullptr;
-    };
-    Stage stage[2];
-    int stage_idx = 0;
-    cudaEvent_t wave_ev = nullptr;
-    // output time alignment (SDBE_OUT_ALIGNED)
-    bool align_pending = false;
-    sdbe_time_template tmpl{};
-    int64_t skip_pending = 0;      // payload words still to drop
-    uint32_t *left[2] = {nullptr, nullptr};  // [2 pols][2048] leftover words, double-buffered
-    int left_idx = 0;
-    int64_t n_left = 0;
-    uint8_t *pay = nullptr;        // plain payload stream before alignment
-    int64_t pay_bytes = 0;
-    bool thresholds_set = false;
-    int64_t carry = 0;
-    // Mar-2015 format: unpacked frames land here first; the last one is held
-    // for the next call because output frame f needs input frame f+1.
-    uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]
-    int64_t raw_pol_stride = 0;   // words
-    int raw_carry = 0;            // 0 or 1 frame held
-    uint32_t secs = 0, df = 0, ref_epoch = 0, station = (uint32_t('S') << 8) | uint32_t('m'), bdc = 0, rx = 0;
-    uint64_t psn = 1;
-    std::string err;
-    // profiling (sdbe_profile_enable / sdbe_profile_read)
-    bool prof = false;
-    struct Timed {
-        cudaEvent_t a, b;
-        int kind;       // 0 = stage A, 1 = stage BC
-        int64_t units;  // snapshots or chunks
-    };
-    std::vector<Timed> timed;     // pool; first n_timed in use
-    size_t n_timed = 0;
-    int64_t launches = 0;
-};
-
-namespace {
+namespace sdbe {
 
 int fail(sdbe_resampler *h, int code, const std::string &msg) {
     if (h) h->err = msg;
@@ -88,25 +29,6 @@ int fail(sdbe_resampler *h, int code, const std::string &msg) {
     return code;
 }
 
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = true;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
-#define SDBE_CK(h, call)                                                                             \
-    do {                                                                                             \
-        cudaError_t e_ = (call);                                                                     \
-        if (e_ != cudaSuccess) return fail((h), SDBE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-// Event pair around one timed launch (profiling only).
 cudaError_t timed_begin(sdbe_resampler *h, int kind, int64_t units, cudaStream_t st, size_t *slot) {
     *slot = SIZE_MAX;
     if (!h->prof) return cudaSuccess;
@@ -142,6 +64,11 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->partials);
     cudaFree(h->thr);
     cudaFree(h->raw);
+    cudaFree(h->ring);
+    cudaFree(h->ring_bitmap);
+    cudaFree(h->ing_batch);
+    cudaFree(h->ing_accept);
+    cudaFree(h->ing_out);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
     cudaFree(h->pay);
@@ -187,7 +114,7 @@ int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const cha
     return SDBE_OK;
 }
 
-}  // namespace
+}  // namespace sdbe
 
 extern "C" {
 
@@ -422,44 +349,11 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
         h->psn += static_cast<uint64_t>(n_out);
     }
 
-    int64_t b = 0;
-    if (n_batches > 0 && !h->thresholds_set) {
-        // First batch: floats + FP64 statistics, thresholds set once (.cu:953-986).
-        SDBE_CK(h, launch_swarm_c2r(h->spec, h->spec_pol_stride, 0, kBatchSnaps, 2, h->ts, h->ts_pol_stride, h->tw, st));
-        ResampleOut o{};
-        o.fout = h->fout;
-        o.fout_pol_stride = static_cast<int64_t>(kChunks) * kNC;
-        o.partials = h->partials;
-        SDBE_CK(h, launch_resample(1, h->ts, h->ts_pol_stride, h->skip, kChunks, 2, o, h->tw, st));
-        SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
-        SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, tgt,
-                                          tgt_pol_stride, tgt_pkt_stride, tgt_off, 0, st));
-        h->thresholds_set = true;
-        h->launches += 4;
-        b = 1;
-        if (!aligned)
-            if (int rc = ship(0, kChunks)) return rc;
-    }
-    for (; b < n_batches; b += h->wave) {
-        const int64_t nb = std::min<int64_t>(h->wave, n_batches - b);
-        size_t slot;
-        SDBE_CK(h, timed_begin(h, 0, 2 * nb * kBatchSnaps, st, &slot));
-        SDBE_CK(h, launch_swarm_c2r(h->spec, h->spec_pol_stride, b * kBatchSnaps, nb * kBatchSnaps, 2, h->ts,
-                                    h->ts_pol_stride, h->tw, st));
-        SDBE_CK(h, timed_end(h, slot, st));
-        SDBE_CK(h, timed_begin(h, 1, 2 * nb * kChunks, st, &slot));
-        ResampleOut o{};
-        o.out = tgt;
-        o.out_pol_stride = tgt_pol_stride;
-        o.pkt_stride = tgt_pkt_stride;
-        o.payload_off = tgt_off;
-        o.pkt0 = b * kChunks;
-        o.thr = h->thr;
-        SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
-        SDBE_CK(h, timed_end(h, slot, st));
-        h->launches += 2;
-        if (!aligned)
-            if (int rc = ship(b * kChunks, (b + nb) * kChunks)) return rc;
+    {
+        PayloadTarget pt{tgt, tgt_pol_stride, tgt_pkt_stride, tgt_off};
+        int rc = fft_chain(h, h->spec, h->spec_pol_stride, n_batches, pt, st,
+                           [&](int64_t lo, int64_t hi) { return aligned ? SDBE_OK : ship(lo, hi); });
+        if (rc) return rc;
     }
     if (aligned) {
         const uint32_t *pay_w = reinterpret_cast<const uint32_t *>(h->pay);

@@ -1,0 +1,167 @@
+// The resampler handle and helpers shared by the host-side translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "launchers.cuh"
+#include "sdbe_internal.cuh"
+
+struct sdbe_resampler {
+    sdbe_config cfg{};
+    int skip = 0;
+    int wave = 4;
+    cudaStream_t stream = nullptr;
+    sdbe::Twiddles tw{};
+    float2 *tw_storage = nullptr;
+    int64_t max_snaps = 0;
+    uint32_t *spec = nullptr;     // [2][max_snaps][2048] packed spectra
+    int64_t spec_pol_stride = 0;  // words
+    uint32_t *bitmap = nullptr;   // [max_frames][64]
+    int32_t *counts = nullptr;    // [max_frames] per-frame packets, then [1] rejected
+    float *ts = nullptr;          // [2][wave*143*32768] stage-A time series
+    int64_t ts_pol_stride = 0;
+    float *fout = nullptr;        // [2][128*32768] first-batch floats
+    double *partials = nullptr;   // [2][128][3]
+    float *thr = nullptr;         // device [8], see k_finalize_thresholds
+    // host I/O: two staging slots so one call's copies overlap another's compute
+    cudaStream_t copy_in = nullptr, copy_out = nullptr, last_stream = nullptr;
+    struct Stage {
+        uint8_t *pkt = nullptr;
+        int64_t pkt_bytes = 0;
+        uint8_t *out = nullptr;
+        int64_t out_bytes = 0;
+        cudaEvent_t pkt_ready = nullptr, pkt_free = nullptr, out_free = nullptr;
+    };
+    Stage stage[2];
+    int stage_idx = 0;
+    cudaEvent_t wave_ev = nullptr;
+    // output time alignment (SDBE_OUT_ALIGNED)
+    bool align_pending = false;
+    sdbe_time_template tmpl{};
+    int64_t skip_pending = 0;      // payload words still to drop
+    uint32_t *left[2] = {nullptr, nullptr};  // [2 pols][2048] leftover words, double-buffered
+    int left_idx = 0;
+    int64_t n_left = 0;
+    uint8_t *pay = nullptr;        // plain payload stream before alignment
+    int64_t pay_bytes = 0;
+    // group assembly (sdbe_ingest): a ring of 4 open groups of 143 B-frames
+    uint32_t *ring = nullptr;      // [2][4*18304][2048] packed spectra
+    uint32_t *ring_bitmap = nullptr;  // [4][143][64]
+    uint8_t *ing_batch = nullptr;  // device copy of the received batch
+    int64_t ing_batch_bytes = 0;
+    uint8_t *ing_accept = nullptr; // device accept mask
+    int64_t ing_accept_bytes = 0;
+    uint8_t *ing_out = nullptr;    // staging for host output
+    int64_t ing_out_bytes = 0;
+    int64_t b_first = -1;
+    int64_t ing_ref = 0;
+    int64_t g_count[4] = {0, 0, 0, 0};
+    std::vector<int32_t> g_fcount = std::vector<int32_t>(4 * 143, 0);
+    int64_t g_id[4] = {-1, -1, -1, -1};  // group held by each slot
+    sdbe_ingest_stats ing{};
+    bool thresholds_set = false;
+    int64_t carry = 0;
+    // Mar-2015 format: unpacked frames land here first; the last one is held
+    // for the next call because output frame f needs input frame f+1.
+    uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]
+    int64_t raw_pol_stride = 0;   // words
+    int raw_carry = 0;            // 0 or 1 frame held
+    uint32_t secs = 0, df = 0, ref_epoch = 0, station = (uint32_t('S') << 8) | uint32_t('m'), bdc = 0, rx = 0;
+    uint64_t psn = 1;
+    std::string err;
+    // profiling (sdbe_profile_enable / sdbe_profile_read)
+    bool prof = false;
+    struct Timed {
+        cudaEvent_t a, b;
+        int kind;       // 0 = stage A, 1 = stage BC
+        int64_t units;  // snapshots or chunks
+    };
+    std::vector<Timed> timed;     // pool; first n_timed in use
+    size_t n_timed = 0;
+    int64_t launches = 0;
+};
+
+namespace sdbe {
+
+int fail(sdbe_resampler *h, int code, const std::string &msg);
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+#define SDBE_CK(h, call)                                                                             \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return ::sdbe::fail((h), SDBE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+cudaError_t timed_begin(sdbe_resampler *h, int kind, int64_t units, cudaStream_t st, size_t *slot);
+cudaError_t timed_end(sdbe_resampler *h, size_t slot, cudaStream_t st);
+int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what);
+
+// Where the FFT waves write their payload packets.
+struct PayloadTarget {
+    uint8_t *base;
+    int64_t pol_stride, pkt_stride, payload_off;
+};
+
+// First-batch threshold path (if thresholds are unset) and the FFT waves over
+// n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,
+// snapshots from 0), payload packets at tgt from packet 0.  on_wave(lo, hi)
+// runs after the waves that completed packets [lo, hi) are queued.
+template <class OnWave>
+int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
+              const PayloadTarget &tgt, cudaStream_t st, OnWave on_wave) {
+    int64_t b = 0;
+    if (n_batches > 0 && !h->thresholds_set) {
+        // First batch: floats + FP64 statistics, thresholds set once (.cu:953-986).
+        SDBE_CK(h, launch_swarm_c2r(spec, spec_pol_stride, 0, kBatchSnaps, 2, h->ts, h->ts_pol_stride, h->tw, st));
+        ResampleOut o{};
+        o.fout = h->fout;
+        o.fout_pol_stride = static_cast<int64_t>(kChunks) * kNC;
+        o.partials = h->partials;
+        SDBE_CK(h, launch_resample(1, h->ts, h->ts_pol_stride, h->skip, kChunks, 2, o, h->tw, st));
+        SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
+        SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, tgt.base,
+                                          tgt.pol_stride, tgt.pkt_stride, tgt.payload_off, 0, st));
+        h->thresholds_set = true;
+        h->launches += 4;
+        b = 1;
+        if (int rc = on_wave(0, kChunks)) return rc;
+    }
+    for (; b < n_batches; b += h->wave) {
+        const int64_t nb = n_batches - b < h->wave ? n_batches - b : h->wave;
+        size_t slot;
+        SDBE_CK(h, timed_begin(h, 0, 2 * nb * kBatchSnaps, st, &slot));
+        SDBE_CK(h, launch_swarm_c2r(spec, spec_pol_stride, b * kBatchSnaps, nb * kBatchSnaps, 2, h->ts,
+                                    h->ts_pol_stride, h->tw, st));
+        SDBE_CK(h, timed_end(h, slot, st));
+        SDBE_CK(h, timed_begin(h, 1, 2 * nb * kChunks, st, &slot));
+        ResampleOut o{};
+        o.out = tgt.base;
+        o.out_pol_stride = tgt.pol_stride;
+        o.pkt_stride = tgt.pkt_stride;
+        o.payload_off = tgt.payload_off;
+        o.pkt0 = b * kChunks;
+        o.thr = h->thr;
+        SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
+        SDBE_CK(h, timed_end(h, slot, st));
+        h->launches += 2;
+        if (int rc = on_wave(b * kChunks, (b + nb) * kChunks)) return rc;
+    }
+    return SDBE_OK;
+}
+
+}  // namespace sdbe

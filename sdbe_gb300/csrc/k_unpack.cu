@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict
                                                        uint32_t *__restrict__ spec, int64_t pol_stride,
                                                        int64_t snap0, uint32_t *__restrict__ bitmap,
                                                        int32_t *__restrict__ counts,
-                                                       int32_t *__restrict__ rejected) {
+                                                       int32_t *__restrict__ rejected,
+                                                       const uint8_t *__restrict__ accept) {
     __shared__ uint4 tile[2][kTilePkts][32];
     __shared__ int64_t s_row[kTilePkts];
     __shared__ int s_group[kTilePkts];
@@ -79,9 +80,10 @@ __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict
             const uint32_t w0 = __ldg(reinterpret_cast<const uint32_t *>(src));
             const uint4 h1 = __ldg(src + 1);
             const PktHeader h = decode_header(w0, h1.x, h1.y, b_zero, n_frames, map);
+            const bool take = h.ok && (accept == nullptr || accept[p] != 0);
             const uint4 a = __ldcs(src + 2 + 2 * lane);
             const uint4 b = __ldcs(src + 3 + 2 * lane);
-            if (h.ok) {
+            if (take) {
                 uint4 o0, o1;
                 pack_snapshot(a.x, a.y, o0.x, o1.x);
                 pack_snapshot(a.z, a.w, o0.y, o1.y);
@@ -93,9 +95,9 @@ __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict
                 group = h.group;
                 if (lane == 0) {
                     atomicOr(bitmap + h.frame * 64 + (h.c >> 2), 1u << ((h.c & 3u) * 8u + h.f));
-                    atomicAdd(counts + h.frame, 1);
+                    if (counts != nullptr) atomicAdd(counts + h.frame, 1);
                 }
-            } else if (lane == 0) {
+            } else if (lane == 0 && rejected != nullptr) {
                 atomicAdd(rejected, 1);
             }
         }
@@ -222,12 +224,12 @@ __global__ void k_beng_to_complex(const int8_t *__restrict__ beng, int64_t n_spe
 // ---- launchers ---------------------------------------------------------------
 cudaError_t launch_unpack(const void *pkts, int64_t n_pkts, uint64_t b_zero, int n_frames, int map,
                           uint32_t *spec, int64_t pol_stride, int64_t snap0, uint32_t *bitmap,
-                          int32_t *counts, int32_t *rejected, cudaStream_t st) {
+                          int32_t *counts, int32_t *rejected, cudaStream_t st, const uint8_t *accept) {
     if (n_pkts <= 0) return cudaSuccess;
     const int64_t blocks = (n_pkts + kTilePkts - 1) / kTilePkts;
     k_unpack_packed<<<static_cast<unsigned>(blocks), 256, 0, st>>>(
         static_cast<const uint8_t *>(pkts), n_pkts, b_zero, n_frames, map, spec, pol_stride, snap0, bitmap,
-        counts, rejected);
+        counts, rejected, accept);
     return cudaGetLastError();
 }
 

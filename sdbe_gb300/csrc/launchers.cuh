@@ -13,7 +13,7 @@ struct ResampleOut {
     double *partials;
 };
 cudaError_t launch_unpack(const void *, int64_t, uint64_t, int, int, uint32_t *, int64_t, int64_t, uint32_t *,
-                          int32_t *, int32_t *, cudaStream_t);
+                          int32_t *, int32_t *, cudaStream_t, const uint8_t *accept = nullptr);
 cudaError_t launch_fill_missing(const uint32_t *, int, int, uint32_t *, int64_t, int64_t, cudaStream_t);
 cudaError_t launch_vdif_to_beng_ref(const void *, int64_t, uint64_t, int, int, int8_t *, int8_t *, cudaStream_t);
 cudaError_t launch_reorder_mar2015(const uint32_t *, int, uint32_t *, cudaStream_t);

@@ -11,8 +11,9 @@
 // bits 4-5/6-7 = pol-0 imag/real.  Headers carry b in w4/w5 and (c, f) in w5
 // (vdif_in_databuf.h:29-59).  Packets are emitted b-major, then c, then f.
 //
-// Every B-frame draws from its own generator seeded by (seed, frame index),
-// so output does not depend on the number of threads.
+// Every B-frame draws from its own generator seeded by (seed, B-counter), so
+// output depends neither on the number of threads nor on how a stream is cut
+// into calls.
 #include <stdint.h>
 
 #include <algorithm>
@@ -103,8 +104,8 @@ int64_t sdbe_synth_packets(uint8_t *out, int64_t n_frames, uint64_t b_start, uin
 
     auto gen_frame = [&](int64_t fi) {
         const uint64_t b = b_start + static_cast<uint64_t>(fi);
-        Xoshiro256 rng(seed * 0x100000001B3ull ^ (static_cast<uint64_t>(fi) + 1) * 0x9E3779B97F4A7C15ull);
-        Xoshiro256 brng(seed ^ 0xB0B5u ^ (static_cast<uint64_t>(fi) << 20));
+        Xoshiro256 rng(seed * 0x100000001B3ull ^ (b + 1) * 0x9E3779B97F4A7C15ull);
+        Xoshiro256 brng(seed ^ 0xB0B5u ^ (b << 20));
         bool burst[128];
         for (int s = 0; s < 128; ++s) burst[s] = cfg->burst_frac > 0.0 && brng.uniform() < cfg->burst_frac;
         uint8_t *frame = out + fi * 2048 * 1056;

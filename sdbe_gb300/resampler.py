@@ -177,6 +177,58 @@ class Resampler:
         N.check(self._lib.sdbe_align_start(self._h, C.byref(t)), self._h)
         return (t.secs_inre, t.df_num_insec, t.ps_early, t.ref_epoch)
 
+    # -- group assembly ------------------------------------------------------
+    GROUP_PACKETS_OUT = 16384  # output packets per pol of one 143-frame group
+
+    def _group_out(self, n_groups, framed):
+        pkt = N.OUT_PKT_BYTES if framed else N.OUT_PKT_DATA_BYTES
+        return np.empty((n_groups, 2, self.GROUP_PACKETS_OUT, pkt), np.uint8)
+
+    def ingest(self, packets, out=None, out_groups: int | None = None, framed: bool = False):
+        """Offer received packets (host ``[n, 1056]`` uint8) to the group ring.
+
+        Returns ``(groups, n)``: the ``n`` groups this batch shipped, as
+        ``[n, 2, 16384, 8192]`` payloads (8224-B frames when ``framed``).
+        Without ``out`` a host array is sized from the packet count and grown
+        once if the batch ships more.
+        """
+        pk = np.ascontiguousarray(packets, dtype=np.uint8).reshape(-1, N.IN_PKT_BYTES)
+        flags = N.OUT_FRAMED if framed else 0
+        auto = out is None
+        if auto:
+            out_groups = pk.shape[0] // 292864 + 1 if out_groups is None else out_groups
+            out = self._group_out(out_groups, framed)
+        elif out_groups is None:
+            out_groups = int(out.shape[0])
+        if not _is_device(out):
+            flags |= N.OUT_HOST
+        n = C.c_int32(0)
+        rc = self._lib.sdbe_ingest(self._h, pk.ctypes.data, pk.shape[0], _addr(out), out_groups, flags,
+                                   C.byref(n))
+        if rc == N.ERR_CAPACITY and auto:  # n holds the number of groups the batch ships
+            out_groups = n.value
+            out = self._group_out(out_groups, framed)
+            rc = self._lib.sdbe_ingest(self._h, pk.ctypes.data, pk.shape[0], _addr(out), out_groups, flags,
+                                       C.byref(n))
+        N.check(rc, self._h)
+        return (out[:n.value] if isinstance(out, np.ndarray) else out), n.value
+
+    def ingest_flush(self, out=None, out_groups: int = 4, framed: bool = False):
+        """Ship every open group that holds packets (end of stream)."""
+        flags = N.OUT_FRAMED if framed else 0
+        if out is None:
+            out = self._group_out(out_groups, framed)
+        if not _is_device(out):
+            flags |= N.OUT_HOST
+        n = C.c_int32(0)
+        N.check(self._lib.sdbe_ingest_flush(self._h, _addr(out), out_groups, flags, C.byref(n)), self._h)
+        return (out[:n.value] if isinstance(out, np.ndarray) else out), n.value
+
+    def ingest_stats(self) -> dict:
+        st = N.IngestStats()
+        N.check(self._lib.sdbe_ingest_get_stats(self._h, C.byref(st)), self._h)
+        return {k: int(getattr(st, k)) for k, _ in N.IngestStats._fields_ if k != "reserved"}
+
     def sync(self):
         N.check(self._lib.sdbe_sync(self._h), self._h)
 

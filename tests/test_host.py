@@ -24,6 +24,8 @@ def test_generator_is_deterministic_and_thread_independent(synth):
     a = synth.generate(spec, n_threads=1)
     b = synth.generate(spec, n_threads=3)
     assert np.array_equal(a, b)
+    # frames are the same whichever call generates them
+    assert np.array_equal(synth.generate(spec, frame_offset=1, n_frames=2), a[2048:])
     spec2 = synth.config1(stream=1)
     spec2.n_frames = 3
     assert not np.array_equal(a, synth.generate(spec2))
