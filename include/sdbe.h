@@ -68,6 +68,9 @@ extern "C" {
                                       buffers must stay valid until sdbe_sync          */
 #define SDBE_OUT_ALIGNED 32u       /* time-aligned 8224-B VDIF frames (implies FRAMED):
                                       the output thread's skip + leftover carry         */
+#define SDBE_IN_8PAC 64u           /* sdbe_ingest: input is 8pac units with new-format
+                                      B-engine headers (unpack + reform first)          */
+#define SDBE_PAC8_BYTES 8504       /* sizeof(vdif_8pac_packet_t), vdif_8pac.h:8-16     */
 
 typedef struct sdbe_config {
     int32_t device;            /* CUDA device ordinal (resampler->deviceId, .cu:147)        */
@@ -200,6 +203,37 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
  * drops them instead). */
 int sdbe_ingest_flush(sdbe_resampler *h, void *out, int64_t out_groups, uint32_t flags, int32_t *n_groups);
 int sdbe_ingest_get_stats(const sdbe_resampler *h, sdbe_ingest_stats *st);
+
+/* Ingest transforms (vdif_in_net_thread.c:291-298), the receive-side
+ * pre-pass for SWARM's 8pac output.
+ *
+ * sdbe_unpack_8pac: n_units 8504-B units -> 8*n_units 1056-B packets, device
+ * memory, 8-byte aligned (unpack_8pac, vdif_8pac.c:47-56): df_len of all 8 set
+ * to ((df_len_1 - 7)/8) & 0xFFFFFF, df_num_insec 8*df_1 + k, psn 8*psn_1 + k,
+ * packet 1's invalid flag copied to the other 7, VTP prefixes dropped.  Unlike
+ * the reference, the input units are left unmodified.
+ *
+ * sdbe_beng_reform: rewrite new-format B-engine headers (a 53-bit SWARM
+ * timestamp, c, 3-bit f) to the old format in place on the device, with the
+ * B-count = frames since the first valid packet (beng_reform_headers,
+ * beng_reform.c:137-186).  The reference keeps T0/TPREV/BPREV in file-scope
+ * statics; here they are the caller's sdbe_reform_state (start from
+ * sdbe_reform_init), read and written by each call, which synchronizes the
+ * stream.  sdbe_header_template(t0_sec, t0_clk, ...) takes T0 from it
+ * (get_beng_t0, beng_reform.c:113-126, applies the one-frame correction). */
+typedef struct sdbe_reform_state {
+    int32_t t0_sec, t0_clk;       /* first valid packet's timestamp; -1, -1 until then      */
+    int32_t tprev_sec, tprev_clk; /* last counted packet's timestamp (TPREV)                */
+    int64_t bprev;                /* its B-count (BPREV; a 32-bit int in the reference)     */
+    int64_t marked_invalid;       /* packets invalidated for a jump beyond 1000 frames      */
+    int64_t slow_tiles;           /* 1024-packet tiles counted one packet at a time         */
+    int64_t reserved;
+} sdbe_reform_state;
+int sdbe_reform_init(sdbe_reform_state *st);
+int sdbe_unpack_8pac(const void *src, int64_t n_units, void *dst, void *stream);
+int sdbe_beng_reform(sdbe_reform_state *st, void *pkts, int64_t n_pkts, void *stream);
+/* The reform state of a handle's sdbe_ingest stream (SDBE_IN_8PAC batches). */
+int sdbe_ingest_reform_state(const sdbe_resampler *h, sdbe_reform_state *st);
 
 /* Wait for all work the handle issued (its streams and the last stream passed
  * to sdbe_process). */

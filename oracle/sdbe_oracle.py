@@ -18,7 +18,11 @@ Pinned against reference code run in this container on seeded inputs: see
 ``sdbe_preprocess.quantize_to_2bit`` + ``vdif.VDIFFrame.to_bin`` packing and
 header words, the Mar-2015 reorder check of ``prototyping/cuda/reorder.py`` and
 the cuFFT scale convention of the FFT-resample check in
-``prototyping/cuda/resample.py``).
+``prototyping/cuda/resample.py``).  The 8pac unpack and header reform are
+pinned against the reference's own C (``software/aphids/vdif_8pac.c``,
+``beng_reform.c``) compiled by ``oracle/Makefile``: see
+``tests/golden/make_8pac_golden.py``.  The ingest policy
+(``ingest_policy``) is a restatement checked by properties only.
 """
 from __future__ import annotations
 
@@ -433,7 +437,7 @@ OUT_WORDS_PER_PKT = OUT_PKT_DATA_BYTES // 4
 
 
 def beng_timestamp_increment(sec, clk):
-    """One B-frame later (``beng_reform.c:56-62``; wraps only when clk > 286e6)."""
+    """One B-frame later (``beng_reform.c:192-198``; wraps only when clk > 286e6)."""
     clk += SWARM_BFRAME_CLK
     if clk > SWARM_CLK_PER_SEC:
         sec += 1
@@ -442,7 +446,7 @@ def beng_timestamp_increment(sec, clk):
 
 
 def beng_timestamp_decrement(sec, clk):
-    """One B-frame earlier (``beng_reform.c:64-70``)."""
+    """One B-frame earlier (``beng_reform.c:200-206``)."""
     clk -= SWARM_BFRAME_CLK
     if clk < 0:
         sec -= 1
@@ -626,3 +630,147 @@ def ingest_policy(packets, st: IngestState, flush=False):
         while st.count:
             ship()
     return accept, ships
+
+
+# ---------------------------------------------------------------------------
+# 8pac input format and the B-engine header reform (ingest transforms)
+# ---------------------------------------------------------------------------
+VTP_BYTES = 8                                       # vdif_8pac.h:6
+PAC8_BYTES = IN_PKT_BYTES + 7 * (VTP_BYTES + IN_PKT_BYTES)   # sizeof(vdif_8pac_packet_t) = 8504
+BFRAME_CLK_TOL = 1024                               # beng_reform.c:29
+MAX_COUNTABLE_BFRAME_OFFSET = 1000                  # beng_reform.c:65
+
+
+def pac8_offsets():
+    """Byte offset of each of the 8 packets inside one 8pac (vdif_8pac.h:8-16)."""
+    return np.array([0] + [IN_PKT_BYTES + k * (VTP_BYTES + IN_PKT_BYTES) + VTP_BYTES for k in range(7)])
+
+
+def unpack_8pac(src):
+    """8pac units -> plain 1056-B packets, ``unpack_8pac`` (vdif_8pac.c:47-56).
+
+    Per unit: df_len of all 8 = ((df_len_1 - 7) / 8) & 0xFFFFFF, the 24-bit
+    bit-field promoted to int and divided toward zero (``reset_8pac_size``,
+    :5-13); df_num_insec = 8*df_1 (+k for packet k, 24-bit field, ``:15-23``);
+    psn = 8*psn_1 (+k, ``:25-34``); the invalid bit of packet 1 copied to the
+    other 7 (``:36-41``).  The 8-byte VTP prefixes are dropped.
+    """
+    s = np.ascontiguousarray(src, dtype=np.uint8).reshape(-1, PAC8_BYTES)
+    n = s.shape[0]
+    off = pac8_offsets()
+    out = np.empty((n, 8, IN_PKT_BYTES), np.uint8)
+    for k in range(8):
+        out[:, k] = s[:, off[k]:off[k] + IN_PKT_BYTES]
+    w = out.view("<u4").reshape(n, 8, IN_PKT_BYTES // 4)
+    w1 = w[:, 0]
+    df_len = (w1[:, 2] & 0xFFFFFF).astype(np.int64) - 7
+    newsize = (np.sign(df_len) * (np.abs(df_len) // 8)).astype(np.int64) & 0xFFFFFF
+    df8 = (8 * (w1[:, 1] & 0xFFFFFF).astype(np.int64))
+    psn1 = w1[:, 6].astype(np.uint64) | (w1[:, 7].astype(np.uint64) << np.uint64(32))
+    inv = w1[:, 0] >> 31
+    for k in range(8):
+        wk = w[:, k]
+        wk[:, 2] = (wk[:, 2] & np.uint32(0xFF000000)) | newsize.astype(np.uint32)
+        wk[:, 1] = (wk[:, 1] & np.uint32(0xFF000000)) | ((df8 + k) & 0xFFFFFF).astype(np.uint32)
+        psn = psn1 * np.uint64(8) + np.uint64(k)
+        wk[:, 6] = (psn & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        wk[:, 7] = (psn >> np.uint64(32)).astype(np.uint32)
+        if k:
+            wk[:, 0] = (wk[:, 0] & np.uint32(0x7FFFFFFF)) | (inv << np.uint32(31))
+    return out.reshape(n * 8, IN_PKT_BYTES)
+
+
+def read_beng_timestamp(w4, w5):
+    """(sec, clk) of the new-format B-engine header (beng_reform.h:14-19,
+    ``_read_beng_timestamp`` beng_reform.c:16-22): b = b_upper<<21 | b_lower
+    (w5 bits 11-31); clk = b & 0x1FFFFFFF, sec = bits 29-52 of b."""
+    b = (int(w4) << 21) | ((int(w5) >> 11) & 0x1FFFFF)
+    return (b & 0x001FFFFFE0000000) >> 29, b & 0x1FFFFFFF
+
+
+def timestamp_compare(then, now):
+    """``_beng_timestamp_compare_then_now`` (beng_reform.c:34-61), as written
+    (the later-second branch does not check that the seconds are adjacent)."""
+    C, T = SWARM_CLK_PER_SEC, BFRAME_CLK_TOL
+    if then[0] < now[0]:
+        if then[0] == now[0] - 1 and then[1] + T > C and (then[1] + T) % C >= now[1]:
+            return 0
+        return -1
+    if then[0] > now[0]:
+        if now[1] + T > C and (now[1] + T) % C >= then[1]:
+            return 0
+        return 1
+    if then[1] + T < now[1]:
+        return -1
+    if now[1] + T < then[1]:
+        return 1
+    return 0
+
+
+def timestamp_offset(then, now):
+    """B-frames from then to now by stepping (beng_reform.c:71-104), capped
+    just beyond MAX_COUNTABLE_BFRAME_OFFSET."""
+    cmp = timestamp_compare(then, now)
+    if cmp == 0:
+        return 0
+    start, end, step = (then, now, 1) if cmp < 0 else (now, then, -1)
+    off = 0
+    while timestamp_compare(start, end) < 0:
+        start = beng_timestamp_increment(*start)
+        off += step
+        if abs(off) > MAX_COUNTABLE_BFRAME_OFFSET:
+            break
+    return off
+
+
+class ReformState:
+    """The reform's stream state: T0, TPREV and BPREV (beng_reform.c:6-14)."""
+
+    def __init__(self):
+        self.t0 = (-1, -1)
+        self.tprev = (-1, -1)
+        self.bprev = -1
+
+
+def _i32(v):
+    return ((int(v) + 2**31) % 2**32) - 2**31
+
+
+def beng_reform_headers(pkts, st: ReformState):
+    """Rewrite new-format B-engine headers to the old format in place
+    (``beng_reform_headers``, beng_reform.c:137-186).
+
+    Invalid packets are left alone; the first valid packet fixes T0; each valid
+    packet's B-count is BPREV + the frame offset from TPREV (a 32-bit int, as
+    in the reference); an offset beyond +-1000 frames marks the packet invalid
+    with count -1 and leaves TPREV/BPREV unchanged.  Only the c, f, b_lower
+    bytes of w5 and all of w4 are written; byte 1 of w5 keeps its old bits.
+    """
+    w = pkts.view("<u4").reshape(-1, IN_PKT_BYTES // 4)
+    for i in range(w.shape[0]):
+        if w[i, 0] >> 31:
+            continue
+        w4, w5 = int(w[i, 4]), int(w[i, 5])
+        if st.t0 == (-1, -1):
+            st.t0 = read_beng_timestamp(w4, w5)
+            st.tprev = st.t0
+            st.bprev = 0
+        now = read_beng_timestamp(w4, w5)
+        off = _i32(timestamp_offset(st.tprev, now))
+        if off > MAX_COUNTABLE_BFRAME_OFFSET or off < -MAX_COUNTABLE_BFRAME_OFFSET:
+            w[i, 0] |= np.uint32(1 << 31)
+            off = -1
+        else:
+            off = _i32(off + st.bprev)
+            st.tprev = now
+            st.bprev = off
+        c, f = w5 & 0xFF, (w5 >> 8) & 0x7
+        w[i, 5] = np.uint32((w5 & 0x0000FF00) | c | (f << 16) | ((off & 0xFF) << 24))
+        w[i, 4] = np.uint32((off & 0x7FFFFF00) >> 8)
+    return pkts
+
+
+def reform_t0(st: ReformState):
+    """``get_beng_t0`` (beng_reform.c:113-126): T0 one B-frame earlier
+    (SWARM_TIMESTAMP_OFF_BY_BENG = -1)."""
+    return beng_timestamp_decrement(*st.t0)

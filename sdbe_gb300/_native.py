@@ -26,7 +26,8 @@ FRAMES_PER_GROUP = 143
 SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED = 0, 1
 MAP_APHIDS, MAP_MAR2015 = 0, 1
-IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED = 1, 2, 4, 8, 16, 32
+IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED, IN_8PAC = 1, 2, 4, 8, 16, 32, 64
+PAC8_BYTES = 8504
 NOALLOC_MAX_SAMPLES = 134217728
 
 
@@ -65,6 +66,12 @@ class IngestStats(C.Structure):
         ("reserved", C.c_int64 * 3)]
 
 
+class ReformState(C.Structure):
+    _fields_ = [("t0_sec", C.c_int32), ("t0_clk", C.c_int32), ("tprev_sec", C.c_int32), ("tprev_clk", C.c_int32),
+                ("bprev", C.c_int64), ("marked_invalid", C.c_int64), ("slow_tiles", C.c_int64),
+                ("reserved", C.c_int64)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("sigma", C.c_double), ("level", C.c_double), ("n_tones", C.c_int32),
                 ("tone_channel", C.c_int32 * 8), ("tone_amp", C.c_double * 8), ("tone_phase", C.c_double * 8),
@@ -89,6 +96,10 @@ SIGNATURES = {
     "sdbe_ingest": (C.c_int, [vp, vp, i64, vp, i64, u32, C.POINTER(i32)]),
     "sdbe_ingest_flush": (C.c_int, [vp, vp, i64, u32, C.POINTER(i32)]),
     "sdbe_ingest_get_stats": (C.c_int, [vp, C.POINTER(IngestStats)]),
+    "sdbe_ingest_reform_state": (C.c_int, [vp, C.POINTER(ReformState)]),
+    "sdbe_reform_init": (C.c_int, [C.POINTER(ReformState)]),
+    "sdbe_unpack_8pac": (C.c_int, [vp, i64, vp, vp]),
+    "sdbe_beng_reform": (C.c_int, [C.POINTER(ReformState), vp, i64, vp]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

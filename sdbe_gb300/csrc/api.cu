@@ -69,6 +69,9 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->ing_batch);
     cudaFree(h->ing_accept);
     cudaFree(h->ing_out);
+    cudaFree(h->ing_raw);
+    cudaFree(h->ing_hdr);
+    cudaFree(h->reform_dev);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
     cudaFree(h->pay);
@@ -429,7 +432,7 @@ int sdbe_header_template(int32_t t0_sec, int32_t t0_clk, uint32_t ref_epoch, sdb
         sec -= 1;
         clk += kClkPerSec;
     }
-    // fill_vdif_header_template: one B-frame later (beng_reform.c:56-62)
+    // fill_vdif_header_template: one B-frame later (beng_reform.c:192-198)
     clk += kBframeClk;
     if (clk > kClkPerSec) {
         sec += 1;

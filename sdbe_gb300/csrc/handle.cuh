@@ -56,11 +56,16 @@ struct sdbe_resampler {
     int64_t ing_accept_bytes = 0;
     uint8_t *ing_out = nullptr;    // staging for host output
     int64_t ing_out_bytes = 0;
+    uint8_t *ing_raw = nullptr;    // device copy of a host 8pac batch
+    int64_t ing_raw_bytes = 0;
+    uint8_t *ing_hdr = nullptr;    // [n][3] header words (w0, w4, w5) read back for the policy
+    int64_t ing_hdr_bytes = 0;
+    sdbe_reform_state reform{-1, -1, -1, -1, -1, 0, 0, 0};  // 8pac batches: reform state
+    sdbe_reform_state *reform_dev = nullptr;                // kernel's output state
     int64_t b_first = -1;
     int64_t ing_ref = 0;
     int64_t g_count[4] = {0, 0, 0, 0};
     std::vector<int32_t> g_fcount = std::vector<int32_t>(4 * 143, 0);
-    int64_t g_id[4] = {-1, -1, -1, -1};  // group held by each slot
     sdbe_ingest_stats ing{};
     bool thresholds_set = false;
     int64_t carry = 0;

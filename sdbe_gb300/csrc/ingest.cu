@@ -57,17 +57,29 @@ void ship(Policy &p, std::vector<int64_t> &ships) {
     p.ref += 1;
 }
 
+// Header words w0, w4, w5 of packet i: at base + i*stride, offsets 0, o4, o5
+// (host packets, or the [n][3] words read back from the device).
+struct HdrView {
+    const uint8_t *base;
+    int64_t stride;
+    int o4, o5;
+    uint32_t word(int64_t i, int off) const {
+        uint32_t v;
+        std::memcpy(&v, base + i * stride + off, sizeof(v));
+        return v;
+    }
+};
+
 // One received batch through the policy: accept[i] for packet i, the groups
 // that ship in order, and the groups that received packets.
-void run_policy(Policy &p, const uint8_t *pkts, int64_t n, std::vector<uint8_t> &accept, std::vector<int64_t> &ships,
+void run_policy(Policy &p, const HdrView &hv, int64_t n, std::vector<uint8_t> &accept, std::vector<int64_t> &ships,
                 std::vector<int64_t> &touched) {
     std::vector<int64_t> key(n);
     std::vector<uint8_t> inval(n);
     for (int64_t i = 0; i < n; ++i) {
-        uint32_t w[6];
-        std::memcpy(w, pkts + i * kPktBytes, sizeof(w));
-        inval[i] = static_cast<uint8_t>(w[0] >> 31);
-        const int64_t b = static_cast<int64_t>((static_cast<uint64_t>(w[4]) << 8) | (w[5] >> 24));
+        const uint32_t w0 = hv.word(i, 0), w4 = hv.word(i, hv.o4), w5 = hv.word(i, hv.o5);
+        inval[i] = static_cast<uint8_t>(w0 >> 31);
+        const int64_t b = static_cast<int64_t>((static_cast<uint64_t>(w4) << 8) | (w5 >> 24));
         key[i] = inval[i] ? INT64_MIN : b;  // compar_beng: invalid first, then by b
     }
     std::vector<int64_t> order(n);
@@ -223,34 +235,81 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
     if (n_packets < 0 || (n_packets > 0 && !packets) || out_groups < 0)
         return fail(h, SDBE_ERR_ARG, "bad argument");
     if (h->cfg.channel_map == SDBE_MAP_MAR2015) return fail(h, SDBE_ERR_STATE, "ingest does not support Mar-2015");
-    const uint8_t *pk = static_cast<const uint8_t *>(packets);
+    const bool pac8 = (flags & SDBE_IN_8PAC) != 0, in_host = (flags & SDBE_IN_HOST) != 0;
+    if (pac8 && !in_host && (reinterpret_cast<uintptr_t>(packets) & 7u))
+        return fail(h, SDBE_ERR_ARG, "8pac input must be 8-byte aligned");
+    if (!pac8 && !in_host && (reinterpret_cast<uintptr_t>(packets) & 15u))
+        return fail(h, SDBE_ERR_ARG, "device packets must be 16-byte aligned");
+    DeviceGuard g(h->cfg.device);
+    if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
+    cudaStream_t st = h->stream;
+    const int64_t n_pk = pac8 ? 8 * n_packets : n_packets;
+    const uint8_t *dev_pkts = nullptr;
+    sdbe_reform_state reform = h->reform;
+    std::vector<uint32_t> hdr;
+    HdrView hv{static_cast<const uint8_t *>(packets), kPktBytes, 16, 20};
+    int rc = SDBE_OK;
+    if ((pac8 || !in_host) && n_pk > 0) {
+        // The policy reads the headers on the host: produce them on the device
+        // (after the 8pac unpack and header reform) and read back 12 B a packet.
+        rc = grow(h, &h->ing_hdr, &h->ing_hdr_bytes, n_pk * 12, "ingest header words");
+        if (rc) return rc;
+        if (pac8) {
+            const void *src = packets;
+            if (in_host) {
+                rc = grow(h, &h->ing_raw, &h->ing_raw_bytes, n_packets * kPac8Bytes, "8pac staging");
+                if (rc) return rc;
+                SDBE_CK(h, cudaMemcpyAsync(h->ing_raw, packets, n_packets * kPac8Bytes, cudaMemcpyHostToDevice, st));
+                src = h->ing_raw;
+            }
+            rc = grow(h, &h->ing_batch, &h->ing_batch_bytes, n_pk * kPktBytes, "ingest batch");
+            if (rc) return rc;
+            if (!h->reform_dev) SDBE_CK(h, cudaMalloc(&h->reform_dev, sizeof(sdbe_reform_state)));
+            SDBE_CK(h, launch_unpack_8pac(src, n_packets, h->ing_batch, st));
+            SDBE_CK(h, launch_beng_reform(h->ing_batch, n_pk, h->reform, h->reform_dev,
+                                          reinterpret_cast<uint32_t *>(h->ing_hdr), st));
+            SDBE_CK(h, cudaMemcpyAsync(&reform, h->reform_dev, sizeof(reform), cudaMemcpyDeviceToHost, st));
+            h->launches += 2;
+            dev_pkts = h->ing_batch;
+        } else {
+            SDBE_CK(h, launch_gather_headers(packets, n_pk, reinterpret_cast<uint32_t *>(h->ing_hdr), st));
+            h->launches += 1;
+            dev_pkts = static_cast<const uint8_t *>(packets);
+        }
+        hdr.resize(static_cast<size_t>(n_pk) * 3);
+        SDBE_CK(h, cudaMemcpyAsync(hdr.data(), h->ing_hdr, n_pk * 12, cudaMemcpyDeviceToHost, st));
+        SDBE_CK(h, cudaStreamSynchronize(st));
+        hv = HdrView{reinterpret_cast<const uint8_t *>(hdr.data()), 12, 4, 8};
+    }
     Policy p = snapshot(h);
     std::vector<uint8_t> accept;
     std::vector<int64_t> ships, touched;
-    run_policy(p, pk, n_packets, accept, ships, touched);
+    run_policy(p, hv, n_pk, accept, ships, touched);
     const int64_t n_ships = static_cast<int64_t>(ships.size());
     if (n_ships > out_groups) {
         if (n_groups) *n_groups = static_cast<int32_t>(n_ships);
         return fail(h, SDBE_ERR_CAPACITY, "output has room for fewer groups than ship");
     }
     if (n_ships > 0 && !out) return fail(h, SDBE_ERR_ARG, "null output");
-    DeviceGuard g(h->cfg.device);
-    if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
-    int rc = ensure_ring(h);
+    rc = ensure_ring(h);
     if (rc) return rc;
-    cudaStream_t st = h->stream;
-    if (n_packets > 0) {
-        rc = grow(h, &h->ing_batch, &h->ing_batch_bytes, n_packets * kPktBytes, "ingest batch");
-        if (!rc) rc = grow(h, &h->ing_accept, &h->ing_accept_bytes, n_packets, "ingest mask");
+    if (n_pk > 0) {
+        if (!dev_pkts) {  // plain host packets
+            rc = grow(h, &h->ing_batch, &h->ing_batch_bytes, n_pk * kPktBytes, "ingest batch");
+            if (rc) return rc;
+            SDBE_CK(h, cudaMemcpyAsync(h->ing_batch, packets, n_pk * kPktBytes, cudaMemcpyHostToDevice, st));
+            dev_pkts = h->ing_batch;
+        }
+        rc = grow(h, &h->ing_accept, &h->ing_accept_bytes, n_pk, "ingest mask");
         if (rc) return rc;
-        SDBE_CK(h, cudaMemcpyAsync(h->ing_batch, pk, n_packets * kPktBytes, cudaMemcpyHostToDevice, st));
-        SDBE_CK(h, cudaMemcpyAsync(h->ing_accept, accept.data(), n_packets, cudaMemcpyHostToDevice, st));
+        SDBE_CK(h, cudaMemcpyAsync(h->ing_accept, accept.data(), n_pk, cudaMemcpyHostToDevice, st));
     }
     uint8_t *dev_out = out_target(h, out, n_ships, flags, &rc);
     if (rc) return rc;
-    rc = run_device(h, p, h->ing_batch, n_packets, h->ing_accept, ships, touched, dev_out, flags, st);
+    rc = run_device(h, p, dev_pkts, n_pk, h->ing_accept, ships, touched, dev_out, flags, st);
     if (rc) return rc;
     commit(h, p);
+    if (pac8) h->reform = reform;
     return finish(h, out, dev_out, n_ships, flags, st, n_groups);
 }
 
@@ -281,6 +340,12 @@ int sdbe_ingest_flush(sdbe_resampler *h, void *out, int64_t out_groups, uint32_t
     if (rc) return rc;
     commit(h, p);
     return finish(h, out, dev_out, n_ships, flags, h->stream, n_groups);
+}
+
+int sdbe_ingest_reform_state(const sdbe_resampler *h, sdbe_reform_state *st) {
+    if (!h || !st) return SDBE_ERR_ARG;
+    *st = h->reform;
+    return SDBE_OK;
 }
 
 int sdbe_ingest_get_stats(const sdbe_resampler *h, sdbe_ingest_stats *st) {

@@ -38,5 +38,9 @@ cudaError_t launch_save_leftover(const uint32_t *, int64_t, const uint32_t *, in
                                  uint32_t *, cudaStream_t);
 cudaError_t launch_vdif_headers(void *, int64_t, int64_t, uint32_t, uint32_t, uint64_t, uint32_t, uint32_t, uint32_t,
                                 uint32_t, cudaStream_t);
+cudaError_t launch_unpack_8pac(const void *, int64_t, void *, cudaStream_t);
+cudaError_t launch_beng_reform(void *, int64_t, const sdbe_reform_state &, sdbe_reform_state *, uint32_t *,
+                               cudaStream_t);
+cudaError_t launch_gather_headers(const void *, int64_t, uint32_t *, cudaStream_t);
 
 }  // namespace sdbe

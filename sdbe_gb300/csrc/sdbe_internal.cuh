@@ -17,6 +17,7 @@ constexpr int kSnapsPerFrame = 128;              // BENG_SNAPSHOTS
 constexpr int kPktsPerFrame = 2048;              // VDIF_PER_BENG
 constexpr int kPktBytes = 1056;                  // VDIF_BYTE_SIZE
 constexpr int kPktWords = kPktBytes / 4;
+constexpr int kPac8Bytes = kPktBytes + 7 * (8 + kPktBytes);  // sizeof(vdif_8pac_packet_t) = 8504
 constexpr int kBatchSnaps = 143;                 // RESAMPLE_BATCH_SNAPSHOTS
 constexpr int kChunks = 128;                     // FFT_BATCHES_SWARM_R2C
 constexpr int kNA = 32768;                       // FFT_SIZE_SWARM_C2R

@@ -184,34 +184,50 @@ class Resampler:
         pkt = N.OUT_PKT_BYTES if framed else N.OUT_PKT_DATA_BYTES
         return np.empty((n_groups, 2, self.GROUP_PACKETS_OUT, pkt), np.uint8)
 
-    def ingest(self, packets, out=None, out_groups: int | None = None, framed: bool = False):
-        """Offer received packets (host ``[n, 1056]`` uint8) to the group ring.
+    def ingest(self, packets, out=None, out_groups: int | None = None, framed: bool = False,
+               pac8: bool = False, n_packets: int | None = None):
+        """Offer received packets to the group ring.
 
+        ``packets``: ``[n, 1056]`` uint8 B-engine packets, or with ``pac8``
+        ``[n, 8504]`` 8pac units carrying new-format headers (unpacked and
+        reformed on the device first); host (numpy) or device memory.
         Returns ``(groups, n)``: the ``n`` groups this batch shipped, as
         ``[n, 2, 16384, 8192]`` payloads (8224-B frames when ``framed``).
         Without ``out`` a host array is sized from the packet count and grown
         once if the batch ships more.
         """
-        pk = np.ascontiguousarray(packets, dtype=np.uint8).reshape(-1, N.IN_PKT_BYTES)
-        flags = N.OUT_FRAMED if framed else 0
+        unit = N.PAC8_BYTES if pac8 else N.IN_PKT_BYTES
+        flags = (N.OUT_FRAMED if framed else 0) | (N.IN_8PAC if pac8 else 0)
+        if _is_device(packets):
+            if n_packets is None:
+                n_packets = _nbytes(packets) // unit
+            src = packets
+        else:
+            src = np.ascontiguousarray(packets, dtype=np.uint8).reshape(-1, unit)
+            n_packets = src.shape[0]
+            flags |= N.IN_HOST
         auto = out is None
         if auto:
-            out_groups = pk.shape[0] // 292864 + 1 if out_groups is None else out_groups
+            n_pk = n_packets * (8 if pac8 else 1)
+            out_groups = n_pk // 292864 + 1 if out_groups is None else out_groups
             out = self._group_out(out_groups, framed)
         elif out_groups is None:
             out_groups = int(out.shape[0])
         if not _is_device(out):
             flags |= N.OUT_HOST
         n = C.c_int32(0)
-        rc = self._lib.sdbe_ingest(self._h, pk.ctypes.data, pk.shape[0], _addr(out), out_groups, flags,
-                                   C.byref(n))
+        rc = self._lib.sdbe_ingest(self._h, _addr(src), n_packets, _addr(out), out_groups, flags, C.byref(n))
         if rc == N.ERR_CAPACITY and auto:  # n holds the number of groups the batch ships
             out_groups = n.value
             out = self._group_out(out_groups, framed)
-            rc = self._lib.sdbe_ingest(self._h, pk.ctypes.data, pk.shape[0], _addr(out), out_groups, flags,
-                                       C.byref(n))
+            rc = self._lib.sdbe_ingest(self._h, _addr(src), n_packets, _addr(out), out_groups, flags, C.byref(n))
         N.check(rc, self._h)
         return (out[:n.value] if isinstance(out, np.ndarray) else out), n.value
+
+    def ingest_reform_state(self) -> N.ReformState:
+        st = N.ReformState()
+        N.check(self._lib.sdbe_ingest_reform_state(self._h, C.byref(st)), self._h)
+        return st
 
     def ingest_flush(self, out=None, out_groups: int = 4, framed: bool = False):
         """Ship every open group that holds packets (end of stream)."""

@@ -118,3 +118,62 @@ def generate(spec: StreamSpec, out: np.ndarray | None = None, n_threads: int = 0
     m = lib.sdbe_synth_impair(raw.ctypes.data, n, dst.ctypes.data, spec.seed + frame_offset,
                               spec.drop_frac, spec.reorder_frac, spec.reorder_max)
     return dst[:m]
+
+
+# -- 8pac input format ------------------------------------------------------
+PAC8_BYTES = 1056 + 7 * (8 + 1056)   # one 8pac unit: packet, then 7 x (8-B VTP + packet)
+CLK_PER_SEC = 286000000              # SWARM FPGA clock
+BFRAME_CLK = 262144                  # clocks per B-frame
+
+
+def new_format_words(c, f, sec, clk):
+    """(w4, w5) of the new-format B-engine header: a 53-bit timestamp
+    (sec << 29 | clk) split as b_upper (w4) and b_lower (w5 bits 11-31), with
+    c in w5 bits 0-7 and f in bits 8-10."""
+    ts = (np.asarray(sec, np.int64) << 29) | np.asarray(clk, np.int64)
+    w4 = (ts >> 21).astype(np.uint32)
+    w5 = (np.asarray(c, np.int64) | (np.asarray(f, np.int64) << 8) | ((ts & 0x1FFFFF) << 11)).astype(np.uint32)
+    return w4, w5
+
+
+def to_8pac(packets, t0_sec: int, t0_clk: int, b_ref: int, seed: int = 0, psn0: int = 0, df0: int = 0):
+    """Packets with old-format headers (b in w4/w5) -> 8pac units whose
+    headers carry the timestamp of frame b (t0 + (b - b_ref) B-frames) in the
+    new format.  The first packet of each unit has df_len = 8504/8, the
+    unit's data-frame number and psn; the other 7 and the VTP prefixes carry
+    seeded garbage in the fields the unpack rewrites.  ``len(packets)`` must
+    be a multiple of 8."""
+    p = np.ascontiguousarray(packets, dtype=np.uint8).reshape(-1, 1056)
+    n = p.shape[0]
+    if n % 8:
+        raise ValueError("packet count must be a multiple of 8")
+    rng = np.random.default_rng(seed)
+    w = p.view("<u4").reshape(n, 264).copy()
+    c = w[:, 5] & 0xFF
+    f = (w[:, 5] >> 16) & 0xFF
+    b = ((w[:, 4].astype(np.int64) << 8) | (w[:, 5].astype(np.int64) >> 24))
+    t = t0_sec * np.int64(CLK_PER_SEC) + t0_clk + (b - b_ref) * BFRAME_CLK
+    w[:, 4], w[:, 5] = new_format_words(c, f & 7, t // CLK_PER_SEC, t % CLK_PER_SEC)
+    units = n // 8
+    w = w.reshape(units, 8, 264)
+    garbage = rng.integers(0, 2**32, (units, 8, 4), dtype=np.uint64).astype(np.uint32)
+    w[:, 1:, 1] = (w[:, 1:, 1] & np.uint32(0xFF000000)) | (garbage[:, 1:, 0] & np.uint32(0xFFFFFF))
+    w[:, 1:, 2] = (w[:, 1:, 2] & np.uint32(0xFF000000)) | (garbage[:, 1:, 1] & np.uint32(0xFFFFFF))
+    w[:, 1:, 6] = garbage[:, 1:, 2]
+    w[:, 1:, 7] = garbage[:, 1:, 3]
+    w[:, 1:, 0] ^= (garbage[:, 1:, 0] & np.uint32(1 << 31))
+    k = np.arange(units, dtype=np.int64)
+    w[:, 0, 1] = (w[:, 0, 1] & np.uint32(0xFF000000)) | ((df0 + k) & 0xFFFFFF).astype(np.uint32)
+    w[:, 0, 2] = (w[:, 0, 2] & np.uint32(0xFF000000)) | np.uint32(PAC8_BYTES // 8)
+    psn = (psn0 + k).astype(np.uint64)
+    w[:, 0, 6] = (psn & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    w[:, 0, 7] = (psn >> np.uint64(32)).astype(np.uint32)
+    out = np.empty((units, PAC8_BYTES), np.uint8)
+    pk = w.view(np.uint8).reshape(units, 8, 1056)
+    out[:, :1056] = pk[:, 0]
+    vtp = rng.integers(0, 256, (units, 7, 8), dtype=np.uint8)
+    for j in range(7):
+        o = 1056 + j * 1064
+        out[:, o:o + 8] = vtp[:, j]
+        out[:, o + 8:o + 1064] = pk[:, j + 1]
+    return out

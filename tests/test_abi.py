@@ -50,6 +50,8 @@ def test_struct_layouts(built):
     assert C.sizeof(built.Config) == 16 * 4
     assert C.sizeof(built.State) == 4 * 2 * 2 + 4 * 4 + 8 + 4 * 4 + 6 * 4
     assert C.sizeof(built.Result) == 6 * 8
+    assert C.sizeof(built.ReformState) == 48
+    assert C.sizeof(built.IngestStats) == 12 * 8
 
 
 def test_constants_match_header(built):
@@ -60,6 +62,7 @@ def test_constants_match_header(built):
     assert d["SDBE_BATCH_SNAPSHOTS"] == built.BATCH_SNAPSHOTS
     assert d["SDBE_OK"] == built.OK and d["SDBE_ERR_CAPACITY"] == built.ERR_CAPACITY
     assert d["SDBE_IN_HOST"] == built.IN_HOST and d["SDBE_OUT_FRAMED"] == built.OUT_FRAMED
+    assert d["SDBE_IN_8PAC"] == built.IN_8PAC and d["SDBE_PAC8_BYTES"] == built.PAC8_BYTES
 
 
 def test_error_paths_without_gpu(built):
@@ -77,6 +80,15 @@ def test_error_paths_without_gpu(built):
     assert lib.sdbe_quantize2bit(None, None, 17, 1.0, 0.0, None) == built.ERR_ARG
     assert lib.sdbe_reorder_mar2015(None, 1, None, None) == built.ERR_ARG
     assert lib.sdbe_process(None, None, 0, 0, 0, None, 0, 0, None, None) == built.ERR_ARG
+    assert lib.sdbe_unpack_8pac(None, 1, None, None) == built.ERR_ARG
+    assert lib.sdbe_unpack_8pac(8, 1, 12, None) == built.ERR_ARG          # misaligned
+    assert "aligned" in built.last_error()
+    assert lib.sdbe_beng_reform(None, None, 0, None) == built.ERR_ARG
+    st = built.ReformState()
+    st.bprev = 77
+    assert lib.sdbe_reform_init(C.byref(st)) == built.OK
+    assert (st.t0_sec, st.t0_clk, st.tprev_sec, st.tprev_clk, st.bprev, st.slow_tiles) == (-1, -1, -1, -1, -1, 0)
+    assert lib.sdbe_beng_reform(C.byref(st), None, 0, None) == built.OK   # nothing to do
 
 
 def test_header_template_matches_oracle(built):
