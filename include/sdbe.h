@@ -344,6 +344,19 @@ int sdbe_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride_bytes, ui
                       uint32_t df0, uint64_t psn0, uint32_t ref_epoch, uint32_t station_id,
                       uint32_t bdc_sideband, uint32_t rx_sideband, void *stream);
 
+/* Inverse polyphase filter bank for PFB-mode spectra (Shaw's least-squares
+ * inversion, software/prototyping/cuda/pfb_inverse.cu:213-488, with the
+ * Hamming window of :51-53 over ntap*32768 samples): complex64
+ * [nblock][16385] -> float [nblock+ntap-1][32768], the time blocks whose
+ * forward PFB (pfb_inverse.cu:173-207) gives the spectra, minimum-norm where
+ * the spectra leave them free.  Pseudo time stream by FP32 C2R, banded
+ * P P^T solve and projection in FP64 (the systems are ill-conditioned).
+ * 2 <= ntap <= 8.  The prototype compiles its solve out (#if 0); this
+ * restates the method it sets up.  Allocates scratch of nblock*(4 + 8*ntap)*
+ * 32768 bytes on the stream. */
+int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t nblock, int32_t ntap, float *out,
+                     void *stream);
+
 /* Mar-2015 snapshot reorder on packed spectra (prototyping/cuda/reorder.py:13-43):
  * [n_frames][128][2048 u32] -> [n_frames-1][128][2048 u32]. */
 int sdbe_reorder_mar2015(const uint32_t *spec_in, int32_t n_frames, uint32_t *spec_out, void *stream);

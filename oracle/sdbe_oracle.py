@@ -774,3 +774,83 @@ def reform_t0(st: ReformState):
     """``get_beng_t0`` (beng_reform.c:113-126): T0 one B-frame earlier
     (SWARM_TIMESTAMP_OFF_BY_BENG = -1)."""
     return beng_timestamp_decrement(*st.t0)
+
+
+# ---------------------------------------------------------------------------
+# Polyphase filter bank and its inverse (PFB-mode SWARM data)
+# ---------------------------------------------------------------------------
+def hamming_pfb(n, m):
+    """``hamming`` of prototyping/cuda/pfb_inverse.cu:51-53: 0.54 - 0.46 cos(2 pi n / (m-1))."""
+    return 0.54 - 0.46 * np.cos(2.0 * np.pi * np.asarray(n, np.float64) / (m - 1.0))
+
+
+def forward_pfb(x, lblock, ntap=4):
+    """PFB spectra of a real time stream, as ``pfb`` builds them
+    (pfb_inverse.cu:173-207): block i windows samples [i*L, i*L + ntap*L)
+    with hamming(n, ntap*L), takes the rFFT of length ntap*L and keeps every
+    ntap-th bin (``decimate``, :57-64) -> [nblock][L/2+1] complex, nblock =
+    len(x)/L - (ntap-1)."""
+    x = np.asarray(x, np.float64)
+    nblock = x.size // lblock - (ntap - 1)
+    w = hamming_pfb(np.arange(ntap * lblock), ntap * lblock)
+    idx = np.arange(nblock)[:, None] * lblock + np.arange(ntap * lblock)[None, :]
+    f = np.fft.rfft(x[idx] * w, axis=1)
+    return f[:, ::ntap][:, :lblock // 2 + 1]
+
+
+def pfb_band(lblock, ntap=4):
+    """Per phase p: the P taps w[t*L + p] (t = 0..ntap-1) and the band of
+    P P^T, a[d] = sum_k w[(k+d)L + p] w[kL + p] (pfb_inverse.cu:261-300)."""
+    w = hamming_pfb(np.arange(ntap * lblock), ntap * lblock).reshape(ntap, lblock)
+    a = np.stack([(w[d:] * w[:ntap - d]).sum(axis=0) for d in range(ntap)])
+    return w, a
+
+
+def banded_ldl_solve(a, y):
+    """Solve T z = y for every column p, T the symmetric banded Toeplitz
+    matrix with band a[0..b] (a[:, p] per column), by LDL^T, vectorised over
+    p (FP64).  y: [n][P]."""
+    b = a.shape[0] - 1
+    n, P = y.shape
+    L = np.zeros((n, b + 1, P))          # L[m, k] = L[m][m-k], k = 1..b
+    d = np.zeros((n, P))
+    for m in range(n):
+        for k in range(b, 0, -1):
+            j = m - k
+            if j < 0:
+                continue
+            s = a[k].copy()
+            for q in range(k + 1, b + 1):     # sum over columns left of j
+                if m - q >= 0 and j - (m - q) <= b and j - (m - q) > 0:
+                    s -= L[m, q] * d[m - q] * L[j, j - (m - q)]
+            L[m, k] = s / d[j]
+        d[m] = a[0] - sum(L[m, k] ** 2 * d[m - k] for k in range(1, b + 1) if m - k >= 0)
+    w = np.zeros((n, P))
+    for m in range(n):
+        w[m] = y[m] - sum(L[m, k] * w[m - k] for k in range(1, b + 1) if m - k >= 0)
+    v = w / d
+    z = np.zeros((n, P))
+    for m in range(n - 1, -1, -1):
+        z[m] = v[m] - sum(L[m + k, k] * z[m + k] for k in range(1, b + 1) if m + k < n)
+    return z
+
+
+def inverse_pfb(spec, ntap=4):
+    """Time stream from PFB spectra by Shaw's least-squares inversion, the
+    method of prototyping/cuda/pfb_inverse.cu:213-488: the pseudo time stream
+    y = irfft(S) (the C2R then the 1/L scale, :395-418), per phase p the
+    banded solve (P P^T) z = y[:, p] (:420-430) and the projection
+    x[:, p] = P^T z (:432-440), with P[i][j] = w[(j-i)L + p] for
+    0 <= j-i < ntap.  Output [nblock + ntap - 1][L] (FP64).  The published
+    method is Shaw's pfb-inverse (github.com/jrs65/pfb-inverse, unpinned);
+    the prototype compiles its solve and projection out (``#if 0``)."""
+    spec = np.asarray(spec, np.complex128)
+    lblock = 2 * (spec.shape[1] - 1)
+    nblock = spec.shape[0]
+    y = np.fft.irfft(spec, n=lblock, axis=1)
+    w, a = pfb_band(lblock, ntap)
+    z = banded_ldl_solve(a, y)
+    x = np.zeros((nblock + ntap - 1, lblock))
+    for t in range(ntap):
+        x[t:t + nblock] += w[t][None, :] * z
+    return x

@@ -100,6 +100,7 @@ SIGNATURES = {
     "sdbe_reform_init": (C.c_int, [C.POINTER(ReformState)]),
     "sdbe_unpack_8pac": (C.c_int, [vp, i64, vp, vp]),
     "sdbe_beng_reform": (C.c_int, [C.POINTER(ReformState), vp, i64, vp]),
+    "sdbe_inverse_pfb": (C.c_int, [vp, vp, i64, i32, vp, vp]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

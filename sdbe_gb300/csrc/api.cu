@@ -72,6 +72,7 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->ing_raw);
     cudaFree(h->ing_hdr);
     cudaFree(h->reform_dev);
+    cudaFree(h->ipfb_tab);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
     cudaFree(h->pay);
@@ -635,7 +636,7 @@ int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int3
     if (!h || n_chunks < 0 || skip_chan < 0 || skip_chan > kMaxSkip || (n_chunks > 0 && (!in_c64 || !out)))
         return fail(h, SDBE_ERR_ARG, "bad argument");
     DeviceGuard g(h->cfg.device);
-    SDBE_CK(h, launch_r2dbe_c2r(in_c64, n_chunks, skip_chan, out, h->tw, pick(h, stream)));
+    SDBE_CK(h, launch_r2dbe_c2r(in_c64, kMB + 1, n_chunks, skip_chan, out, h->tw, pick(h, stream)));
     return SDBE_OK;
 }
 

@@ -62,6 +62,8 @@ struct sdbe_resampler {
     int64_t ing_hdr_bytes = 0;
     sdbe_reform_state reform{-1, -1, -1, -1, -1, 0, 0, 0};  // 8pac batches: reform state
     sdbe_reform_state *reform_dev = nullptr;                // kernel's output state
+    double *ipfb_tab = nullptr;   // inverse PFB: [2][ntap][32768] band of P P^T and P taps (FP64)
+    int ipfb_ntap = 0;
     int64_t b_first = -1;
     int64_t ing_ref = 0;
     int64_t g_count[4] = {0, 0, 0, 0};

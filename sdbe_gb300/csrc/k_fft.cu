@@ -459,7 +459,8 @@ __global__ void __launch_bounds__(kNTB, 1)
 
 // R2dbeC2R alone: complex64 [n][18305] from bin skip -> float [n][32768].
 __global__ void __launch_bounds__(kNTB, 1)
-    k_r2dbe_c2r(const float2 *__restrict__ in, int64_t n_chunks, int skip, float *__restrict__ out, Twiddles tw) {
+    k_r2dbe_c2r(const float2 *__restrict__ in, int64_t in_stride, int64_t n_chunks, int skip, float *__restrict__ out,
+                Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(kNTB, 1)
     const float2 wc = conjf2(__ldg(tw.w32768 + tid));
     for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         __syncthreads();
-        const float2 *y = in + c * (kMB + 1) + skip;
+        const float2 *y = in + c * in_stride + skip;
         auto zin = [&](float2 *v) {
             for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
                 constexpr int r = decltype(rc)::value;
@@ -691,11 +692,11 @@ cudaError_t launch_swarm_r2c(const float *in, int64_t n_chunks, void *out, const
     return cudaGetLastError();
 }
 
-cudaError_t launch_r2dbe_c2r(const void *in, int64_t n_chunks, int skip, float *out, const Twiddles &tw,
-                             cudaStream_t st) {
+cudaError_t launch_r2dbe_c2r(const void *in, int64_t in_stride, int64_t n_chunks, int skip, float *out,
+                             const Twiddles &tw, cudaStream_t st) {
     if (n_chunks <= 0) return cudaSuccess;
-    k_r2dbe_c2r<<<persistent_grid(n_chunks), kNTB, kSmemB, st>>>(static_cast<const float2 *>(in), n_chunks, skip, out,
-                                                                  tw);
+    k_r2dbe_c2r<<<persistent_grid(n_chunks), kNTB, kSmemB, st>>>(static_cast<const float2 *>(in), in_stride, n_chunks,
+                                                                  skip, out, tw);
     return cudaGetLastError();
 }
 

@@ -25,7 +25,7 @@ cudaError_t launch_swarm_c2r(const uint32_t *, int64_t, int64_t, int64_t, int, f
 cudaError_t launch_resample(int, const float *, int64_t, int, int64_t, int, const ResampleOut &, const Twiddles &,
                             cudaStream_t);
 cudaError_t launch_swarm_r2c(const float *, int64_t, void *, const Twiddles &, cudaStream_t);
-cudaError_t launch_r2dbe_c2r(const void *, int64_t, int, float *, const Twiddles &, cudaStream_t);
+cudaError_t launch_r2dbe_c2r(const void *, int64_t, int64_t, int, float *, const Twiddles &, cudaStream_t);
 cudaError_t launch_finalize_thresholds(const double *, int, int, float *, cudaStream_t);
 cudaError_t launch_quantize_chunks(const float *, int64_t, int64_t, const float *, uint8_t *, int64_t, int64_t,
                                    int64_t, int64_t, cudaStream_t);
