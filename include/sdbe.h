@@ -235,6 +235,31 @@ int sdbe_beng_reform(sdbe_reform_state *st, void *pkts, int64_t n_pkts, void *st
 /* The reform state of a handle's sdbe_ingest stream (SDBE_IN_8PAC batches). */
 int sdbe_ingest_reform_state(const sdbe_resampler *h, sdbe_reform_state *st);
 
+/* Several packet streams in one pass: each handle keeps its own state
+ * (thresholds, carry, header counters, alignment) and its own descriptor, as
+ * if sdbe_process were called on each in turn, but the FFT work of all of
+ * them runs in shared launches: the first-batch threshold path of every
+ * handle that needs it in one pair of launches, then waves in which one
+ * stage-A and one stage-BC launch cover every handle's next batches (wave =
+ * the smallest wave_batches of the handles).  Outputs equal the per-handle
+ * calls bit for bit.  1 <= n <= 32 distinct handles on one device; flags and
+ * stream apply to all (NULL: the first handle's stream); results (optional)
+ * has n entries.  Every descriptor is checked before any work is queued.
+ * With device buffers, no SDBE_SYNC/ASYNC and results NULL, the call issues
+ * only stream-ordered work on `stream` and can be captured into a CUDA graph
+ * (the handles' host-side state advances once, at capture). */
+typedef struct sdbe_stream_desc {
+    const void *packets;
+    int64_t n_packets;
+    int32_t n_frames;
+    int32_t reserved;
+    uint64_t b_zero;
+    void *out;
+    int64_t out_bytes;
+} sdbe_stream_desc;
+int sdbe_process_multi(sdbe_resampler *const *handles, const sdbe_stream_desc *descs, int32_t n, uint32_t flags,
+                       void *stream, sdbe_result *results);
+
 /* Wait for all work the handle issued (its streams and the last stream passed
  * to sdbe_process). */
 int sdbe_sync(sdbe_resampler *h);

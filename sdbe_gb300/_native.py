@@ -72,6 +72,11 @@ class ReformState(C.Structure):
                 ("reserved", C.c_int64)]
 
 
+class StreamDesc(C.Structure):
+    _fields_ = [("packets", C.c_void_p), ("n_packets", C.c_int64), ("n_frames", C.c_int32), ("reserved", C.c_int32),
+                ("b_zero", C.c_uint64), ("out", C.c_void_p), ("out_bytes", C.c_int64)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("sigma", C.c_double), ("level", C.c_double), ("n_tones", C.c_int32),
                 ("tone_channel", C.c_int32 * 8), ("tone_amp", C.c_double * 8), ("tone_phase", C.c_double * 8),
@@ -101,6 +106,7 @@ SIGNATURES = {
     "sdbe_unpack_8pac": (C.c_int, [vp, i64, vp, vp]),
     "sdbe_beng_reform": (C.c_int, [C.POINTER(ReformState), vp, i64, vp]),
     "sdbe_inverse_pfb": (C.c_int, [vp, vp, i64, i32, vp, vp]),
+    "sdbe_process_multi": (C.c_int, [C.POINTER(vp), C.POINTER(StreamDesc), i32, u32, vp, C.POINTER(Result)]),
     "sdbe_profile_enable": (C.c_int, [vp, i32]),
     "sdbe_profile_read": (C.c_int, [vp, C.POINTER(Profile)]),
     "sdbe_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),

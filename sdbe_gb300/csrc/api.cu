@@ -118,6 +118,349 @@ int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const cha
     return SDBE_OK;
 }
 
+
+// One sdbe_process call, split so that several handles can share the FFT
+// launches (sdbe_process_multi): plan (checks, no side effects), prepare
+// (staging, unpack, headers), the FFT chain, complete (alignment, carry, sync).
+struct CallPlan {
+    sdbe_resampler *h = nullptr;
+    cudaStream_t st = nullptr;
+    const void *packets = nullptr;
+    int64_t n_packets = 0;
+    int32_t n_frames = 0;
+    uint64_t b_zero = 0;
+    void *out = nullptr;
+    uint32_t flags = 0;
+    bool aligned = false, framed = false, host_in = false, host_out = false;
+    int64_t n_frames_out = 0;  // B-frames of spectra this call adds (Mar-2015 holds one back)
+    int64_t n_batches = 0, n_pay = 0, n_out = 0, pkt_stride = 0, payload_off = 0, out_pol_stride = 0;
+    uint32_t a_secs = 0, a_df = 0, a_epoch = 0;
+    uint64_t a_psn = 0;
+    int64_t a_skip = 0, a_new_left = 0, a_skip_after = 0;
+    sdbe_resampler::Stage *sg = nullptr;
+    uint8_t *dev_out = nullptr;
+    PayloadTarget pt{};
+};
+
+int plan_call(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames, uint64_t b_zero, void *out,
+              int64_t out_bytes, uint32_t flags, cudaStream_t st, CallPlan &c) {
+    if (n_frames < 0 || n_frames > h->cfg.max_frames)
+        return fail(h, SDBE_ERR_CAPACITY, "n_frames outside [0, max_frames]");
+    if (n_packets < 0 || (n_packets > 0 && !packets)) return fail(h, SDBE_ERR_ARG, "bad packets");
+    c.h = h;
+    c.st = st;
+    c.packets = packets;
+    c.n_packets = n_packets;
+    c.n_frames = n_frames;
+    c.b_zero = b_zero;
+    c.out = out;
+    c.flags = flags;
+    c.aligned = (flags & SDBE_OUT_ALIGNED) != 0;
+    c.framed = (flags & (SDBE_OUT_FRAMED | SDBE_OUT_ALIGNED)) != 0;
+    c.n_frames_out = frames_out(h, n_frames);
+    c.n_batches = batches_for(h, n_frames);
+    c.n_pay = c.n_batches * kChunks;  // payload packets per pol the FFTs produce
+    // Time alignment (vdif_out_net_thread.c:199-317): first block after a
+    // template starts on the next second boundary if it would cross one and
+    // skips the sub-packet offset; every block frames whole packets of
+    // [leftover | payload] and carries the rest.
+    c.a_secs = h->secs;
+    c.a_df = h->df;
+    c.a_psn = h->psn;
+    c.a_epoch = h->ref_epoch;
+    int64_t a_skip_total = h->skip_pending;
+    c.n_out = c.n_pay;
+    if (c.aligned) {
+        if (h->align_pending) {
+            c.a_secs = h->tmpl.secs_inre;
+            c.a_df = h->tmpl.df_num_insec;
+            int64_t skip_frames = 0;
+            if (static_cast<int64_t>(c.a_df) > 125000 - c.n_pay) {
+                skip_frames = 125000 - static_cast<int64_t>(c.a_df);
+                c.a_df = 0;
+                c.a_secs += 1;
+            }
+            const double skip_ps = static_cast<double>(h->tmpl.ps_early + 3715791ull);
+            const double skip_samples = std::floor(skip_ps * 4096e6 / 1e12);
+            a_skip_total += static_cast<int64_t>(std::floor(skip_samples / (8.0 / 2.0) / 4.0)) + skip_frames * kOutWords;
+            c.a_psn = 1;
+            c.a_epoch = h->tmpl.ref_epoch;
+        }
+        const int64_t stream_len = h->n_left + c.n_pay * kOutWords - a_skip_total;
+        if (stream_len < 0) {
+            c.n_out = 0;
+            c.a_skip_after = -stream_len;
+        } else {
+            c.a_skip = a_skip_total;
+            c.n_out = stream_len / kOutWords;
+            c.a_new_left = stream_len - c.n_out * kOutWords;
+        }
+    }
+    c.pkt_stride = c.framed ? kOutPkt : kOutPktData;
+    c.payload_off = c.framed ? 32 : 0;
+    c.out_pol_stride = c.n_out * c.pkt_stride;
+    if (out_bytes < 2 * c.out_pol_stride) return fail(h, SDBE_ERR_CAPACITY, "output buffer too small");
+    if (c.n_out > 0 && !out) return fail(h, SDBE_ERR_ARG, "null output");
+    if (h->cfg.threshold_mode == SDBE_THRESH_FIXED && !h->thresholds_set && c.n_batches > 0)
+        return fail(h, SDBE_ERR_STATE, "fixed threshold mode needs sdbe_set_state first");
+    c.host_in = (flags & SDBE_IN_HOST) && n_packets > 0;
+    c.host_out = (flags & SDBE_OUT_HOST) && c.n_out > 0;
+    if (!c.host_in && n_packets > 0 && (reinterpret_cast<uintptr_t>(packets) & 15u))
+        return fail(h, SDBE_ERR_ARG, "device packet buffer must be 16-byte aligned");
+    if (!c.host_out && c.n_out > 0 && (reinterpret_cast<uintptr_t>(out) & 15u))
+        return fail(h, SDBE_ERR_ARG, "device output buffer must be 16-byte aligned");
+    return SDBE_OK;
+}
+
+// Payload packets [lo, hi) of both pols are final: send them to the host on
+// the copy stream while the next wave computes.
+int ship_call(CallPlan &c, int64_t lo, int64_t hi) {
+    sdbe_resampler *h = c.h;
+    if (!c.host_out || hi <= lo) return SDBE_OK;
+    SDBE_CK(h, cudaEventRecord(h->wave_ev, c.st));
+    SDBE_CK(h, cudaStreamWaitEvent(h->copy_out, h->wave_ev, 0));
+    SDBE_CK(h, cudaMemcpy2DAsync(static_cast<uint8_t *>(c.out) + lo * c.pkt_stride, c.out_pol_stride,
+                                 c.dev_out + lo * c.pkt_stride, c.out_pol_stride, (hi - lo) * c.pkt_stride, 2,
+                                 cudaMemcpyDeviceToHost, h->copy_out));
+    return SDBE_OK;
+}
+
+int prepare_call(CallPlan &c) {
+    sdbe_resampler *h = c.h;
+    cudaStream_t st = c.st;
+    c.sg = &h->stage[h->stage_idx];
+    sdbe_resampler::Stage &sg = *c.sg;
+    if (c.host_in || c.host_out) h->stage_idx ^= 1;
+    const uint8_t *src = static_cast<const uint8_t *>(c.packets);
+    if (c.host_in) {
+        int rc = grow(h, &sg.pkt, &sg.pkt_bytes, c.n_packets * kPktBytes, "packet staging");
+        if (rc) return rc;
+        // the slot's previous packets must have been unpacked before they are overwritten
+        SDBE_CK(h, cudaStreamWaitEvent(h->copy_in, sg.pkt_free, 0));
+        SDBE_CK(h, cudaMemcpyAsync(sg.pkt, c.packets, c.n_packets * kPktBytes, cudaMemcpyHostToDevice, h->copy_in));
+        SDBE_CK(h, cudaEventRecord(sg.pkt_ready, h->copy_in));
+        SDBE_CK(h, cudaStreamWaitEvent(st, sg.pkt_ready, 0));
+        src = sg.pkt;
+    }
+    c.dev_out = static_cast<uint8_t *>(c.out);
+    if (c.host_out) {
+        int rc = grow(h, &sg.out, &sg.out_bytes, 2 * c.out_pol_stride, "output staging");
+        if (rc) return rc;
+        // the slot's previous payloads must have left for the host before they are overwritten
+        SDBE_CK(h, cudaStreamWaitEvent(st, sg.out_free, 0));
+        c.dev_out = sg.out;
+    }
+    // Where the FFT waves write: the output itself, or the plain payload
+    // stream that the alignment step frames afterwards.
+    c.pt = PayloadTarget{c.dev_out, c.out_pol_stride, c.pkt_stride, c.payload_off};
+    if (c.aligned && c.n_pay > 0) {
+        int rc = grow(h, &h->pay, &h->pay_bytes, 2 * c.n_pay * kOutPktData, "payload stream");
+        if (rc) return rc;
+        c.pt = PayloadTarget{h->pay, c.n_pay * kOutPktData, kOutPktData, 0};
+    }
+    const int map = h->cfg.channel_map;
+    const bool mar = map == SDBE_MAP_MAR2015;
+    const int32_t n_frames = c.n_frames;
+    if (n_frames > 0) {
+        // Mar-2015: unpack after the held frame in `raw`; otherwise straight
+        // into the snapshot stream after the carried snapshots.
+        uint32_t *dst = mar ? h->raw : h->spec;
+        const int64_t dst_stride = mar ? h->raw_pol_stride : h->spec_pol_stride;
+        const int64_t snap0 = mar ? static_cast<int64_t>(h->raw_carry) * kSnapsPerFrame : h->carry;
+        SDBE_CK(h, cudaMemsetAsync(h->bitmap, 0, static_cast<size_t>(n_frames) * 256, st));
+        SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
+        SDBE_CK(h, launch_unpack(src, c.n_packets, c.b_zero, n_frames, map, dst, dst_stride, snap0, h->bitmap, h->counts,
+                                 h->counts + h->cfg.max_frames, st));
+        if (c.host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
+        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, dst, dst_stride, snap0, st));
+        h->launches += c.n_packets > 0 ? 2 : 1;
+        if (mar) {
+            const int n_in = h->raw_carry + n_frames;
+            for (int pol = 0; pol < 2 && n_in >= 2; ++pol) {
+                SDBE_CK(h, launch_reorder_mar2015(h->raw + pol * h->raw_pol_stride, n_in,
+                                                  h->spec + pol * h->spec_pol_stride + h->carry * kGroups, st));
+                h->launches += 1;
+            }
+            if (n_in >= 2) {  // hold the newest frame
+                for (int pol = 0; pol < 2; ++pol) {
+                    uint32_t *base = h->raw + pol * h->raw_pol_stride;
+                    SDBE_CK(h, cudaMemcpyAsync(base, base + static_cast<int64_t>(n_in - 1) * kSnapsPerFrame * kGroups,
+                                               static_cast<size_t>(kSnapsPerFrame) * kGroups * sizeof(uint32_t),
+                                               cudaMemcpyDeviceToDevice, st));
+                }
+            }
+            h->raw_carry = 1;
+        }
+    }
+    if (c.framed && !c.aligned && c.n_out > 0) {  // headers first, so every shipped wave is complete
+        SDBE_CK(h, launch_vdif_headers(c.dev_out, c.n_out, c.out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
+                                       h->station, h->bdc, h->rx, st));
+        h->launches += 1;
+        const uint64_t dfs = static_cast<uint64_t>(h->df) + static_cast<uint64_t>(c.n_out);
+        h->secs += static_cast<uint32_t>(dfs / 125000u);
+        h->df = static_cast<uint32_t>(dfs % 125000u);
+        h->psn += static_cast<uint64_t>(c.n_out);
+    }
+    return SDBE_OK;
+}
+
+int complete_call(CallPlan &c, sdbe_result *result) {
+    sdbe_resampler *h = c.h;
+    cudaStream_t st = c.st;
+    if (c.aligned) {
+        const uint32_t *pay_w = reinterpret_cast<const uint32_t *>(h->pay);
+        const int64_t pay_ws = c.n_pay * kOutWords;
+        uint32_t *cur = h->left[h->left_idx], *nxt = h->left[h->left_idx ^ 1];
+        if (c.n_out > 0) {
+            SDBE_CK(h, launch_align_frames(pay_w, pay_ws, cur, kOutWords, h->n_left, c.a_skip, c.n_out, c.dev_out,
+                                           c.out_pol_stride, st));
+            SDBE_CK(h, launch_vdif_headers(c.dev_out, c.n_out, c.out_pol_stride, c.a_secs, c.a_df, c.a_psn, c.a_epoch,
+                                           h->station, h->bdc, h->rx, st));
+            h->launches += 2;
+        }
+        if (c.a_skip_after == 0) {
+            SDBE_CK(h, launch_save_leftover(pay_w, pay_ws, cur, kOutWords, h->n_left, c.a_skip, c.n_out * kOutWords,
+                                            c.a_new_left, nxt, st));
+            h->launches += c.a_new_left > 0 ? 1 : 0;
+            h->left_idx ^= 1;
+            h->n_left = c.a_new_left;
+        } else {
+            h->n_left = 0;
+        }
+        h->skip_pending = c.a_skip_after;
+        h->align_pending = false;
+        const uint64_t dfs = static_cast<uint64_t>(c.a_df) + static_cast<uint64_t>(c.n_out);
+        h->secs = c.a_secs + static_cast<uint32_t>(dfs / 125000u);
+        h->df = static_cast<uint32_t>(dfs % 125000u);
+        h->psn = c.a_psn + static_cast<uint64_t>(c.n_out);
+        h->ref_epoch = c.a_epoch;
+        if (int rc = ship_call(c, 0, c.n_out)) return rc;
+    }
+    if (c.host_out) SDBE_CK(h, cudaEventRecord(c.sg->out_free, h->copy_out));
+    const int64_t total = h->carry + c.n_frames_out * kSnapsPerFrame;
+    const int64_t new_carry = total - c.n_batches * kBatchSnaps;
+    if (c.n_batches > 0 && new_carry > 0) {
+        for (int pol = 0; pol < 2; ++pol) {
+            uint32_t *base = h->spec + pol * h->spec_pol_stride;
+            SDBE_CK(h, cudaMemcpyAsync(base, base + c.n_batches * kBatchSnaps * kGroups,
+                                       new_carry * kGroups * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    h->carry = new_carry;
+    h->last_stream = st;
+    const bool need_sync =
+        result || (!(c.flags & SDBE_ASYNC) && (c.flags & (SDBE_SYNC | SDBE_IN_HOST | SDBE_OUT_HOST)));
+    if (need_sync) {
+        SDBE_CK(h, cudaStreamSynchronize(st));
+        if (c.host_out) SDBE_CK(h, cudaStreamSynchronize(h->copy_out));
+    }
+    if (result) {
+        std::vector<int32_t> cnt(static_cast<size_t>(h->cfg.max_frames) + 1);
+        SDBE_CK(h, cudaMemcpy(cnt.data(), h->counts, cnt.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        int64_t acc = 0, incomplete = 0;
+        for (int32_t f = 0; f < c.n_frames; ++f) {
+            acc += cnt[f];
+            if (cnt[f] < kPktsPerFrame) ++incomplete;
+        }
+        result->n_batches = c.n_batches;
+        result->n_out_packets = c.n_out;
+        result->packets_accepted = acc;
+        result->packets_rejected = cnt[h->cfg.max_frames];
+        result->frames_incomplete = incomplete;
+        result->carry_snapshots = h->carry;
+    }
+    return SDBE_OK;
+}
+
+// The FFT chain of several handles on one stream: the first-batch threshold
+// path of every handle that needs it in one pair of launches, then waves in
+// which one stage-A and one stage-BC launch cover every handle's batches.
+int fft_chain_multi(std::vector<CallPlan> &cs) {
+    sdbe_resampler *h0 = cs[0].h;
+    cudaStream_t st = cs[0].st;
+    const int n = static_cast<int>(cs.size());
+    std::vector<int64_t> b(static_cast<size_t>(n), 0);
+    {
+        SegsA A{};
+        SegsB B{};
+        std::vector<int> first;
+        for (int i = 0; i < n; ++i) {
+            sdbe_resampler *h = cs[i].h;
+            if (cs[i].n_batches == 0 || h->thresholds_set) continue;
+            A.s[A.n] = SegA{h->spec, h->ts, h->spec_pol_stride, 0, kBatchSnaps, h->ts_pol_stride, A.n_items};
+            A.n_items += 2 * kBatchSnaps;
+            ++A.n;
+            ResampleOut o{};
+            o.fout = h->fout;
+            o.fout_pol_stride = static_cast<int64_t>(kChunks) * kNC;
+            o.partials = h->partials;
+            B.s[B.n] = SegB{h->ts, h->ts_pol_stride, B.n_items, kChunks, h->skip, o};
+            B.n_items += 2 * kChunks;
+            ++B.n;
+            first.push_back(i);
+        }
+        if (!first.empty()) {
+            SDBE_CK(h0, launch_swarm_c2r_segs(A, h0->tw, st));
+            SDBE_CK(h0, launch_resample_segs(1, B, h0->tw, st));
+            h0->launches += 2;
+            for (int i : first) {
+                sdbe_resampler *h = cs[i].h;
+                const PayloadTarget &t = cs[i].pt;
+                SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
+                SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, t.base,
+                                                  t.pol_stride, t.pkt_stride, t.payload_off, 0, st));
+                h->thresholds_set = true;
+                h->launches += 2;
+                b[i] = 1;
+                if (!cs[i].aligned)
+                    if (int rc = ship_call(cs[i], 0, kChunks)) return rc;
+            }
+        }
+    }
+    int wave = h0->wave;
+    for (const auto &c : cs) wave = std::min(wave, c.h->wave);
+    while (true) {
+        SegsA A{};
+        SegsB B{};
+        std::vector<std::pair<int, int64_t>> act;  // handle index, batches this wave
+        for (int i = 0; i < n; ++i) {
+            sdbe_resampler *h = cs[i].h;
+            if (b[i] >= cs[i].n_batches) continue;
+            const int64_t nb = std::min<int64_t>(wave, cs[i].n_batches - b[i]);
+            A.s[A.n] = SegA{h->spec, h->ts, h->spec_pol_stride, b[i] * kBatchSnaps, nb * kBatchSnaps, h->ts_pol_stride,
+                            A.n_items};
+            A.n_items += 2 * nb * kBatchSnaps;
+            ++A.n;
+            const PayloadTarget &t = cs[i].pt;
+            ResampleOut o{};
+            o.out = t.base;
+            o.out_pol_stride = t.pol_stride;
+            o.pkt_stride = t.pkt_stride;
+            o.payload_off = t.payload_off;
+            o.pkt0 = b[i] * kChunks;
+            o.thr = h->thr;
+            B.s[B.n] = SegB{h->ts, h->ts_pol_stride, B.n_items, static_cast<int>(nb * kChunks), h->skip, o};
+            B.n_items += 2 * nb * kChunks;
+            ++B.n;
+            act.emplace_back(i, nb);
+        }
+        if (act.empty()) break;
+        size_t slot;
+        SDBE_CK(h0, timed_begin(h0, 0, A.n_items, st, &slot));
+        SDBE_CK(h0, launch_swarm_c2r_segs(A, h0->tw, st));
+        SDBE_CK(h0, timed_end(h0, slot, st));
+        SDBE_CK(h0, timed_begin(h0, 1, B.n_items, st, &slot));
+        SDBE_CK(h0, launch_resample_segs(0, B, h0->tw, st));
+        SDBE_CK(h0, timed_end(h0, slot, st));
+        h0->launches += 2;
+        for (auto [i, nb] : act) {
+            if (!cs[i].aligned)
+                if (int rc = ship_call(cs[i], b[i] * kChunks, (b[i] + nb) * kChunks)) return rc;
+            b[i] += nb;
+        }
+    }
+    return SDBE_OK;
+}
 }  // namespace sdbe
 
 extern "C" {
@@ -205,222 +548,40 @@ int64_t sdbe_output_bytes(const sdbe_resampler *h, int32_t n_frames, uint32_t fl
 int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int32_t n_frames, uint64_t b_zero,
                  void *out, int64_t out_bytes, uint32_t flags, void *stream, sdbe_result *result) {
     if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
-    if (n_frames < 0 || n_frames > h->cfg.max_frames)
-        return fail(h, SDBE_ERR_CAPACITY, "n_frames outside [0, max_frames]");
-    if (n_packets < 0 || (n_packets > 0 && !packets)) return fail(h, SDBE_ERR_ARG, "bad packets");
     DeviceGuard g(h->cfg.device);
     if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
-    cudaStream_t st = pick(h, stream);
-    const bool aligned = (flags & SDBE_OUT_ALIGNED) != 0;
-    const bool framed = (flags & (SDBE_OUT_FRAMED | SDBE_OUT_ALIGNED)) != 0;
-    const int64_t n_batches = batches_for(h, n_frames);
-    const int64_t n_pay = n_batches * kChunks;  // payload packets per pol the FFTs produce
-    // Time alignment (vdif_out_net_thread.c:199-317): first block after a
-    // template starts on the next second boundary if it would cross one and
-    // skips the sub-packet offset; every block frames whole packets of
-    // [leftover | payload] and carries the rest.
-    uint32_t a_secs = h->secs, a_df = h->df;
-    uint64_t a_psn = h->psn;
-    uint32_t a_epoch = h->ref_epoch;
-    int64_t a_skip_total = h->skip_pending, a_skip = 0, a_new_left = 0, a_skip_after = 0;
-    int64_t n_out = n_pay;
-    if (aligned) {
-        if (h->align_pending) {
-            a_secs = h->tmpl.secs_inre;
-            a_df = h->tmpl.df_num_insec;
-            int64_t skip_frames = 0;
-            if (static_cast<int64_t>(a_df) > 125000 - n_pay) {
-                skip_frames = 125000 - static_cast<int64_t>(a_df);
-                a_df = 0;
-                a_secs += 1;
-            }
-            const double skip_ps = static_cast<double>(h->tmpl.ps_early + 3715791ull);
-            const double skip_samples = std::floor(skip_ps * 4096e6 / 1e12);
-            a_skip_total += static_cast<int64_t>(std::floor(skip_samples / (8.0 / 2.0) / 4.0)) + skip_frames * kOutWords;
-            a_psn = 1;
-            a_epoch = h->tmpl.ref_epoch;
-        }
-        const int64_t stream_len = h->n_left + n_pay * kOutWords - a_skip_total;
-        if (stream_len < 0) {
-            n_out = 0;
-            a_skip_after = -stream_len;
-        } else {
-            a_skip = a_skip_total;
-            n_out = stream_len / kOutWords;
-            a_new_left = stream_len - n_out * kOutWords;
-        }
-    }
-    const int64_t pkt_stride = framed ? kOutPkt : kOutPktData;
-    const int64_t payload_off = framed ? 32 : 0;
-    const int64_t out_pol_stride = n_out * pkt_stride;
-    if (out_bytes < 2 * out_pol_stride) return fail(h, SDBE_ERR_CAPACITY, "output buffer too small");
-    if (n_out > 0 && !out) return fail(h, SDBE_ERR_ARG, "null output");
-    if (h->cfg.threshold_mode == SDBE_THRESH_FIXED && !h->thresholds_set && n_batches > 0)
-        return fail(h, SDBE_ERR_STATE, "fixed threshold mode needs sdbe_set_state first");
+    CallPlan c;
+    int rc = plan_call(h, packets, n_packets, n_frames, b_zero, out, out_bytes, flags, pick(h, stream), c);
+    if (!rc) rc = prepare_call(c);
+    if (!rc) rc = fft_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st,
+                            [&](int64_t lo, int64_t hi) { return c.aligned ? SDBE_OK : ship_call(c, lo, hi); });
+    if (!rc) rc = complete_call(c, result);
+    return rc;
+}
 
-    const bool host_in = (flags & SDBE_IN_HOST) && n_packets > 0;
-    const bool host_out = (flags & SDBE_OUT_HOST) && n_out > 0;
-    sdbe_resampler::Stage &sg = h->stage[h->stage_idx];
-    if (host_in || host_out) h->stage_idx ^= 1;
-    const uint8_t *src = static_cast<const uint8_t *>(packets);
-    if (host_in) {
-        int rc = grow(h, &sg.pkt, &sg.pkt_bytes, n_packets * kPktBytes, "packet staging");
-        if (rc) return rc;
-        // the slot's previous packets must have been unpacked before they are overwritten
-        SDBE_CK(h, cudaStreamWaitEvent(h->copy_in, sg.pkt_free, 0));
-        SDBE_CK(h, cudaMemcpyAsync(sg.pkt, packets, n_packets * kPktBytes, cudaMemcpyHostToDevice, h->copy_in));
-        SDBE_CK(h, cudaEventRecord(sg.pkt_ready, h->copy_in));
-        SDBE_CK(h, cudaStreamWaitEvent(st, sg.pkt_ready, 0));
-        src = sg.pkt;
-    } else if (n_packets > 0 && (reinterpret_cast<uintptr_t>(packets) & 15u)) {
-        return fail(h, SDBE_ERR_ARG, "device packet buffer must be 16-byte aligned");
+int sdbe_process_multi(sdbe_resampler *const *hs, const sdbe_stream_desc *d, int32_t n, uint32_t flags, void *stream,
+                       sdbe_result *results) {
+    if (!hs || !d || n < 1 || n > kMaxSegs) return fail(nullptr, SDBE_ERR_ARG, "need 1..32 handles and descriptors");
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i]) return fail(nullptr, SDBE_ERR_ARG, "null handle");
+        if (hs[i]->cfg.device != hs[0]->cfg.device) return fail(hs[i], SDBE_ERR_ARG, "handles on different devices");
+        for (int j = 0; j < i; ++j)
+            if (hs[j] == hs[i]) return fail(hs[i], SDBE_ERR_ARG, "a handle appears twice");
     }
-    uint8_t *dev_out = static_cast<uint8_t *>(out);
-    if (host_out) {
-        int rc = grow(h, &sg.out, &sg.out_bytes, 2 * out_pol_stride, "output staging");
-        if (rc) return rc;
-        // the slot's previous payloads must have left for the host before they are overwritten
-        SDBE_CK(h, cudaStreamWaitEvent(st, sg.out_free, 0));
-        dev_out = sg.out;
-    } else if (n_out > 0 && (reinterpret_cast<uintptr_t>(out) & 15u)) {
-        return fail(h, SDBE_ERR_ARG, "device output buffer must be 16-byte aligned");
-    }
-    // Where the FFT waves write: the output itself, or the plain payload
-    // stream that the alignment step frames afterwards.
-    uint8_t *tgt = dev_out;
-    int64_t tgt_pol_stride = out_pol_stride, tgt_pkt_stride = pkt_stride, tgt_off = payload_off;
-    if (aligned && n_pay > 0) {
-        int rc = grow(h, &h->pay, &h->pay_bytes, 2 * n_pay * kOutPktData, "payload stream");
-        if (rc) return rc;
-        tgt = h->pay;
-        tgt_pol_stride = n_pay * kOutPktData;
-        tgt_pkt_stride = kOutPktData;
-        tgt_off = 0;
-    }
-    // Payload packets [lo, hi) of both pols are final: send them to the host
-    // on the copy stream while the next wave computes.
-    auto ship = [&](int64_t lo, int64_t hi) -> int {
-        if (!host_out || hi <= lo) return SDBE_OK;
-        SDBE_CK(h, cudaEventRecord(h->wave_ev, st));
-        SDBE_CK(h, cudaStreamWaitEvent(h->copy_out, h->wave_ev, 0));
-        SDBE_CK(h, cudaMemcpy2DAsync(static_cast<uint8_t *>(out) + lo * pkt_stride, out_pol_stride,
-                                     dev_out + lo * pkt_stride, out_pol_stride, (hi - lo) * pkt_stride, 2,
-                                     cudaMemcpyDeviceToHost, h->copy_out));
-        return SDBE_OK;
-    };
-
-    const int map = h->cfg.channel_map;
-    const bool mar = map == SDBE_MAP_MAR2015;
-    const int64_t n_frames_out = frames_out(h, n_frames);
-    if (n_frames > 0) {
-        // Mar-2015: unpack after the held frame in `raw`; otherwise straight
-        // into the snapshot stream after the carried snapshots.
-        uint32_t *dst = mar ? h->raw : h->spec;
-        const int64_t dst_stride = mar ? h->raw_pol_stride : h->spec_pol_stride;
-        const int64_t snap0 = mar ? static_cast<int64_t>(h->raw_carry) * kSnapsPerFrame : h->carry;
-        SDBE_CK(h, cudaMemsetAsync(h->bitmap, 0, static_cast<size_t>(n_frames) * 256, st));
-        SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
-        SDBE_CK(h, launch_unpack(src, n_packets, b_zero, n_frames, map, dst, dst_stride, snap0, h->bitmap, h->counts,
-                                 h->counts + h->cfg.max_frames, st));
-        if (host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
-        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, dst, dst_stride, snap0, st));
-        h->launches += n_packets > 0 ? 2 : 1;
-        if (mar) {
-            const int n_in = h->raw_carry + n_frames;
-            for (int pol = 0; pol < 2 && n_in >= 2; ++pol) {
-                SDBE_CK(h, launch_reorder_mar2015(h->raw + pol * h->raw_pol_stride, n_in,
-                                                  h->spec + pol * h->spec_pol_stride + h->carry * kGroups, st));
-                h->launches += 1;
-            }
-            if (n_in >= 2) {  // hold the newest frame
-                for (int pol = 0; pol < 2; ++pol) {
-                    uint32_t *base = h->raw + pol * h->raw_pol_stride;
-                    SDBE_CK(h, cudaMemcpyAsync(base, base + static_cast<int64_t>(n_in - 1) * kSnapsPerFrame * kGroups,
-                                               static_cast<size_t>(kSnapsPerFrame) * kGroups * sizeof(uint32_t),
-                                               cudaMemcpyDeviceToDevice, st));
-                }
-            }
-            h->raw_carry = 1;
-        }
-    }
-    if (framed && !aligned && n_out > 0) {  // headers first, so every shipped wave is complete
-        SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, h->secs, h->df, h->psn, h->ref_epoch,
-                                       h->station, h->bdc, h->rx, st));
-        h->launches += 1;
-        const uint64_t dfs = static_cast<uint64_t>(h->df) + static_cast<uint64_t>(n_out);
-        h->secs += static_cast<uint32_t>(dfs / 125000u);
-        h->df = static_cast<uint32_t>(dfs % 125000u);
-        h->psn += static_cast<uint64_t>(n_out);
-    }
-
-    {
-        PayloadTarget pt{tgt, tgt_pol_stride, tgt_pkt_stride, tgt_off};
-        int rc = fft_chain(h, h->spec, h->spec_pol_stride, n_batches, pt, st,
-                           [&](int64_t lo, int64_t hi) { return aligned ? SDBE_OK : ship(lo, hi); });
+    DeviceGuard g(hs[0]->cfg.device);
+    if (!g.ok) return fail(hs[0], SDBE_ERR_CUDA, "cudaSetDevice failed");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : hs[0]->stream;
+    std::vector<CallPlan> c(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) {  // every check before any work is queued
+        int rc = plan_call(hs[i], d[i].packets, d[i].n_packets, d[i].n_frames, d[i].b_zero, d[i].out, d[i].out_bytes,
+                           flags, st, c[i]);
         if (rc) return rc;
     }
-    if (aligned) {
-        const uint32_t *pay_w = reinterpret_cast<const uint32_t *>(h->pay);
-        const int64_t pay_ws = n_pay * kOutWords;
-        uint32_t *cur = h->left[h->left_idx], *nxt = h->left[h->left_idx ^ 1];
-        if (n_out > 0) {
-            SDBE_CK(h, launch_align_frames(pay_w, pay_ws, cur, kOutWords, h->n_left, a_skip, n_out, dev_out,
-                                           out_pol_stride, st));
-            SDBE_CK(h, launch_vdif_headers(dev_out, n_out, out_pol_stride, a_secs, a_df, a_psn, a_epoch, h->station,
-                                           h->bdc, h->rx, st));
-            h->launches += 2;
-        }
-        if (a_skip_after == 0) {
-            SDBE_CK(h, launch_save_leftover(pay_w, pay_ws, cur, kOutWords, h->n_left, a_skip, n_out * kOutWords,
-                                            a_new_left, nxt, st));
-            h->launches += a_new_left > 0 ? 1 : 0;
-            h->left_idx ^= 1;
-            h->n_left = a_new_left;
-        } else {
-            h->n_left = 0;
-        }
-        h->skip_pending = a_skip_after;
-        h->align_pending = false;
-        const uint64_t dfs = static_cast<uint64_t>(a_df) + static_cast<uint64_t>(n_out);
-        h->secs = a_secs + static_cast<uint32_t>(dfs / 125000u);
-        h->df = static_cast<uint32_t>(dfs % 125000u);
-        h->psn = a_psn + static_cast<uint64_t>(n_out);
-        h->ref_epoch = a_epoch;
-        if (int rc = ship(0, n_out)) return rc;
-    }
-    if (host_out) SDBE_CK(h, cudaEventRecord(sg.out_free, h->copy_out));
-    const int64_t total = h->carry + n_frames_out * kSnapsPerFrame;
-    const int64_t new_carry = total - n_batches * kBatchSnaps;
-    if (n_batches > 0 && new_carry > 0) {
-        for (int pol = 0; pol < 2; ++pol) {
-            uint32_t *base = h->spec + pol * h->spec_pol_stride;
-            SDBE_CK(h, cudaMemcpyAsync(base, base + n_batches * kBatchSnaps * kGroups,
-                                       new_carry * kGroups * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
-        }
-    }
-    h->carry = new_carry;
-    h->last_stream = st;
-    const bool need_sync =
-        result || (!(flags & SDBE_ASYNC) && (flags & (SDBE_SYNC | SDBE_IN_HOST | SDBE_OUT_HOST)));
-    if (need_sync) {
-        SDBE_CK(h, cudaStreamSynchronize(st));
-        if (host_out) SDBE_CK(h, cudaStreamSynchronize(h->copy_out));
-    }
-    if (result) {
-        std::vector<int32_t> cnt(static_cast<size_t>(h->cfg.max_frames) + 1);
-        SDBE_CK(h, cudaMemcpy(cnt.data(), h->counts, cnt.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
-        int64_t acc = 0, incomplete = 0;
-        for (int32_t f = 0; f < n_frames; ++f) {
-            acc += cnt[f];
-            if (cnt[f] < kPktsPerFrame) ++incomplete;
-        }
-        result->n_batches = n_batches;
-        result->n_out_packets = n_out;
-        result->packets_accepted = acc;
-        result->packets_rejected = cnt[h->cfg.max_frames];
-        result->frames_incomplete = incomplete;
-        result->carry_snapshots = h->carry;
-    }
+    for (auto &ci : c)
+        if (int rc = prepare_call(ci)) return rc;
+    if (int rc = fft_chain_multi(c)) return rc;
+    for (int i = 0; i < n; ++i)
+        if (int rc = complete_call(c[i], results ? results + i : nullptr)) return rc;
     return SDBE_OK;
 }
 

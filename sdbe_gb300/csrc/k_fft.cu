@@ -282,18 +282,25 @@ __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_
 // Stage A (persistent): items = n_snaps x n_pols.  Packed spectrum of snapshot
 // s of pol p at spec + p*spec_pol_stride + (snap0 + s)*2048; time series to
 // out + p*out_pol_stride + s*32768.
-__global__ void __launch_bounds__(kNTA, 1)
-    k_swarm_c2r(const uint32_t *__restrict__ spec, int64_t spec_pol_stride, int64_t snap0, int64_t n_snaps,
-                int n_pols, float *__restrict__ out, int64_t out_pol_stride, Twiddles tw) {
+template <class Segs>
+__device__ __forceinline__ int seg_of(const Segs &S, int64_t item) {
+    int j = 0;
+    while (j + 1 < S.n && item >= S.s[j + 1].item0) ++j;
+    return j;
+}
+
+__global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ SegsA S, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *sp = reinterpret_cast<uint32_t *>(smem_raw);  // [2][2048] double buffer
     float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
     TabsA T{sm + kPadA, sm + kPadA + kT1024, sm + kPadA + kT1024 + kT128};
     load_tabs_a(T, tw);
-    const int64_t n_items = n_snaps * n_pols;
+    const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
-        const int64_t pol = item / n_snaps, s = item % n_snaps;
-        return reinterpret_cast<const uint4 *>(spec + pol * spec_pol_stride + (snap0 + s) * kGroups);
+        const SegA &g = S.s[seg_of(S, item)];
+        const int64_t local = item - g.item0;
+        const int64_t pol = local / g.n_snaps, s = local % g.n_snaps;
+        return reinterpret_cast<const uint4 *>(g.spec + pol * g.spec_pol_stride + (g.snap0 + s) * kGroups);
     };
     int64_t item = blockIdx.x;
     if (item < n_items) cp_async16(sp + 4 * threadIdx.x, src_of(item) + threadIdx.x);
@@ -305,8 +312,10 @@ __global__ void __launch_bounds__(kNTA, 1)
         cp_async_wait_1();
         __syncthreads();  // this item's spectrum landed; tables loaded
         const uint32_t *cur = sp + buf * kGroups;
-        const int64_t pol = item / n_snaps, s = item % n_snaps;
-        float2 *dst = reinterpret_cast<float2 *>(out + pol * out_pol_stride + s * kNA);
+        const SegA &g = S.s[seg_of(S, item)];
+        const int64_t local = item - g.item0;
+        const int64_t pol = local / g.n_snaps, s = local % g.n_snaps;
+        float2 *dst = reinterpret_cast<float2 *>(g.out + pol * g.out_pol_stride + s * kNA);
         // Hermitian pairing: Z[k], Z[M-k] for k = 0..8192 from X[k], X[M-k];
         // X[16384] (Nyquist) = 0 and the imaginary part of X[0] are dropped.
         for (int k = threadIdx.x; k <= kMA / 2; k += kNTA) {
@@ -344,9 +353,7 @@ __global__ void __launch_bounds__(kNTA, 1)
 //           (n, mean, M2) in FP64 to partials[(p*n_chunks + c)*3].
 //   MODE 2: floats only.
 template <int MODE>
-__global__ void __launch_bounds__(kNTB, 1)
-    k_resample(const float *__restrict__ in, int64_t in_pol_stride, int skip, int n_chunks, int n_pols,
-               ResampleOut o, Twiddles tw) {
+__global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ SegsB S, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
@@ -356,12 +363,16 @@ __global__ void __launch_bounds__(kNTB, 1)
     load_tabs_a(TA, tw);
     load_tabs_b(TB, tw);
     const int tid = threadIdx.x;
-    const int64_t n_items = static_cast<int64_t>(n_chunks) * n_pols;
+    const int64_t n_items = S.n_items;
     for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
-        const int pol = static_cast<int>(item / n_chunks);
-        const int64_t c = item % n_chunks;
+        const SegB &g = S.s[seg_of(S, item)];
+        const ResampleOut &o = g.o;
+        const int n_chunks = g.n_chunks, skip = g.skip;
+        const int64_t local = item - g.item0;
+        const int pol = static_cast<int>(local / n_chunks);
+        const int64_t c = local % n_chunks;
         __syncthreads();  // tables loaded / previous item's last smem reads done
-        const float2 *z = reinterpret_cast<const float2 *>(in + pol * in_pol_stride + c * kNB);
+        const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
         fft18304_from_global(sm, z, TB);
         // R2C post-processing in place: X[q], X[M'-q] from Z[q], Z[M'-q];
         // X[0] and X[18304] (both real) from Z[0], X[18304] in the spare slot.
@@ -664,26 +675,44 @@ static unsigned persistent_grid(int64_t items) {
 }
 
 // ---- launchers ----------------------------------------------------------------
+cudaError_t launch_swarm_c2r_segs(const SegsA &S, const Twiddles &tw, cudaStream_t st) {
+    if (S.n_items <= 0) return cudaSuccess;
+    if (S.n < 1 || S.n > kMaxSegs) return cudaErrorInvalidValue;
+    k_swarm_c2r<<<persistent_grid(S.n_items), kNTA, kSmemA, st>>>(S, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resample_segs(int mode, const SegsB &S, const Twiddles &tw, cudaStream_t st) {
+    if (S.n_items <= 0) return cudaSuccess;
+    if (S.n < 1 || S.n > kMaxSegs) return cudaErrorInvalidValue;
+    const unsigned grid = persistent_grid(S.n_items);
+    if (mode == 0)
+        k_resample<0><<<grid, kNTB, kSmemB, st>>>(S, tw);
+    else if (mode == 1)
+        k_resample<1><<<grid, kNTB, kSmemB, st>>>(S, tw);
+    else
+        k_resample<2><<<grid, kNTB, kSmemB, st>>>(S, tw);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_swarm_c2r(const uint32_t *spec, int64_t spec_pol_stride, int64_t snap0, int64_t n_snaps, int n_pols,
                              float *out, int64_t out_pol_stride, const Twiddles &tw, cudaStream_t st) {
     if (n_snaps <= 0) return cudaSuccess;
-    k_swarm_c2r<<<persistent_grid(n_snaps * n_pols), kNTA, kSmemA, st>>>(spec, spec_pol_stride, snap0, n_snaps, n_pols,
-                                                                          out, out_pol_stride, tw);
-    return cudaGetLastError();
+    SegsA S{};
+    S.n = 1;
+    S.n_items = n_snaps * n_pols;
+    S.s[0] = SegA{spec, out, spec_pol_stride, snap0, n_snaps, out_pol_stride, 0};
+    return launch_swarm_c2r_segs(S, tw, st);
 }
 
 cudaError_t launch_resample(int mode, const float *in, int64_t in_pol_stride, int skip, int64_t n_chunks, int n_pols,
                             const ResampleOut &o, const Twiddles &tw, cudaStream_t st) {
     if (n_chunks <= 0) return cudaSuccess;
-    const unsigned grid = persistent_grid(n_chunks * n_pols);
-    const int nc = static_cast<int>(n_chunks);
-    if (mode == 0)
-        k_resample<0><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
-    else if (mode == 1)
-        k_resample<1><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
-    else
-        k_resample<2><<<grid, kNTB, kSmemB, st>>>(in, in_pol_stride, skip, nc, n_pols, o, tw);
-    return cudaGetLastError();
+    SegsB S{};
+    S.n = 1;
+    S.n_items = n_chunks * n_pols;
+    S.s[0] = SegB{in, in_pol_stride, 0, static_cast<int>(n_chunks), skip, o};
+    return launch_resample_segs(mode, S, tw, st);
 }
 
 cudaError_t launch_swarm_r2c(const float *in, int64_t n_chunks, void *out, const Twiddles &tw, cudaStream_t st) {

@@ -12,6 +12,34 @@ struct ResampleOut {
     int64_t fout_pol_stride;
     double *partials;
 };
+
+// Work of one persistent FFT launch as segments: each handle (stream pair)
+// contributes n_pols x n items, pol-major, starting at global item item0.
+// Passed by value as a __grid_constant__ kernel parameter.
+constexpr int kMaxSegs = 32;
+struct SegA {  // stage A: snapshots snap0 .. snap0+n_snaps of each pol
+    const uint32_t *spec;
+    float *out;
+    int64_t spec_pol_stride, snap0, n_snaps, out_pol_stride, item0;
+};
+struct SegsA {
+    int64_t n_items;
+    int n;
+    SegA s[kMaxSegs];
+};
+struct SegB {  // stage BC: n_chunks 36608-sample chunks of each pol
+    const float *in;
+    int64_t in_pol_stride, item0;
+    int n_chunks, skip;
+    ResampleOut o;
+};
+struct SegsB {
+    int64_t n_items;
+    int n;
+    SegB s[kMaxSegs];
+};
+cudaError_t launch_swarm_c2r_segs(const SegsA &, const Twiddles &, cudaStream_t);
+cudaError_t launch_resample_segs(int mode, const SegsB &, const Twiddles &, cudaStream_t);
 cudaError_t launch_unpack(const void *, int64_t, uint64_t, int, int, uint32_t *, int64_t, int64_t, uint32_t *,
                           int32_t *, int32_t *, cudaStream_t, const uint8_t *accept = nullptr);
 cudaError_t launch_fill_missing(const uint32_t *, int, int, uint32_t *, int64_t, int64_t, cudaStream_t);

@@ -284,3 +284,52 @@ class _PinnedArray(np.ndarray):
         if getattr(self, "_pinned_ptr", None):
             N.lib().sdbe_host_free(self._pinned_ptr)
             self._pinned_ptr = None
+
+
+def process_multi(resamplers, items, framed: bool = False, stream=None, want_results: bool = False,
+                  host: bool | None = None):
+    """One pass over several packet streams with shared FFT launches
+    (``sdbe_process_multi``).
+
+    ``items``: per resampler ``(packets, n_frames, b_zero, out)``; ``out`` may
+    be None for host runs (allocated).  Buffers are all host (numpy) or all
+    device (torch CUDA tensors).  Returns the outputs (and the per-stream
+    ``GroupResult`` list when ``want_results``).
+    """
+    n = len(resamplers)
+    if n != len(items) or n == 0:
+        raise ValueError("one item per resampler")
+    lib = resamplers[0]._lib
+    if host is None:
+        host = not _is_device(items[0][0])
+    flags = (N.IN_HOST | N.OUT_HOST) if host else 0
+    if framed:
+        flags |= N.OUT_FRAMED
+    hs = (C.c_void_p * n)(*[r.handle.value for r in resamplers])
+    descs = (N.StreamDesc * n)()
+    outs = []
+    keep = []
+    for i, (r, (pk, n_frames, b_zero, out)) in enumerate(zip(resamplers, items)):
+        need = r.output_bytes(n_frames, framed)
+        if out is None:
+            pkt = N.OUT_PKT_BYTES if framed else N.OUT_PKT_DATA_BYTES
+            out = np.empty((2, need // (2 * pkt) if need else 0, pkt), np.uint8)
+        if host:
+            pk = np.ascontiguousarray(pk, dtype=np.uint8)
+            keep.append(pk)
+        descs[i].packets = _addr(pk)
+        descs[i].n_packets = int(pk.shape[0]) if hasattr(pk, "shape") else 0
+        descs[i].n_frames = n_frames
+        descs[i].b_zero = b_zero
+        descs[i].out = _addr(out)
+        descs[i].out_bytes = _nbytes(out)
+        outs.append(out)
+    res = (N.Result * n)() if want_results else None
+    st = C.c_void_p(stream) if isinstance(stream, int) else (
+        C.c_void_p(stream.cuda_stream) if stream is not None else None)
+    rc = lib.sdbe_process_multi(hs, descs, n, flags, st, res)
+    N.check(rc, resamplers[0].handle)
+    if not want_results:
+        return outs
+    return outs, [GroupResult(x.n_batches, x.n_out_packets, x.packets_accepted, x.packets_rejected,
+                              x.frames_incomplete, x.carry_snapshots) for x in res]
