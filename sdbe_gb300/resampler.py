@@ -287,14 +287,16 @@ class _PinnedArray(np.ndarray):
 
 
 def process_multi(resamplers, items, framed: bool = False, stream=None, want_results: bool = False,
-                  host: bool | None = None):
+                  host: bool | None = None, asynchronous: bool = False):
     """One pass over several packet streams with shared FFT launches
     (``sdbe_process_multi``).
 
     ``items``: per resampler ``(packets, n_frames, b_zero, out)``; ``out`` may
     be None for host runs (allocated).  Buffers are all host (numpy) or all
     device (torch CUDA tensors).  Returns the outputs (and the per-stream
-    ``GroupResult`` list when ``want_results``).
+    ``GroupResult`` list when ``want_results``).  With ``asynchronous`` (host
+    buffers, no results) the call returns once the work is queued; ``sync()``
+    each resampler before reading the outputs or reusing the inputs.
     """
     n = len(resamplers)
     if n != len(items) or n == 0:
@@ -305,6 +307,8 @@ def process_multi(resamplers, items, framed: bool = False, stream=None, want_res
     flags = (N.IN_HOST | N.OUT_HOST) if host else 0
     if framed:
         flags |= N.OUT_FRAMED
+    if asynchronous:
+        flags |= N.ASYNC
     hs = (C.c_void_p * n)(*[r.handle.value for r in resamplers])
     descs = (N.StreamDesc * n)()
     outs = []
