@@ -23,30 +23,41 @@ namespace sdbe {
 
 constexpr int kNTA = 512;   // stage A threads: 512 radix-32 butterflies per pass
 constexpr int kNTB = 512;   // stage BC threads: 4 warps per SM sub-partition -> 128 registers
+// The 18304-point data (stage BC) is padded one float2 per 16, so that the
+// first pass's digit-reversed stores, 16 lanes at a time, land in 16
+// distinct bank pairs (see fft18304_from_global); the 16384-point transforms
+// keep one per 32 (their layouts are built on it).
+__host__ __device__ constexpr int padb(int a) { return a + (a >> 4); }
 constexpr int kPadA = padded_len(kMA);
-constexpr int kPadB = padded_len(kMB);
+constexpr int kPadB = padb(kMB) + 1;
 
-// Shared-memory twiddle tables (float2, padded with tp()).
-constexpr int kT1024 = tp_len(1024);   // W_1024^m            (16384-point pass 2)
+// Shared-memory twiddle tables (float2).  The per-pass tables are laid out
+// [r][k] so that the 16 lanes of a half-warp, which hold consecutive k, read
+// consecutive words; the two-level tables are padded with tp().
+constexpr int kT32 = 10 * 32;          // W_1024^{j s}, s = 1..7, then W_1024^{8 j a}, a = 1..3 (16384-point pass 2)
 constexpr int kT128 = tp_len(128);     // two-level halves
-constexpr int kT208 = tp_len(208);     // W_208^m             (18304-point radix-13 pass)
-constexpr int kT2288 = tp_len(2288);   // W_2288^m            (18304-point radix-11 pass)
+constexpr int kT13 = 12 * 16;          // W_208^{k r}, r = 1..12, k = 0..15   (18304-point radix-13 pass)
+constexpr int kT11 = 10 * 208;         // W_2288^{k r}, r = 1..10, k = 0..207 (18304-point radix-11 pass)
 constexpr int kH18304 = tp_len(143);   // W_18304^{128 a}
-constexpr int kTwA = kT1024 + 2 * kT128;                              // stage A tables
-constexpr int kTwB = kTwA + kT208 + kT2288 + kH18304 + kT128;          // stage BC tables
+constexpr int kTwA = kT32 + 2 * kT128;                              // stage A tables
+constexpr int kTwB = kTwA + kT13 + kT11 + kH18304 + kT128;          // stage BC tables
 constexpr size_t kSmemA = 2 * kGroups * sizeof(uint32_t) + (kPadA + kTwA) * sizeof(float2);
 constexpr size_t kSmemB = (kPadB + kTwB) * sizeof(float2);
 
 // ---- table loading --------------------------------------------------------
 struct TabsA {  // inverse-16384 tables
-    float2 *t1024, *h16384, *l16384;
+    float2 *t32, *h16384, *l16384;
 };
 struct TabsB {  // forward-18304 tables
-    float2 *t208, *t2288, *h18304, *l18304;
+    float2 *t13, *t11, *h18304, *l18304;
 };
 
 __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
-    for (int m = threadIdx.x; m < 1024; m += blockDim.x) t.t1024[tp(m)] = __ldg(tw.w16384 + 16 * m);
+    for (int m = threadIdx.x; m < kT32; m += blockDim.x) {
+        const int j = m & 31, g = m >> 5;                       // g < 7: s = g + 1; else a = g - 6
+        const int e = g < 7 ? j * (g + 1) : 8 * j * (g - 6);   // exponent of W_1024
+        t.t32[m] = __ldg(tw.w16384 + 16 * e);
+    }
     for (int m = threadIdx.x; m < 128; m += blockDim.x) {
         t.h16384[tp(m)] = __ldg(tw.w16384 + 128 * m);
         t.l16384[tp(m)] = __ldg(tw.w16384 + m);
@@ -54,16 +65,37 @@ __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
 }
 
 __device__ __forceinline__ void load_tabs_b(TabsB t, const Twiddles &tw) {
-    for (int m = threadIdx.x; m < 2288; m += blockDim.x) t.t2288[tp(m)] = __ldg(tw.w18304 + 8 * m);
-    for (int m = threadIdx.x; m < 208; m += blockDim.x) t.t208[tp(m)] = __ldg(tw.w18304 + 88 * m);
+    for (int m = threadIdx.x; m < kT11; m += blockDim.x) {
+        const int r = m / 208 + 1, k = m % 208;
+        t.t11[m] = __ldg(tw.w18304 + 8 * k * r);
+    }
+    for (int m = threadIdx.x; m < kT13; m += blockDim.x) {
+        const int r = (m >> 4) + 1, k = m & 15;
+        t.t13[m] = __ldg(tw.w18304 + 88 * k * r);
+    }
     for (int m = threadIdx.x; m < 143; m += blockDim.x) t.h18304[tp(m)] = __ldg(tw.w18304 + 128 * m);
     for (int m = threadIdx.x; m < 128; m += blockDim.x) t.l18304[tp(m)] = __ldg(tw.w18304 + m);
 }
 
 __device__ __forceinline__ TabsB tabs_b_at(float2 *tb) {
     float2 *p = tb + kTwA;
-    return TabsB{p, p + kT208, p + kT208 + kT2288, p + kT208 + kT2288 + kH18304};
+    return TabsB{p, p + kT13, p + kT13 + kT11, p + kT13 + kT11 + kH18304};
 }
+
+// First-pass lane order of the 18304-point transform: half-warp h takes the
+// groups of 8 consecutive inputs g0 = kFirstPassGroups[2h], g1 = [2h+1]
+// (inputs j = 8g + c, c = 0..7; 255 = none).  Output slot 16*rho(j) + r has
+// rho(8g + c) = rho(8g) - c (mod 16); the pairs are chosen with rho(8 g1) =
+// rho(8 g0) + 8 (mod 16), so the 16 lanes' padded slots cover all 16 bank
+// pairs and every store is one wavefront.
+__constant__ uint8_t kFirstPassGroups[144] = {
+    0,   8,   28,  14,  34,  42,  62,  48,  68,  76,  96,  82,  102, 88,  130, 116, 136, 122, 5,   19,  11,  25,
+    39,  53,  45,  59,  73,  87,  79,  93,  107, 99,  113, 127, 141, 133, 10,  2,   16,  30,  22,  36,  50,  64,
+    56,  70,  84,  98,  90,  104, 118, 110, 124, 138, 21,  7,   27,  13,  33,  41,  61,  47,  67,  75,  95,  81,
+    101, 109, 129, 115, 135, 121, 4,   18,  32,  24,  38,  52,  44,  58,  72,  86,  78,  92,  106, 120, 112, 126,
+    140, 132, 9,   1,   15,  29,  43,  35,  49,  63,  55,  69,  83,  97,  89,  103, 117, 131, 123, 137, 20,  6,
+    26,  12,  54,  40,  60,  46,  66,  74,  94,  80,  100, 108, 128, 114, 134, 142, 3,   17,  31,  23,  37,  51,
+    65,  57,  71,  85,  77,  91,  105, 119, 111, 125, 139, 255};
 
 // ---------------------------------------------------------------------------
 // Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(r) gives
@@ -93,12 +125,12 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
 #pragma unroll
         for (int r = 0; r < 32; ++r) v[r] = src[528 * r];
         // W_1024^{jm r} = A[r/8] * S[r%8]
-        const int jm = tid & 31;
+        const float2 *tj = T.t32 + (tid & 31);
         float2 S[8], A[4];
 #pragma unroll
-        for (int s = 1; s < 8; ++s) S[s] = T.t1024[tp(jm * s)];
+        for (int s = 1; s < 8; ++s) S[s] = tj[32 * (s - 1)];
 #pragma unroll
-        for (int a = 1; a < 4; ++a) A[a] = T.t1024[tp(jm * 8 * a)];
+        for (int a = 1; a < 4; ++a) A[a] = tj[32 * (6 + a)];
 #pragma unroll
         for (int r = 1; r < 32; ++r) {
             const int a = r >> 3, s = r & 7;
@@ -137,21 +169,25 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
 }
 
 // Forward 18304-point FFT of z[m] = x[2m] + i x[2m+1] read from global memory;
-// result Z in natural order in `sm`.  In-place decimation in time, radices
-// 16 (from global) x 13 x 11 x 8: the first pass reads z[j + 1144 r] (coalesced)
-// and writes its 16 outputs to slots 16*rho(j) + r, rho = digit reversal of j
-// over (8, 11, 13); every later butterfly reads and writes the same slots
-// g*Ns*R + k + Ns*r with twiddles W_{Ns*R}^{k r}, so passes need no staging.
+// result Z in natural order in `sm` (padded with padb).  In-place decimation
+// in time, radices 16 (from global) x 13 x 11 x 8: the first pass reads
+// z[j + 1144 r] (8 consecutive j per 8 lanes: 64-B segments) and writes its 16
+// outputs to slots 16*rho(j) + r, rho = digit reversal of j over (8, 11, 13);
+// every later butterfly reads and writes the same slots g*Ns*R + k + Ns*r
+// with twiddles W_{Ns*R}^{k r}, so passes need no staging.
 __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *__restrict__ z, const TabsB &T) {
-    constexpr int NB1 = kMB / 16;  // 1144
-    for (int j = threadIdx.x; j < NB1; j += blockDim.x) {
+    constexpr int NB1 = kMB / 16;  // 1144 = 143 groups of 8
+    for (int h = threadIdx.x >> 4; h < 72; h += blockDim.x >> 4) {
+        const int g = kFirstPassGroups[2 * h + ((threadIdx.x >> 3) & 1)];
+        if (g == 255) continue;
+        const int j = 8 * g + (threadIdx.x & 7);
         float2 v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = __ldcs(z + j + NB1 * r);
         dft<16, false>(v);
         const int rho = (j / 88) + 13 * (((j >> 3) % 11) + 11 * (j & 7));
 #pragma unroll
-        for (int r = 0; r < 16; ++r) sm[pad(16 * rho + r)] = v[r];
+        for (int r = 0; r < 16; ++r) sm[padb(16 * rho + r)] = v[r];
     }
     __syncthreads();
     // radix 13, Ns = 16: twiddles W_208^{k r}
@@ -159,12 +195,12 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         const int k = b & 15, base = (b >> 4) * 208 + k;
         float2 v[13];
 #pragma unroll
-        for (int r = 0; r < 13; ++r) v[r] = sm[pad(base + 16 * r)];
+        for (int r = 0; r < 13; ++r) v[r] = sm[padb(base + 16 * r)];
 #pragma unroll
-        for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], T.t208[tp(k * r)]);
+        for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], T.t13[16 * (r - 1) + k]);
         dft<13, false>(v);
 #pragma unroll
-        for (int r = 0; r < 13; ++r) sm[pad(base + 16 * r)] = v[r];
+        for (int r = 0; r < 13; ++r) sm[padb(base + 16 * r)] = v[r];
     }
     __syncthreads();
     // radix 11, Ns = 208: twiddles W_2288^{k r}
@@ -172,19 +208,19 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         const int k = b % 208, base = (b / 208) * 2288 + k;
         float2 v[11];
 #pragma unroll
-        for (int r = 0; r < 11; ++r) v[r] = sm[pad(base + 208 * r)];
+        for (int r = 0; r < 11; ++r) v[r] = sm[padb(base + 208 * r)];
 #pragma unroll
-        for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], T.t2288[tp(k * r)]);
+        for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], T.t11[208 * (r - 1) + k]);
         dft<11, false>(v);
 #pragma unroll
-        for (int r = 0; r < 11; ++r) sm[pad(base + 208 * r)] = v[r];
+        for (int r = 0; r < 11; ++r) sm[padb(base + 208 * r)] = v[r];
     }
     __syncthreads();
     // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
     for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
         float2 v[8];
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = sm[pad(k + 2288 * r)];
+        for (int r = 0; r < 8; ++r) v[r] = sm[padb(k + 2288 * r)];
         float2 S[4];
 #pragma unroll
         for (int q = 1; q < 4; ++q) S[q] = tw2(T.h18304, T.l18304, k * q);
@@ -196,7 +232,7 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         }
         dft<8, false>(v);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) sm[pad(k + 2288 * r)] = v[r];
+        for (int r = 0; r < 8; ++r) sm[padb(k + 2288 * r)] = v[r];
     }
     __syncthreads();
 }
@@ -207,8 +243,8 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
 __device__ __forceinline__ float2 r2c_bin(const float2 *sm, int q, float2 w) {
     const int qa = q == kMB ? 0 : q;
     const int qb = q == 0 ? 0 : kMB - q;
-    const float2 za = sm[pad(qa)];
-    const float2 zb = conjf2(sm[pad(qb)]);
+    const float2 za = sm[padb(qa)];
+    const float2 zb = conjf2(sm[padb(qb)]);
     const float2 s = cadd(za, zb), d = csub(za, zb);
     const float2 wd = cmul(w, d);
     return make_float2(0.5f * (s.x + wd.y), 0.5f * (s.y - wd.x));
@@ -293,7 +329,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *sp = reinterpret_cast<uint32_t *>(smem_raw);  // [2][2048] double buffer
     float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
-    TabsA T{sm + kPadA, sm + kPadA + kT1024, sm + kPadA + kT1024 + kT128};
+    TabsA T{sm + kPadA, sm + kPadA + kT32, sm + kPadA + kT32 + kT128};
     load_tabs_a(T, tw);
     const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
@@ -357,7 +393,7 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
-    TabsA TA{tb, tb + kT1024, tb + kT1024 + kT128};
+    TabsA TA{tb, tb + kT32, tb + kT32 + kT128};
     TabsB TB = tabs_b_at(tb);
     __shared__ double red[64];
     load_tabs_a(TA, tw);
@@ -380,32 +416,32 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
             if (q == 0) {
                 const float2 z0 = sm[0];
                 sm[0] = make_float2(z0.x + z0.y, 0.f);
-                sm[pad(kMB)] = make_float2(z0.x - z0.y, 0.f);
+                sm[padb(kMB)] = make_float2(z0.x - z0.y, 0.f);
             } else {
                 float2 xq, xmq;
-                r2c_pair(sm[pad(q)], sm[pad(kMB - q)], __ldg(tw.w36608 + q), xq, xmq);
-                sm[pad(q)] = xq;
-                if (q != kMB / 2) sm[pad(kMB - q)] = xmq;
+                r2c_pair(sm[padb(q)], sm[padb(kMB - q)], __ldg(tw.w36608 + q), xq, xmq);
+                sm[padb(q)] = xq;
+                if (q != kMB / 2) sm[padb(kMB - q)] = xmq;
             }
         }
         __syncthreads();
         // C2R pre-processing in place on the window Y[j] = X[skip + j], j = 0..16384:
         // Z'[j] is stored in the slot of Y[j].
         for (int j = tid; j <= kMA / 2; j += kNTB) {
-            float2 y = sm[pad(skip + j)], ym = sm[pad(skip + kMA - j)];
+            float2 y = sm[padb(skip + j)], ym = sm[padb(skip + kMA - j)];
             if (j == 0) {
                 y.y = 0.f;
                 ym.y = 0.f;
             }
             float2 zk, zmk;
             c2r_pair(y, ym, conjf2(__ldg(tw.w32768 + j)), zk, zmk);
-            sm[pad(skip + j)] = zk;
-            if (j != 0 && j != kMA / 2) sm[pad(skip + kMA - j)] = zmk;
+            sm[padb(skip + j)] = zk;
+            if (j != 0 && j != kMA / 2) sm[padb(skip + kMA - j)] = zmk;
         }
         __syncthreads();
         auto zin = [&](float2 *v) {
 #pragma unroll
-            for (int r = 0; r < 32; ++r) v[r] = sm[pad(skip + tid + 512 * r)];
+            for (int r = 0; r < 32; ++r) v[r] = sm[padb(skip + tid + 512 * r)];
         };
         if constexpr (MODE == 0) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
@@ -475,7 +511,7 @@ __global__ void __launch_bounds__(kNTB, 1)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
-    TabsA TA{tb, tb + kT1024, tb + kT1024 + kT128};
+    TabsA TA{tb, tb + kT32, tb + kT32 + kT128};
     load_tabs_a(TA, tw);
     const int tid = threadIdx.x;
     const float2 wc = conjf2(__ldg(tw.w32768 + tid));
