@@ -54,6 +54,16 @@ extern "C" {
 /* threshold modes */
 #define SDBE_THRESH_FIRST_BATCH 0  /* reference: mean/std of the first batch, set once (.cu:953-986) */
 #define SDBE_THRESH_FIXED 1        /* thresholds supplied by sdbe_set_state                          */
+/* Windowed thresholds (no counterpart in the reference, which sets them
+ * once): batch 0 of the stream sets them as SDBE_THRESH_FIRST_BATCH does;
+ * from then on, at every SDBE_THRESH_BLOCK-batch boundary T of the stream,
+ * the mean and standard deviation of the FP64 statistics of batches
+ * [max(0, T - threshold_window), T) set the thresholds of the next block.
+ * The statistics are gathered in the same pass that quantizes (no extra
+ * read of the floats); waves are cut at block boundaries, so results do not
+ * depend on wave_batches. */
+#define SDBE_THRESH_WINDOW 2
+#define SDBE_THRESH_BLOCK 16
 
 /* channel maps */
 #define SDBE_MAP_APHIDS 0          /* ((c>>1)*16 + (c&1) + 2f)*8, .cu:442                */
@@ -81,7 +91,8 @@ typedef struct sdbe_config {
                                          pol 0's threshold/offset); 0 = each pol its own    */
     int32_t channel_map;       /* SDBE_MAP_*                                                */
     int32_t wave_batches;      /* batches per FFT wave (0 = default); bounds scratch        */
-    int32_t reserved[9];
+    int32_t threshold_window;  /* SDBE_THRESH_WINDOW: batches in the window (0 = 64)        */
+    int32_t reserved[8];
 } sdbe_config;
 
 typedef struct sdbe_state {

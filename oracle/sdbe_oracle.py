@@ -332,12 +332,41 @@ class StreamState:
         self.offset = [0.0, 0.0]
         self.carry = [np.zeros((0, BENG_CHANNELS), np.complex128) for _ in range(2)]
         self.raw = [None, None]   # Mar-2015 format: last unpacked B-frame, held for the next call
+        # windowed thresholds: per pol the (n, mean, M2) of every batch so far and
+        # the (offset, threshold) each batch was quantized with
+        self.batch_stats = [[], []]
+        self.used = [[], []]
+
+
+THRESH_BLOCK = 16   # windowed thresholds move every 16 batches
+
+
+def merge_stats(stats):
+    """(n, mean, M2) of the union of batches given their (n, mean, M2)."""
+    st = np.asarray(stats, np.float64).reshape(-1, 3)
+    n = st[:, 0].sum()
+    mean = (st[:, 0] * st[:, 1]).sum() / n
+    m2 = st[:, 2].sum() + (st[:, 0] * (st[:, 1] - mean) ** 2).sum()
+    return n, mean, m2
+
+
+def window_thresholds(state: StreamState, pol: int, t: int, window: int):
+    """(offset, threshold) for stream batch t in windowed mode (a
+    restatement of this library's SDBE_THRESH_WINDOW; the reference sets the
+    thresholds once): batch 0's own statistics for the first block, then at
+    every block boundary T the statistics of batches [max(0, T - window), T)."""
+    T = (t // THRESH_BLOCK) * THRESH_BLOCK
+    if T == 0:
+        n, mean, m2 = state.batch_stats[pol][0]
+    else:
+        n, mean, m2 = merge_stats(state.batch_stats[pol][max(0, T - window):T])
+    return float(mean), float(np.sqrt(m2 / (n - 1.0)))
 
 
 def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
                   state: StreamState | None = None, precision="f64", workers=1,
                   pol1_uses_pol0_threshold=False, channel_map="aphids",
-                  return_float=False):
+                  return_float=False, threshold_window=None):
     """One call of the GPU stage on ``n_frames`` B-frames of packets.
 
     Follows the body of ``run_method`` (``vdif_inout_gpu_thread.cu:894-1017``):
@@ -347,7 +376,8 @@ def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
     (``vdif_out_databuf.h:110-116``), packet ``iter*128 + k`` holding chunk k
     of batch iter (``.cu:994``).  The reference applies pol 0's threshold to
     pol 1 (``.cu:1004-1005``); ``pol1_uses_pol0_threshold`` reproduces that,
-    the default uses each pol's own.
+    the default uses each pol's own.  ``threshold_window`` (batches) switches
+    to windowed thresholds (``window_thresholds``).
     """
     if state is None:
         state = StreamState()
@@ -373,13 +403,23 @@ def process_group(packets, b_zero: int, n_frames: int, trim_mhz: int,
             block = spec[it * BATCH_SNAPSHOTS:(it + 1) * BATCH_SNAPSHOTS]
             ts = swarm_c2r(block, precision, workers).reshape(-1)
             y = r2dbe_c2r(swarm_r2c(ts, N_B, precision, workers), skip, N_C, precision, workers)
-            if state.threshold[pol] == 0.0:
-                state.offset[pol], state.threshold[pol] = summary_stats(y)
-            th_pol = 0 if pol1_uses_pol0_threshold else pol
-            if pol1_uses_pol0_threshold and state.threshold[0] == 0.0:
-                raise RuntimeError("pol 0 threshold unset")
             cd = np.float32 if precision == "f32" else np.float64
-            codes = quantize2bit_codes(y, state.threshold[th_pol], state.offset[th_pol], cd)
+            if threshold_window:
+                y64 = np.asarray(y, np.float64).ravel()
+                mu = y64.mean()
+                state.batch_stats[pol].append((float(y64.size), float(mu), float(((y64 - mu) ** 2).sum())))
+                t = len(state.batch_stats[pol]) - 1
+                state.offset[pol], state.threshold[pol] = window_thresholds(state, pol, t, threshold_window)
+                state.used[pol].append((state.offset[pol], state.threshold[pol]))
+                off, th = state.used[0][t] if pol1_uses_pol0_threshold else state.used[pol][t]
+                codes = quantize2bit_codes(y, th, off, cd)
+            else:
+                if state.threshold[pol] == 0.0:
+                    state.offset[pol], state.threshold[pol] = summary_stats(y)
+                th_pol = 0 if pol1_uses_pol0_threshold else pol
+                if pol1_uses_pol0_threshold and state.threshold[0] == 0.0:
+                    raise RuntimeError("pol 0 threshold unset")
+                codes = quantize2bit_codes(y, state.threshold[th_pol], state.offset[th_pol], cd)
             words[it * CHUNKS_PER_BATCH:(it + 1) * CHUNKS_PER_BATCH] = pack2bit(codes).reshape(CHUNKS_PER_BATCH, -1)
             if return_float:
                 fl.append(y)

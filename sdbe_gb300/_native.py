@@ -24,7 +24,8 @@ BATCH_SNAPSHOTS = 143
 PKTS_PER_BATCH = 128
 FRAMES_PER_GROUP = 143
 SAMPLES_PER_OUT_PKT = 32768
-THRESH_FIRST_BATCH, THRESH_FIXED = 0, 1
+THRESH_FIRST_BATCH, THRESH_FIXED, THRESH_WINDOW = 0, 1, 2
+THRESH_BLOCK = 16
 MAP_APHIDS, MAP_MAR2015 = 0, 1
 IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED, IN_8PAC = 1, 2, 4, 8, 16, 32, 64
 PAC8_BYTES = 8504
@@ -34,7 +35,8 @@ NOALLOC_MAX_SAMPLES = 134217728
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("trim_mhz", C.c_int32), ("max_frames", C.c_int32),
                 ("threshold_mode", C.c_int32), ("pol1_uses_pol0_threshold", C.c_int32),
-                ("channel_map", C.c_int32), ("wave_batches", C.c_int32), ("reserved", C.c_int32 * 9)]
+                ("channel_map", C.c_int32), ("wave_batches", C.c_int32), ("threshold_window", C.c_int32),
+                ("reserved", C.c_int32 * 8)]
 
 
 class State(C.Structure):

@@ -73,6 +73,8 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->ing_hdr);
     cudaFree(h->reform_dev);
     cudaFree(h->ipfb_tab);
+    cudaFree(h->wring);
+    cudaFree(h->wpart);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
     cudaFree(h->pay);
@@ -411,6 +413,8 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
                                                   t.pol_stride, t.pkt_stride, t.payload_off, 0, st));
                 h->thresholds_set = true;
                 h->launches += 2;
+                h->stream_batch = 0;
+                if (int rc = window_after_wave(h, h->partials, 1, st)) return rc;
                 b[i] = 1;
                 if (!cs[i].aligned)
                     if (int rc = ship_call(cs[i], 0, kChunks)) return rc;
@@ -419,6 +423,8 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
     }
     int wave = h0->wave;
     for (const auto &c : cs) wave = std::min(wave, c.h->wave);
+    bool any_win = false;
+    for (const auto &c : cs) any_win = any_win || c.h->cfg.threshold_mode == SDBE_THRESH_WINDOW;
     while (true) {
         SegsA A{};
         SegsB B{};
@@ -426,7 +432,7 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
         for (int i = 0; i < n; ++i) {
             sdbe_resampler *h = cs[i].h;
             if (b[i] >= cs[i].n_batches) continue;
-            const int64_t nb = std::min<int64_t>(wave, cs[i].n_batches - b[i]);
+            const int64_t nb = wave_len(h, wave, cs[i].n_batches - b[i]);
             A.s[A.n] = SegA{h->spec, h->ts, h->spec_pol_stride, b[i] * kBatchSnaps, nb * kBatchSnaps, h->ts_pol_stride,
                             A.n_items};
             A.n_items += 2 * nb * kBatchSnaps;
@@ -439,6 +445,7 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
             o.payload_off = t.payload_off;
             o.pkt0 = b[i] * kChunks;
             o.thr = h->thr;
+            o.partials = h->cfg.threshold_mode == SDBE_THRESH_WINDOW ? h->wpart : nullptr;
             B.s[B.n] = SegB{h->ts, h->ts_pol_stride, B.n_items, static_cast<int>(nb * kChunks), h->skip, o};
             B.n_items += 2 * nb * kChunks;
             ++B.n;
@@ -450,9 +457,11 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
         SDBE_CK(h0, launch_swarm_c2r_segs(A, h0->tw, st));
         SDBE_CK(h0, timed_end(h0, slot, st));
         SDBE_CK(h0, timed_begin(h0, 1, B.n_items, st, &slot));
-        SDBE_CK(h0, launch_resample_segs(0, B, h0->tw, st));
+        SDBE_CK(h0, launch_resample_segs(any_win ? 3 : 0, B, h0->tw, st));
         SDBE_CK(h0, timed_end(h0, slot, st));
         h0->launches += 2;
+        for (auto [i, nb] : act)
+            if (int rc = window_after_wave(cs[i].h, cs[i].h->wpart, nb, st)) return rc;
         for (auto [i, nb] : act) {
             if (!cs[i].aligned)
                 if (int rc = ship_call(cs[i], b[i] * kChunks, (b[i] + nb) * kChunks)) return rc;
@@ -472,8 +481,11 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
         return fail(nullptr, SDBE_ERR_ARG, "max_frames must be in [1, 65536]");
     const int skip = static_cast<int>(cfg->trim_mhz * 1e6 / (4576e6 / kNB));  // .cu:269
     if (cfg->trim_mhz < 0 || skip > kMaxSkip) return fail(nullptr, SDBE_ERR_ARG, "trim_mhz must be in [0, 240]");
-    if (cfg->threshold_mode != SDBE_THRESH_FIRST_BATCH && cfg->threshold_mode != SDBE_THRESH_FIXED)
+    if (cfg->threshold_mode != SDBE_THRESH_FIRST_BATCH && cfg->threshold_mode != SDBE_THRESH_FIXED &&
+        cfg->threshold_mode != SDBE_THRESH_WINDOW)
         return fail(nullptr, SDBE_ERR_ARG, "unknown threshold_mode");
+    if (cfg->threshold_window < 0 || cfg->threshold_window > (1 << 16))
+        return fail(nullptr, SDBE_ERR_ARG, "threshold_window in [0, 65536]");
     if (cfg->channel_map != SDBE_MAP_APHIDS && cfg->channel_map != SDBE_MAP_MAR2015)
         return fail(nullptr, SDBE_ERR_ARG, "unknown channel_map");
     if (cfg->wave_batches < 0 || cfg->wave_batches > 64) return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
@@ -516,6 +528,11 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
               cudaMalloc(&h->fout, 2 * static_cast<size_t>(kChunks) * kNC * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&h->partials, 2 * kChunks * 3 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&h->thr, 8 * sizeof(float)) == cudaSuccess;
+    if (ok && cfg->threshold_mode == SDBE_THRESH_WINDOW) {
+        h->window = cfg->threshold_window > 0 ? cfg->threshold_window : 64;
+        ok = cudaMalloc(&h->wring, 2 * static_cast<size_t>(h->window) * 3 * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&h->wpart, 2 * static_cast<size_t>(h->wave) * kChunks * 3 * sizeof(double)) == cudaSuccess;
+    }
     ok = ok && cudaMalloc(&h->left[0], 2 * kOutWords * sizeof(uint32_t)) == cudaSuccess &&
          cudaMalloc(&h->left[1], 2 * kOutWords * sizeof(uint32_t)) == cudaSuccess;
     if (ok && cfg->channel_map == SDBE_MAP_MAR2015) {
@@ -680,6 +697,7 @@ int sdbe_reset(sdbe_resampler *h) {
     if (!h) return fail(nullptr, SDBE_ERR_ARG, "null handle");
     h->thresholds_set = false;
     h->carry = 0;
+    h->stream_batch = 0;
     h->raw_carry = 0;
     h->n_left = 0;
     h->skip_pending = 0;

@@ -260,6 +260,34 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-thread FP32 sums a, b reduced in FP32 within each warp and in FP64
+// across warps; results valid in thread 0.  scratch >= 2*32 doubles.
+__device__ __forceinline__ void block_sum2_f(float a, float b, double &sa, double &sb, double *scratch) {
+    a = warp_sum_f(a);
+    b = warp_sum_f(b);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        scratch[warp] = a;
+        scratch[32 + warp] = b;
+    }
+    __syncthreads();
+    sa = 0.0;
+    sb = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; ++w) {
+            sa += scratch[w];
+            sb += scratch[32 + w];
+        }
+}
+
 // Sums a and b over the block; result valid in thread 0.  scratch >= 2*32 doubles.
 __device__ __forceinline__ void block_sum2(double &a, double &b, double *scratch) {
     a = warp_sum(a);

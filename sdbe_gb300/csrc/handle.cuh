@@ -71,6 +71,10 @@ struct sdbe_resampler {
     sdbe_ingest_stats ing{};
     bool thresholds_set = false;
     int64_t carry = 0;
+    int64_t stream_batch = 0;     // batches quantized since the stream started (window blocks)
+    int window = 0;               // SDBE_THRESH_WINDOW: batches per window
+    double *wring = nullptr;      // [2][window][3] batch statistics (n, mean, M2)
+    double *wpart = nullptr;      // [2][wave*128][3] chunk statistics of one wave
     // Mar-2015 format: unpacked frames land here first; the last one is held
     // for the next call because output frame f needs input frame f+1.
     uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]
@@ -128,10 +132,42 @@ struct PayloadTarget {
 // n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,
 // snapshots from 0), payload packets at tgt from packet 0.  on_wave(lo, hi)
 // runs after the waves that completed packets [lo, hi) are queued.
+// Batches the next wave may take from stream batch t: up to `wave`, and with
+// windowed thresholds not past the next block boundary.
+inline int64_t wave_len(const sdbe_resampler *h, int64_t wave, int64_t remaining) {
+    int64_t nb = remaining < wave ? remaining : wave;
+    if (h->cfg.threshold_mode == SDBE_THRESH_WINDOW) {
+        const int64_t to_block = SDBE_THRESH_BLOCK - h->stream_batch % SDBE_THRESH_BLOCK;
+        if (nb > to_block) nb = to_block;
+    }
+    return nb;
+}
+
+// After a wave of nb batches from stream batch t0 was quantized: windowed
+// thresholds take in its statistics (and move at a block boundary).
+inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t nb, cudaStream_t st) {
+    if (h->cfg.threshold_mode != SDBE_THRESH_WINDOW) {
+        h->stream_batch += nb;
+        return SDBE_OK;
+    }
+    const int64_t t0 = h->stream_batch;
+    const bool update = (t0 + nb) % SDBE_THRESH_BLOCK == 0;
+    SDBE_CK(h, launch_window_update(partials, static_cast<int>(nb), t0, h->wring, h->window, update,
+                                    h->cfg.pol1_uses_pol0_threshold, h->thr, st));
+    h->launches += 1;
+    h->stream_batch += nb;
+    return SDBE_OK;
+}
+
+// First-batch threshold path (if thresholds are unset) and the FFT waves over
+// n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,
+// snapshots from 0), payload packets at tgt from packet 0.  on_wave(lo, hi)
+// runs after the waves that completed packets [lo, hi) are queued.
 template <class OnWave>
 int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
               const PayloadTarget &tgt, cudaStream_t st, OnWave on_wave) {
     int64_t b = 0;
+    const bool win = h->cfg.threshold_mode == SDBE_THRESH_WINDOW;
     if (n_batches > 0 && !h->thresholds_set) {
         // First batch: floats + FP64 statistics, thresholds set once (.cu:953-986).
         SDBE_CK(h, launch_swarm_c2r(spec, spec_pol_stride, 0, kBatchSnaps, 2, h->ts, h->ts_pol_stride, h->tw, st));
@@ -145,11 +181,13 @@ int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, 
                                           tgt.pol_stride, tgt.pkt_stride, tgt.payload_off, 0, st));
         h->thresholds_set = true;
         h->launches += 4;
+        h->stream_batch = 0;
+        if (int rc = window_after_wave(h, h->partials, 1, st)) return rc;
         b = 1;
         if (int rc = on_wave(0, kChunks)) return rc;
     }
-    for (; b < n_batches; b += h->wave) {
-        const int64_t nb = n_batches - b < h->wave ? n_batches - b : h->wave;
+    while (b < n_batches) {
+        const int64_t nb = wave_len(h, h->wave, n_batches - b);
         size_t slot;
         SDBE_CK(h, timed_begin(h, 0, 2 * nb * kBatchSnaps, st, &slot));
         SDBE_CK(h, launch_swarm_c2r(spec, spec_pol_stride, b * kBatchSnaps, nb * kBatchSnaps, 2, h->ts,
@@ -163,10 +201,13 @@ int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, 
         o.payload_off = tgt.payload_off;
         o.pkt0 = b * kChunks;
         o.thr = h->thr;
-        SDBE_CK(h, launch_resample(0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
+        o.partials = win ? h->wpart : nullptr;
+        SDBE_CK(h, launch_resample(win ? 3 : 0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
         SDBE_CK(h, timed_end(h, slot, st));
         h->launches += 2;
+        if (int rc = window_after_wave(h, h->wpart, nb, st)) return rc;
         if (int rc = on_wave(b * kChunks, (b + nb) * kChunks)) return rc;
+        b += nb;
     }
     return SDBE_OK;
 }

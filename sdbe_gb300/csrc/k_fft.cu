@@ -388,6 +388,9 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
 //   MODE 1: floats to fout + p*fout_pol_stride + c*32768 and per-chunk
 //           (n, mean, M2) in FP64 to partials[(p*n_chunks + c)*3].
 //   MODE 2: floats only.
+//   MODE 3: MODE 0, plus the (n, mean, M2) of each chunk's floats (FP32
+//           sums per thread and warp, FP64 across warps) to partials when
+//           the segment has them (windowed thresholds).
 template <int MODE>
 __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ SegsB S, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -443,10 +446,11 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
 #pragma unroll
             for (int r = 0; r < 32; ++r) v[r] = sm[padb(skip + tid + 512 * r)];
         };
-        if constexpr (MODE == 0) {
+        if constexpr (MODE == 0 || MODE == 3) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
                                                            (o.pkt0 + c) * o.pkt_stride + o.payload_off);
             const float th = o.thr[pol], off = o.thr[2 + pol];
+            float f1 = 0.f, f2 = 0.f;
             auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
                 for (int r = 0; r < 16; ++r) {
@@ -455,9 +459,27 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
                     q |= __shfl_xor_sync(0xffffffffu, q, 2);
                     q |= __shfl_xor_sync(0xffffffffu, q, 4);
                     if ((jj & 7) == 0) words[(jj >> 3) + 128 * r] = q;
+                    if constexpr (MODE == 3) {
+                        f1 += u[r].x + u[r].y;
+                        f2 = fmaf(u[r].x, u[r].x, fmaf(u[r].y, u[r].y, f2));
+                    }
                 }
             };
             ifft16384(sm, TA, zin, epi);
+            if constexpr (MODE == 3) {
+                if (o.partials != nullptr) {  // uniform over the block
+                    double s1, s2;
+                    block_sum2_f(f1, f2, s1, s2, red);
+                    if (tid == 0) {
+                        const double n = static_cast<double>(kNC);
+                        const double mean = s1 / n;
+                        double *pp = o.partials + (static_cast<int64_t>(pol) * n_chunks + c) * 3;
+                        pp[0] = n;
+                        pp[1] = mean;
+                        pp[2] = s2 - s1 * mean;
+                    }
+                }
+            }
         } else {
             float2 *fo = reinterpret_cast<float2 *>(o.fout + pol * o.fout_pol_stride + c * kNC);
             double s1 = 0.0, s2 = 0.0;
@@ -588,6 +610,69 @@ __global__ void k_finalize_thresholds(const double *__restrict__ partials, int n
     }
 }
 
+// Windowed thresholds, one warp per pol.  Pushes the statistics of the nb
+// batches just quantized (partials [pol][nb*128][3]) into the ring of batch
+// statistics (slot t mod W, FP64), then, if `update`, sets the thresholds
+// from batches [max(0, T-W), T), T = t0 + nb, each lane merging its batches
+// in order and a fixed butterfly merging the lanes (deterministic).
+__global__ void k_window_update(const double *__restrict__ partials, int nb, int64_t t0, double *__restrict__ ring,
+                                int W, int update, int pol1_uses_pol0, float *__restrict__ thr_state) {
+    __shared__ float th_s[2], off_s[2];
+    const int pol = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_chunks = nb * kChunks;
+    if (pol < 2) {
+        for (int b = 0; b < nb; ++b) {
+            Moments m{0.0, 0.0, 0.0};
+            for (int c = lane; c < kChunks; c += 32) {
+                const double *pp = partials + (static_cast<int64_t>(pol) * n_chunks + b * kChunks + c) * 3;
+                m = merge_moments(m, Moments{pp[0], pp[1], pp[2]});
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                Moments other{__shfl_xor_sync(0xffffffffu, m.n, o), __shfl_xor_sync(0xffffffffu, m.mean, o),
+                              __shfl_xor_sync(0xffffffffu, m.m2, o)};
+                m = (lane & o) ? merge_moments(other, m) : merge_moments(m, other);
+            }
+            if (lane == 0) {
+                double *slot = ring + (static_cast<int64_t>(pol) * W + (t0 + b) % W) * 3;
+                slot[0] = m.n;
+                slot[1] = m.mean;
+                slot[2] = m.m2;
+            }
+        }
+        __syncwarp();
+        if (update) {
+            const int64_t T = t0 + nb, lo = T - W > 0 ? T - W : 0;
+            Moments m{0.0, 0.0, 0.0};
+            for (int64_t t = lo + lane; t < T; t += 32) {
+                const double *slot = ring + (static_cast<int64_t>(pol) * W + t % W) * 3;
+                m = merge_moments(m, Moments{slot[0], slot[1], slot[2]});
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                Moments other{__shfl_xor_sync(0xffffffffu, m.n, o), __shfl_xor_sync(0xffffffffu, m.mean, o),
+                              __shfl_xor_sync(0xffffffffu, m.m2, o)};
+                m = (lane & o) ? merge_moments(other, m) : merge_moments(m, other);
+            }
+            if (lane == 0) {
+                th_s[pol] = static_cast<float>(sqrt(m.m2 / (m.n - 1.0)));
+                off_s[pol] = static_cast<float>(m.mean);
+            }
+        }
+    }
+    __syncthreads();
+    if (update && threadIdx.x == 0) {
+        thr_state[4] = th_s[0];
+        thr_state[5] = th_s[1];
+        thr_state[6] = off_s[0];
+        thr_state[7] = off_s[1];
+        thr_state[0] = th_s[0];
+        thr_state[1] = pol1_uses_pol0 ? th_s[0] : th_s[1];
+        thr_state[2] = off_s[0];
+        thr_state[3] = pol1_uses_pol0 ? off_s[0] : off_s[1];
+    }
+}
+
 // quantize2bit over float chunks: each thread packs 16 samples into one word.
 // grid (n_chunks*2048/256, 2 pols).
 __global__ void k_quantize_chunks(const float *__restrict__ fin, int64_t fin_pol_stride, int64_t n_words,
@@ -688,6 +773,8 @@ cudaError_t configure_fft_kernels() {
         return e;
     if ((e = cudaFuncSetAttribute(k_resample<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemB))) != cudaSuccess)
         return e;
+    if ((e = cudaFuncSetAttribute(k_resample<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemB))) != cudaSuccess)
+        return e;
     if ((e = cudaFuncSetAttribute(k_resample<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemB))) != cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(k_resample<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemB))) != cudaSuccess)
@@ -724,6 +811,8 @@ cudaError_t launch_resample_segs(int mode, const SegsB &S, const Twiddles &tw, c
     const unsigned grid = persistent_grid(S.n_items);
     if (mode == 0)
         k_resample<0><<<grid, kNTB, kSmemB, st>>>(S, tw);
+    else if (mode == 3)
+        k_resample<3><<<grid, kNTB, kSmemB, st>>>(S, tw);
     else if (mode == 1)
         k_resample<1><<<grid, kNTB, kSmemB, st>>>(S, tw);
     else
@@ -762,6 +851,12 @@ cudaError_t launch_r2dbe_c2r(const void *in, int64_t in_stride, int64_t n_chunks
     if (n_chunks <= 0) return cudaSuccess;
     k_r2dbe_c2r<<<persistent_grid(n_chunks), kNTB, kSmemB, st>>>(static_cast<const float2 *>(in), in_stride, n_chunks,
                                                                   skip, out, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_window_update(const double *partials, int nb, int64_t t0, double *ring, int W, bool update,
+                                 int pol1_uses_pol0, float *thr_state, cudaStream_t st) {
+    k_window_update<<<1, 64, 0, st>>>(partials, nb, t0, ring, W, update ? 1 : 0, pol1_uses_pol0, thr_state);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,7 @@ cudaError_t launch_resample(int, const float *, int64_t, int, int64_t, int, cons
 cudaError_t launch_swarm_r2c(const float *, int64_t, void *, const Twiddles &, cudaStream_t);
 cudaError_t launch_r2dbe_c2r(const void *, int64_t, int64_t, int, float *, const Twiddles &, cudaStream_t);
 cudaError_t launch_finalize_thresholds(const double *, int, int, float *, cudaStream_t);
+cudaError_t launch_window_update(const double *, int, int64_t, double *, int, bool, int, float *, cudaStream_t);
 cudaError_t launch_quantize_chunks(const float *, int64_t, int64_t, const float *, uint8_t *, int64_t, int64_t,
                                    int64_t, int64_t, cudaStream_t);
 cudaError_t launch_quantize_flat(const float *, uint32_t *, int64_t, float, float, cudaStream_t);
