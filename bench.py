@@ -460,6 +460,127 @@ def run_streams(args):
     return 0
 
 
+def run_stress(args):
+    """--workload stress32: 32 streams (16 packet streams x 2 phased sums) x
+    2048 B-frames with 1% dropped and 0.5% displaced packets and sigma x4
+    noise bursts on 1% of snapshots, windowed thresholds (64 batches).  The
+    streams run as consecutive 143-frame groups, all 16 in one
+    sdbe_process_multi pass per group; 15 passes cover the 2048 frames.  Two
+    distinct groups per stream are generated and resident in HBM (the
+    generator is far slower than the stage) and alternate."""
+    import torch
+
+    rank, local_rank, world = _env_rank()
+    torch.cuda.set_device(local_rank)
+    if rank != 0 and world > 1:
+        return 0
+    from sdbe_gb300 import Resampler, host_buffer, process_multi, synth
+    from sdbe_gb300 import _native as N
+
+    G = 143
+    n_streams = 16
+    specs = synth.config5(n_packet_streams=n_streams, n_frames=2048)
+    pool = [[synth.generate(sp, frame_offset=g * G, n_frames=G) for g in range(2)] for sp in specs]
+    d_pool = [[torch.from_numpy(p).cuda() for p in row] for row in pool]
+    wave = args.wave or 16
+    hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=G, wave_batches=wave,
+                    threshold_mode=N.THRESH_WINDOW, threshold_window=64) for _ in specs]
+    out_bytes = hs[0].output_bytes(G)
+    outs = [torch.empty(out_bytes, dtype=torch.uint8, device="cuda") for _ in hs]
+    stream = torch.cuda.Stream()
+    n_passes = -(-2048 // G)  # 15
+
+    def one_pass(i, want=False):
+        g = i % 2
+        items = [(d_pool[s][g], G, specs[s].b_start + g * G, outs[s]) for s in range(n_streams)]
+        return process_multi(hs, items, stream=stream.cuda_stream, want_results=want)
+
+    for h in hs:
+        h.reset()
+    _, res = one_pass(0, want=True)
+    accepted = sum(r.packets_accepted for r in res)
+    incomplete = sum(r.frames_incomplete for r in res)
+    for i in range(1, max(args.warmup, 3)):
+        one_pass(i)
+    torch.cuda.synchronize()
+    # samples per pass: the 128 batches of a group for every stream and pol
+    samples = n_streams * 2 * 128 * OUT_SAMPLES_PER_BATCH
+    for h in hs:
+        h.read_profile()
+    hs[0].profile(True)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for h in hs:
+        h.reset()  # a fresh 2048-frame run: thresholds from its first batch, then windowed
+    e0.record(stream)
+    for i in range(n_passes):
+        one_pass(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    profs = [h.read_profile() for h in hs]
+    hs[0].profile(False)
+    prof = profs[0]
+    ms_total = e0.elapsed_time(e1)
+    value = n_passes * samples / (ms_total * 1e-3) / 1e9
+    st = hs[0].get_state()
+    # end to end: pinned host groups, passes queued asynchronously
+    h_pool = []
+    for row in pool:
+        hrow = []
+        for p in row:
+            hb = host_buffer(p.nbytes).reshape(p.shape)
+            hb[...] = p
+            hrow.append(hb)
+        h_pool.append(hrow)
+    h_out = [host_buffer(out_bytes) for _ in hs]
+    for h in hs:
+        h.reset()
+    t0 = time.perf_counter()
+    for i in range(n_passes):
+        g = i % 2
+        process_multi(hs, [(h_pool[s][g], G, specs[s].b_start + g * G, h_out[s]) for s in range(n_streams)],
+                      asynchronous=True)
+    for h in hs:
+        h.sync()
+    e2e_s = time.perf_counter() - t0
+    peak, peak_kind = _load_peaks()
+    bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
+    bc_bytes = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) * (36608 * 4 + 8192)
+    achieved = bc_bytes / (bc_ms * 1e-3) / 1e9 if bc_ms else None
+    pkt_bytes = sum(p.nbytes for p in (row[0] for row in pool))
+    whole_bytes = n_passes * (pkt_bytes + n_streams * out_bytes)
+    line = {
+        "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": 1, "steps": n_passes,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_total / n_passes, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "32 streams (16 packet streams x 2 phased sums) x 2048 B-frames in 143-frame "
+                               "groups; 1% dropped, 0.5% displaced (<= 64) packets, sigma x4 bursts on 1% of "
+                               "snapshots; windowed thresholds (64 batches); one sdbe_process_multi pass per group",
+                   "packet_streams": n_streams, "frames_per_stream": n_passes * G, "wave_batches": wave,
+                   "packets_accepted_first_pass": int(accepted), "frames_incomplete_first_pass": int(incomplete),
+                   "l2": "inputs larger than L2 (4.9 GB of packets per pass)"},
+        "x_realtime": value / (REALTIME_GSPS * 2 * n_streams),
+        "whole_pipeline_hbm": {"algorithmic_gbs": whole_bytes / (ms_total * 1e-3) / 1e9, "peak": peak,
+                               "frac": whole_bytes / (ms_total * 1e-3) / 1e9 / peak},
+        "roofline": {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
+                     "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes},
+        "thresholds_after_run": {"pol0": float(st.threshold[0]), "pol1": float(st.threshold[1])},
+        "stage_ms_per_step": {"stage_a": prof.stage_a_ms / n_passes, "stage_bc": prof.stage_bc_ms / n_passes},
+        "e2e": {"value": n_passes * samples / e2e_s / 1e9, "unit": "GS/s", "ms_per_step": e2e_s / n_passes * 1e3,
+                "h2d_bytes_per_step": int(pkt_bytes), "d2h_bytes_per_step": int(n_streams * out_bytes),
+                "api": "process_multi(host pinned buffers, asynchronous) per group, sdbe_sync at the end"},
+        "gpu_launches": int(sum(int(q.launches) for q in profs)),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    for h in hs:
+        h.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -469,13 +590,16 @@ def main():
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--workload", default="group512", choices=["group512", "streams8"],
-                    help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi pass")
+    ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
+                    help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
+                         "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "streams8":
         return run_streams(args)
+    if args.workload == "stress32":
+        return run_stress(args)
     return run_ours(args)
 
 

@@ -405,6 +405,7 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
             SDBE_CK(h0, launch_swarm_c2r_segs(A, h0->tw, st));
             SDBE_CK(h0, launch_resample_segs(1, B, h0->tw, st));
             h0->launches += 2;
+            WinUpds U{};
             for (int i : first) {
                 sdbe_resampler *h = cs[i].h;
                 const PayloadTarget &t = cs[i].pt;
@@ -414,10 +415,14 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
                 h->thresholds_set = true;
                 h->launches += 2;
                 h->stream_batch = 0;
-                if (int rc = window_after_wave(h, h->partials, 1, st)) return rc;
+                window_step(h, h->partials, 1, true, U);
                 b[i] = 1;
                 if (!cs[i].aligned)
                     if (int rc = ship_call(cs[i], 0, kChunks)) return rc;
+            }
+            if (U.n) {
+                SDBE_CK(h0, launch_window_update(U, st));
+                h0->launches += 1;
             }
         }
     }
@@ -460,8 +465,12 @@ int fft_chain_multi(std::vector<CallPlan> &cs) {
         SDBE_CK(h0, launch_resample_segs(any_win ? 3 : 0, B, h0->tw, st));
         SDBE_CK(h0, timed_end(h0, slot, st));
         h0->launches += 2;
-        for (auto [i, nb] : act)
-            if (int rc = window_after_wave(cs[i].h, cs[i].h->wpart, nb, st)) return rc;
+        WinUpds U{};
+        for (auto [i, nb] : act) window_step(cs[i].h, cs[i].h->wpart, nb, false, U);
+        if (U.n) {
+            SDBE_CK(h0, launch_window_update(U, st));
+            h0->launches += 1;
+        }
         for (auto [i, nb] : act) {
             if (!cs[i].aligned)
                 if (int rc = ship_call(cs[i], b[i] * kChunks, (b[i] + nb) * kChunks)) return rc;

@@ -128,12 +128,8 @@ struct PayloadTarget {
     int64_t pol_stride, pkt_stride, payload_off;
 };
 
-// First-batch threshold path (if thresholds are unset) and the FFT waves over
-// n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,
-// snapshots from 0), payload packets at tgt from packet 0.  on_wave(lo, hi)
-// runs after the waves that completed packets [lo, hi) are queued.
-// Batches the next wave may take from stream batch t: up to `wave`, and with
-// windowed thresholds not past the next block boundary.
+// Batches the next wave may take: up to `wave` of the `remaining`, and with
+// windowed thresholds not past the stream's next block boundary.
 inline int64_t wave_len(const sdbe_resampler *h, int64_t wave, int64_t remaining) {
     int64_t nb = remaining < wave ? remaining : wave;
     if (h->cfg.threshold_mode == SDBE_THRESH_WINDOW) {
@@ -143,19 +139,24 @@ inline int64_t wave_len(const sdbe_resampler *h, int64_t wave, int64_t remaining
     return nb;
 }
 
-// After a wave of nb batches from stream batch t0 was quantized: windowed
-// thresholds take in its statistics (and move at a block boundary).
-inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t nb, cudaStream_t st) {
-    if (h->cfg.threshold_mode != SDBE_THRESH_WINDOW) {
-        h->stream_batch += nb;
-        return SDBE_OK;
+// After a wave of nb batches was quantized: the handle's windowed-threshold
+// step (appended to U, launched by the caller) and its batch counter.
+inline void window_step(sdbe_resampler *h, const double *partials, int64_t nb, bool moments, WinUpds &U) {
+    if (h->cfg.threshold_mode == SDBE_THRESH_WINDOW) {
+        const int64_t t0 = h->stream_batch;
+        U.u[U.n++] = WinUpd{partials, h->wring, h->thr, t0, static_cast<int>(nb), h->window,
+                            (t0 + nb) % SDBE_THRESH_BLOCK == 0 ? 1 : 0, h->cfg.pol1_uses_pol0_threshold,
+                            moments ? 1 : 0};
     }
-    const int64_t t0 = h->stream_batch;
-    const bool update = (t0 + nb) % SDBE_THRESH_BLOCK == 0;
-    SDBE_CK(h, launch_window_update(partials, static_cast<int>(nb), t0, h->wring, h->window, update,
-                                    h->cfg.pol1_uses_pol0_threshold, h->thr, st));
-    h->launches += 1;
     h->stream_batch += nb;
+}
+
+inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t nb, bool moments, cudaStream_t st) {
+    WinUpds U{};
+    window_step(h, partials, nb, moments, U);
+    if (U.n == 0) return SDBE_OK;
+    SDBE_CK(h, launch_window_update(U, st));
+    h->launches += 1;
     return SDBE_OK;
 }
 
@@ -182,7 +183,7 @@ int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, 
         h->thresholds_set = true;
         h->launches += 4;
         h->stream_batch = 0;
-        if (int rc = window_after_wave(h, h->partials, 1, st)) return rc;
+        if (int rc = window_after_wave(h, h->partials, 1, true, st)) return rc;
         b = 1;
         if (int rc = on_wave(0, kChunks)) return rc;
     }
@@ -205,7 +206,7 @@ int fft_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, 
         SDBE_CK(h, launch_resample(win ? 3 : 0, h->ts, h->ts_pol_stride, h->skip, nb * kChunks, 2, o, h->tw, st));
         SDBE_CK(h, timed_end(h, slot, st));
         h->launches += 2;
-        if (int rc = window_after_wave(h, h->wpart, nb, st)) return rc;
+        if (int rc = window_after_wave(h, h->wpart, nb, false, st)) return rc;
         if (int rc = on_wave(b * kChunks, (b + nb) * kChunks)) return rc;
         b += nb;
     }

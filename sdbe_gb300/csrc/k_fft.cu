@@ -388,9 +388,9 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
 //   MODE 1: floats to fout + p*fout_pol_stride + c*32768 and per-chunk
 //           (n, mean, M2) in FP64 to partials[(p*n_chunks + c)*3].
 //   MODE 2: floats only.
-//   MODE 3: MODE 0, plus the (n, mean, M2) of each chunk's floats (FP32
-//           sums per thread and warp, FP64 across warps) to partials when
-//           the segment has them (windowed thresholds).
+//   MODE 3: MODE 0, plus the (n, sum, sum of squares) of each chunk's
+//           floats (FP32 per thread and warp, FP64 across warps) to partials
+//           when the segment has them (windowed thresholds).
 template <int MODE>
 __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ SegsB S, Twiddles tw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -471,12 +471,10 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
                     double s1, s2;
                     block_sum2_f(f1, f2, s1, s2, red);
                     if (tid == 0) {
-                        const double n = static_cast<double>(kNC);
-                        const double mean = s1 / n;
                         double *pp = o.partials + (static_cast<int64_t>(pol) * n_chunks + c) * 3;
-                        pp[0] = n;
-                        pp[1] = mean;
-                        pp[2] = s2 - s1 * mean;
+                        pp[0] = static_cast<double>(kNC);
+                        pp[1] = s1;
+                        pp[2] = s2;
                     }
                 }
             }
@@ -610,66 +608,81 @@ __global__ void k_finalize_thresholds(const double *__restrict__ partials, int n
     }
 }
 
-// Windowed thresholds, one warp per pol.  Pushes the statistics of the nb
-// batches just quantized (partials [pol][nb*128][3]) into the ring of batch
-// statistics (slot t mod W, FP64), then, if `update`, sets the thresholds
-// from batches [max(0, T-W), T), T = t0 + nb, each lane merging its batches
-// in order and a fixed butterfly merging the lanes (deterministic).
-__global__ void k_window_update(const double *__restrict__ partials, int nb, int64_t t0, double *__restrict__ ring,
-                                int W, int update, int pol1_uses_pol0, float *__restrict__ thr_state) {
-    __shared__ float th_s[2], off_s[2];
-    const int pol = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_chunks = nb * kChunks;
-    if (pol < 2) {
-        for (int b = 0; b < nb; ++b) {
-            Moments m{0.0, 0.0, 0.0};
-            for (int c = lane; c < kChunks; c += 32) {
-                const double *pp = partials + (static_cast<int64_t>(pol) * n_chunks + b * kChunks + c) * 3;
-                m = merge_moments(m, Moments{pp[0], pp[1], pp[2]});
-            }
+// Windowed thresholds: one CTA per handle, warps 0-3 pol 0 and 4-7 pol 1.
+// Pushes the (n, sum, sum of squares) of each of the nb batches just
+// quantized (128 chunk partials each, [pol][nb*128][3]; the first batch's
+// partials are (n, mean, M2) and are converted) into the handle's FP64 ring
+// (slot t mod W), then, if `update`, sets the thresholds from the sums over
+// batches [max(0, T-W), T), T = t0 + nb.  Plain FP64 sums in a fixed order:
+// no division but the final mean and variance.
+__device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                Moments other{__shfl_xor_sync(0xffffffffu, m.n, o), __shfl_xor_sync(0xffffffffu, m.mean, o),
-                              __shfl_xor_sync(0xffffffffu, m.m2, o)};
-                m = (lane & o) ? merge_moments(other, m) : merge_moments(m, other);
-            }
-            if (lane == 0) {
-                double *slot = ring + (static_cast<int64_t>(pol) * W + (t0 + b) % W) * 3;
-                slot[0] = m.n;
-                slot[1] = m.mean;
-                slot[2] = m.m2;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_window_update(const __grid_constant__ WinUpds U) {
+    const WinUpd &u = U.u[blockIdx.x];
+    __shared__ float th_s[2], off_s[2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pol = warp >> 2, wq = warp & 3;
+    const int64_t n_chunks = static_cast<int64_t>(u.nb) * kChunks;
+    for (int b = wq; b < u.nb; b += 4) {
+        double n = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int c = lane; c < kChunks; c += 32) {
+            const double *pp = u.partials + (pol * n_chunks + static_cast<int64_t>(b) * kChunks + c) * 3;
+            if (u.moments) {  // (n, mean, M2)
+                const double cn = pp[0], cm = pp[1];
+                n += cn;
+                s1 += cn * cm;
+                s2 += pp[2] + cn * cm * cm;
+            } else {
+                n += pp[0];
+                s1 += pp[1];
+                s2 += pp[2];
             }
         }
-        __syncwarp();
-        if (update) {
-            const int64_t T = t0 + nb, lo = T - W > 0 ? T - W : 0;
-            Moments m{0.0, 0.0, 0.0};
-            for (int64_t t = lo + lane; t < T; t += 32) {
-                const double *slot = ring + (static_cast<int64_t>(pol) * W + t % W) * 3;
-                m = merge_moments(m, Moments{slot[0], slot[1], slot[2]});
-            }
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                Moments other{__shfl_xor_sync(0xffffffffu, m.n, o), __shfl_xor_sync(0xffffffffu, m.mean, o),
-                              __shfl_xor_sync(0xffffffffu, m.m2, o)};
-                m = (lane & o) ? merge_moments(other, m) : merge_moments(m, other);
-            }
-            if (lane == 0) {
-                th_s[pol] = static_cast<float>(sqrt(m.m2 / (m.n - 1.0)));
-                off_s[pol] = static_cast<float>(m.mean);
-            }
+        n = warp_sum_d(n);
+        s1 = warp_sum_d(s1);
+        s2 = warp_sum_d(s2);
+        if (lane == 0) {
+            double *slot = u.ring + (static_cast<int64_t>(pol) * u.W + (u.t0 + b) % u.W) * 3;
+            slot[0] = n;
+            slot[1] = s1;
+            slot[2] = s2;
         }
     }
     __syncthreads();
-    if (update && threadIdx.x == 0) {
-        thr_state[4] = th_s[0];
-        thr_state[5] = th_s[1];
-        thr_state[6] = off_s[0];
-        thr_state[7] = off_s[1];
-        thr_state[0] = th_s[0];
-        thr_state[1] = pol1_uses_pol0 ? th_s[0] : th_s[1];
-        thr_state[2] = off_s[0];
-        thr_state[3] = pol1_uses_pol0 ? off_s[0] : off_s[1];
+    if (!u.update) return;  // uniform over the CTA
+    if (wq == 0) {
+        const int64_t T = u.t0 + u.nb, lo = T - u.W > 0 ? T - u.W : 0;
+        double n = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int64_t t = lo + lane; t < T; t += 32) {
+            const double *slot = u.ring + (static_cast<int64_t>(pol) * u.W + t % u.W) * 3;
+            n += slot[0];
+            s1 += slot[1];
+            s2 += slot[2];
+        }
+        n = warp_sum_d(n);
+        s1 = warp_sum_d(s1);
+        s2 = warp_sum_d(s2);
+        if (lane == 0) {
+            const double mean = s1 / n;
+            th_s[pol] = static_cast<float>(sqrt((s2 - s1 * mean) / (n - 1.0)));
+            off_s[pol] = static_cast<float>(mean);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float *t = u.thr;
+        t[4] = th_s[0];
+        t[5] = th_s[1];
+        t[6] = off_s[0];
+        t[7] = off_s[1];
+        t[0] = th_s[0];
+        t[1] = u.pol1 ? th_s[0] : th_s[1];
+        t[2] = off_s[0];
+        t[3] = u.pol1 ? off_s[0] : off_s[1];
     }
 }
 
@@ -854,9 +867,10 @@ cudaError_t launch_r2dbe_c2r(const void *in, int64_t in_stride, int64_t n_chunks
     return cudaGetLastError();
 }
 
-cudaError_t launch_window_update(const double *partials, int nb, int64_t t0, double *ring, int W, bool update,
-                                 int pol1_uses_pol0, float *thr_state, cudaStream_t st) {
-    k_window_update<<<1, 64, 0, st>>>(partials, nb, t0, ring, W, update ? 1 : 0, pol1_uses_pol0, thr_state);
+cudaError_t launch_window_update(const WinUpds &U, cudaStream_t st) {
+    if (U.n <= 0) return cudaSuccess;
+    if (U.n > kMaxSegs) return cudaErrorInvalidValue;
+    k_window_update<<<U.n, 256, 0, st>>>(U);
     return cudaGetLastError();
 }
 

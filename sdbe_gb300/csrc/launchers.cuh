@@ -55,7 +55,18 @@ cudaError_t launch_resample(int, const float *, int64_t, int, int64_t, int, cons
 cudaError_t launch_swarm_r2c(const float *, int64_t, void *, const Twiddles &, cudaStream_t);
 cudaError_t launch_r2dbe_c2r(const void *, int64_t, int64_t, int, float *, const Twiddles &, cudaStream_t);
 cudaError_t launch_finalize_thresholds(const double *, int, int, float *, cudaStream_t);
-cudaError_t launch_window_update(const double *, int, int64_t, double *, int, bool, int, float *, cudaStream_t);
+struct WinUpd {  // one handle's windowed-threshold step after a wave
+    const double *partials;  // [2][nb*128][3]
+    double *ring;            // [2][W][3]
+    float *thr;
+    int64_t t0;              // stream batch of the wave's first batch
+    int nb, W, update, pol1, moments;  // moments: partials are (n, mean, M2), else (n, sum, sum of squares)
+};
+struct WinUpds {
+    int n;
+    WinUpd u[kMaxSegs];
+};
+cudaError_t launch_window_update(const WinUpds &, cudaStream_t);
 cudaError_t launch_quantize_chunks(const float *, int64_t, int64_t, const float *, uint8_t *, int64_t, int64_t,
                                    int64_t, int64_t, cudaStream_t);
 cudaError_t launch_quantize_flat(const float *, uint32_t *, int64_t, float, float, cudaStream_t);
