@@ -51,11 +51,15 @@ __device__ __forceinline__ void pack_snapshot(uint32_t wlo, uint32_t whi, uint32
 
 constexpr int kTilePkts = 32;
 
-// 32 packets per CTA.  Phase 1: each warp loads 4 packets with coalesced
-// 16-B loads (lane l owns snapshots 4l..4l+3) and writes their packed words to
-// a [pol][packet][snapshot-quad] tile swizzled by quad ^ packet.  Phase 2:
-// lanes = packets, so each store instruction writes the 32 packets' channel
-// groups of one snapshot row (128 contiguous bytes for in-order packets).
+// 32 packets per CTA.  Phase 1: each warp issues the loads of all 4 of its
+// packets first (headers broadcast, payloads as coalesced 16-B loads: lane l
+// owns snapshots 4l..4l+3), then writes their packed words to a
+// [pol][packet][snapshot-quad] tile swizzled by quad ^ packet.  Completion
+// bits and per-frame counts are aggregated over the CTA's packets by warp 0
+// (one atomic per distinct bitmap word / frame, not one per packet).
+// Phase 2: lanes = packets, so each store instruction writes the 32 packets'
+// channel groups of one snapshot row (128 contiguous bytes for in-order
+// packets).
 __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict__ pkts, int64_t n_pkts,
                                                        uint64_t b_zero, int n_frames, int map,
                                                        uint32_t *__restrict__ spec, int64_t pol_stride,
@@ -66,47 +70,82 @@ __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict
     __shared__ uint4 tile[2][kTilePkts][32];
     __shared__ int64_t s_row[kTilePkts];
     __shared__ int s_group[kTilePkts];
+    __shared__ int s_frame[kTilePkts];  // -1 not taken, -2 no packet
+    __shared__ uint32_t s_cf[kTilePkts];  // c | f << 8
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t p_base = static_cast<int64_t>(blockIdx.x) * kTilePkts;
 
+    uint32_t w0[4], w4[4], w5[4];
+    uint4 a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int64_t p = p_base + warp * 4 + q;
+        if (p < n_pkts) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(pkts + p * kPktBytes);
+            w0[q] = __ldg(reinterpret_cast<const uint32_t *>(src));
+            const uint4 h1 = __ldg(src + 1);
+            w4[q] = h1.x;
+            w5[q] = h1.y;
+            a[q] = __ldcs(src + 2 + 2 * lane);
+            b[q] = __ldcs(src + 3 + 2 * lane);
+        }
+    }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int pl = warp * 4 + q;
         const int64_t p = p_base + pl;
         int64_t row = -1;
-        int group = 0;
+        int group = 0, frame = -2;
+        uint32_t cf = 0;
         if (p < n_pkts) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(pkts + p * kPktBytes);
-            const uint32_t w0 = __ldg(reinterpret_cast<const uint32_t *>(src));
-            const uint4 h1 = __ldg(src + 1);
-            const PktHeader h = decode_header(w0, h1.x, h1.y, b_zero, n_frames, map);
+            const PktHeader h = decode_header(w0[q], w4[q], w5[q], b_zero, n_frames, map);
             const bool take = h.ok && (accept == nullptr || accept[p] != 0);
-            const uint4 a = __ldcs(src + 2 + 2 * lane);
-            const uint4 b = __ldcs(src + 3 + 2 * lane);
+            frame = -1;
             if (take) {
                 uint4 o0, o1;
-                pack_snapshot(a.x, a.y, o0.x, o1.x);
-                pack_snapshot(a.z, a.w, o0.y, o1.y);
-                pack_snapshot(b.x, b.y, o0.z, o1.z);
-                pack_snapshot(b.z, b.w, o0.w, o1.w);
+                pack_snapshot(a[q].x, a[q].y, o0.x, o1.x);
+                pack_snapshot(a[q].z, a[q].w, o0.y, o1.y);
+                pack_snapshot(b[q].x, b[q].y, o0.z, o1.z);
+                pack_snapshot(b[q].z, b[q].w, o0.w, o1.w);
                 tile[0][pl][lane ^ pl] = o0;
                 tile[1][pl][lane ^ pl] = o1;
                 row = snap0 + h.frame * kSnapsPerFrame;
                 group = h.group;
-                if (lane == 0) {
-                    atomicOr(bitmap + h.frame * 64 + (h.c >> 2), 1u << ((h.c & 3u) * 8u + h.f));
-                    if (counts != nullptr) atomicAdd(counts + h.frame, 1);
-                }
-            } else if (lane == 0 && rejected != nullptr) {
-                atomicAdd(rejected, 1);
+                frame = static_cast<int>(h.frame);
+                cf = h.c | (h.f << 8);
             }
         }
         if (lane == 0) {
             s_row[pl] = row;
             s_group[pl] = group;
+            s_frame[pl] = frame;
+            s_cf[pl] = cf;
         }
     }
     __syncthreads();
+
+    if (warp == 0) {  // lane = packet of the CTA
+        const int frame = s_frame[lane];
+        const uint32_t cf = s_cf[lane];
+        const bool take = frame >= 0;
+        // completion bits: lanes with the same bitmap word OR their bits, the lowest issues the atomic
+        const int key = take ? frame * 64 + static_cast<int>((cf & 0xFFu) >> 2) : -1 - (frame == -2);
+        const uint32_t bit = take ? 1u << (((cf & 0xFFu) & 3u) * 8u + (cf >> 8)) : 0u;
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        uint32_t bits = 0;
+        for (int i = 0; i < 32; ++i) {
+            const uint32_t bi = __shfl_sync(0xffffffffu, bit, i);
+            if ((same >> i) & 1u) bits |= bi;
+        }
+        const bool leader = lane == __ffs(same) - 1;
+        if (take && leader) atomicOr(bitmap + key, bits);
+        if (counts != nullptr) {
+            const unsigned same_f = __match_any_sync(0xffffffffu, take ? frame : -1);
+            if (take && lane == __ffs(same_f) - 1) atomicAdd(counts + frame, __popc(same_f));
+        }
+        const unsigned rej = __ballot_sync(0xffffffffu, frame == -1);
+        if (lane == 0 && rejected != nullptr && rej) atomicAdd(rejected, __popc(rej));
+    }
 
     const int64_t row = s_row[lane];
     const int group = s_group[lane];
