@@ -39,18 +39,24 @@ constexpr int kT128 = tp_len(128);     // two-level halves
 constexpr int kT13 = 12 * 16;          // W_208^{k r}, r = 1..12, k = 0..15   (18304-point radix-13 pass)
 constexpr int kT11 = 10 * 208;         // W_2288^{k r}, r = 1..10, k = 0..207 (18304-point radix-11 pass)
 constexpr int kH18304 = tp_len(143);   // W_18304^{128 a}
-constexpr int kTwA = kT32 + 2 * kT128;                              // stage A tables
-constexpr int kTwB = kTwA + kT13 + kT11 + kH18304 + kT128;          // stage BC tables
+constexpr int kH32768 = tp_len(65);    // W_32768^{128 a}, a <= 64   (C2R pairing, k <= 8192)
+constexpr int kH36608 = tp_len(72);    // W_36608^{128 a}, a <= 71   (R2C pairing, q <= 9152)
+constexpr int kTwA = kT32 + 2 * kT128 + kH32768 + kT128;                       // stage A tables
+constexpr int kTwB = kTwA + kT13 + kT11 + kH18304 + kT128 + kH36608 + kT128;   // stage BC tables
 constexpr size_t kSmemA = 2 * kGroups * sizeof(uint32_t) + (kPadA + kTwA) * sizeof(float2);
 constexpr size_t kSmemB = (kPadB + kTwB) * sizeof(float2);
 
 // ---- table loading --------------------------------------------------------
-struct TabsA {  // inverse-16384 tables
-    float2 *t32, *h16384, *l16384;
+struct TabsA {  // inverse-16384 tables, and the C2R pairing twiddles W_32768^k (two-level)
+    float2 *t32, *h16384, *l16384, *h32768, *l32768;
 };
-struct TabsB {  // forward-18304 tables
-    float2 *t13, *t11, *h18304, *l18304;
+struct TabsB {  // forward-18304 tables, and the R2C pairing twiddles W_36608^q (two-level)
+    float2 *t13, *t11, *h18304, *l18304, *h36608, *l36608;
 };
+
+__device__ __forceinline__ TabsA tabs_a_at(float2 *p) {
+    return TabsA{p, p + kT32, p + kT32 + kT128, p + kT32 + 2 * kT128, p + kT32 + 2 * kT128 + kH32768};
+}
 
 __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
     for (int m = threadIdx.x; m < kT32; m += blockDim.x) {
@@ -61,7 +67,9 @@ __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
     for (int m = threadIdx.x; m < 128; m += blockDim.x) {
         t.h16384[tp(m)] = __ldg(tw.w16384 + 128 * m);
         t.l16384[tp(m)] = __ldg(tw.w16384 + m);
+        t.l32768[tp(m)] = __ldg(tw.w32768 + m);
     }
+    for (int m = threadIdx.x; m < 65; m += blockDim.x) t.h32768[tp(m)] = __ldg(tw.w32768 + 128 * m);
 }
 
 __device__ __forceinline__ void load_tabs_b(TabsB t, const Twiddles &tw) {
@@ -74,12 +82,17 @@ __device__ __forceinline__ void load_tabs_b(TabsB t, const Twiddles &tw) {
         t.t13[m] = __ldg(tw.w18304 + 88 * k * r);
     }
     for (int m = threadIdx.x; m < 143; m += blockDim.x) t.h18304[tp(m)] = __ldg(tw.w18304 + 128 * m);
-    for (int m = threadIdx.x; m < 128; m += blockDim.x) t.l18304[tp(m)] = __ldg(tw.w18304 + m);
+    for (int m = threadIdx.x; m < 128; m += blockDim.x) {
+        t.l18304[tp(m)] = __ldg(tw.w18304 + m);
+        t.l36608[tp(m)] = __ldg(tw.w36608 + m);
+    }
+    for (int m = threadIdx.x; m < 72; m += blockDim.x) t.h36608[tp(m)] = __ldg(tw.w36608 + 128 * m);
 }
 
 __device__ __forceinline__ TabsB tabs_b_at(float2 *tb) {
     float2 *p = tb + kTwA;
-    return TabsB{p, p + kT13, p + kT13 + kT11, p + kT13 + kT11 + kH18304};
+    float2 *q = p + kT13 + kT11 + kH18304 + kT128;
+    return TabsB{p, p + kT13, p + kT13 + kT11, p + kT13 + kT11 + kH18304, q, q + kH36608};
 }
 
 // First-pass lane order of the 18304-point transform: half-warp h takes the
@@ -180,47 +193,51 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
     for (int h = threadIdx.x >> 4; h < 72; h += blockDim.x >> 4) {
         const int g = kFirstPassGroups[2 * h + ((threadIdx.x >> 3) & 1)];
         if (g == 255) continue;
-        const int j = 8 * g + (threadIdx.x & 7);
+        const int c = threadIdx.x & 7, j = 8 * g + c;
         float2 v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = __ldcs(z + j + NB1 * r);
         dft<16, false>(v);
-        const int rho = (j / 88) + 13 * (((j >> 3) % 11) + 11 * (j & 7));
+        // rho(8g + c) = g/11 + 13 (g%11) + 143 c; padb(16 rho + r) = 17 rho + r (r < 16)
+        float2 *d = sm + 17 * (g / 11 + 13 * (g % 11) + 143 * c);
 #pragma unroll
-        for (int r = 0; r < 16; ++r) sm[padb(16 * rho + r)] = v[r];
+        for (int r = 0; r < 16; ++r) d[r] = v[r];
     }
     __syncthreads();
     // radix 13, Ns = 16: twiddles W_208^{k r}
     for (int b = threadIdx.x; b < kMB / 13; b += blockDim.x) {
-        const int k = b & 15, base = (b >> 4) * 208 + k;
+        const int k = b & 15;
+        float2 *p = sm + padb((b >> 4) * 208 + k);  // padb(base + 16 r) = padb(base) + 17 r
         float2 v[13];
 #pragma unroll
-        for (int r = 0; r < 13; ++r) v[r] = sm[padb(base + 16 * r)];
+        for (int r = 0; r < 13; ++r) v[r] = p[17 * r];
 #pragma unroll
         for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], T.t13[16 * (r - 1) + k]);
         dft<13, false>(v);
 #pragma unroll
-        for (int r = 0; r < 13; ++r) sm[padb(base + 16 * r)] = v[r];
+        for (int r = 0; r < 13; ++r) p[17 * r] = v[r];
     }
     __syncthreads();
     // radix 11, Ns = 208: twiddles W_2288^{k r}
     for (int b = threadIdx.x; b < kMB / 11; b += blockDim.x) {
-        const int k = b % 208, base = (b / 208) * 2288 + k;
+        const int k = b % 208;
+        float2 *p = sm + padb((b / 208) * 2288 + k);  // padb(base + 208 r) = padb(base) + 221 r
         float2 v[11];
 #pragma unroll
-        for (int r = 0; r < 11; ++r) v[r] = sm[padb(base + 208 * r)];
+        for (int r = 0; r < 11; ++r) v[r] = p[221 * r];
 #pragma unroll
         for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], T.t11[208 * (r - 1) + k]);
         dft<11, false>(v);
 #pragma unroll
-        for (int r = 0; r < 11; ++r) sm[padb(base + 208 * r)] = v[r];
+        for (int r = 0; r < 11; ++r) p[221 * r] = v[r];
     }
     __syncthreads();
     // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
     for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
         float2 v[8];
+        float2 *p = sm + padb(k);  // padb(k + 2288 r) = padb(k) + 2431 r
 #pragma unroll
-        for (int r = 0; r < 8; ++r) v[r] = sm[padb(k + 2288 * r)];
+        for (int r = 0; r < 8; ++r) v[r] = p[2431 * r];
         float2 S[4];
 #pragma unroll
         for (int q = 1; q < 4; ++q) S[q] = tw2(T.h18304, T.l18304, k * q);
@@ -232,7 +249,7 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         }
         dft<8, false>(v);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) sm[padb(k + 2288 * r)] = v[r];
+        for (int r = 0; r < 8; ++r) p[2431 * r] = v[r];
     }
     __syncthreads();
 }
@@ -329,7 +346,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *sp = reinterpret_cast<uint32_t *>(smem_raw);  // [2][2048] double buffer
     float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
-    TabsA T{sm + kPadA, sm + kPadA + kT32, sm + kPadA + kT32 + kT128};
+    TabsA T = tabs_a_at(sm + kPadA);
     load_tabs_a(T, tw);
     const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
@@ -362,7 +379,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
             else
                 b = nib_value(cur, kMA - k);
             float2 zk, zmk;
-            c2r_pair(a, b, conjf2(__ldg(tw.w32768 + k)), zk, zmk);
+            c2r_pair(a, b, conjf2(tw2(T.h32768, T.l32768, k)), zk, zmk);
             sm[pad(k)] = zk;
             if (k != 0 && k != kMA / 2) sm[pad(kMA - k)] = zmk;
         }
@@ -396,7 +413,7 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
-    TabsA TA{tb, tb + kT32, tb + kT32 + kT128};
+    TabsA TA = tabs_a_at(tb);
     TabsB TB = tabs_b_at(tb);
     __shared__ double red[64];
     load_tabs_a(TA, tw);
@@ -422,7 +439,7 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
                 sm[padb(kMB)] = make_float2(z0.x - z0.y, 0.f);
             } else {
                 float2 xq, xmq;
-                r2c_pair(sm[padb(q)], sm[padb(kMB - q)], __ldg(tw.w36608 + q), xq, xmq);
+                r2c_pair(sm[padb(q)], sm[padb(kMB - q)], tw2(TB.h36608, TB.l36608, q), xq, xmq);
                 sm[padb(q)] = xq;
                 if (q != kMB / 2) sm[padb(kMB - q)] = xmq;
             }
@@ -437,14 +454,15 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
                 ym.y = 0.f;
             }
             float2 zk, zmk;
-            c2r_pair(y, ym, conjf2(__ldg(tw.w32768 + j)), zk, zmk);
+            c2r_pair(y, ym, conjf2(tw2(TA.h32768, TA.l32768, j)), zk, zmk);
             sm[padb(skip + j)] = zk;
             if (j != 0 && j != kMA / 2) sm[padb(skip + kMA - j)] = zmk;
         }
         __syncthreads();
         auto zin = [&](float2 *v) {
+            const float2 *src = sm + padb(skip + tid);  // padb(a + 512 r) = padb(a) + 544 r
 #pragma unroll
-            for (int r = 0; r < 32; ++r) v[r] = sm[padb(skip + tid + 512 * r)];
+            for (int r = 0; r < 32; ++r) v[r] = src[544 * r];
         };
         if constexpr (MODE == 0 || MODE == 3) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
@@ -531,7 +549,7 @@ __global__ void __launch_bounds__(kNTB, 1)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
-    TabsA TA{tb, tb + kT32, tb + kT32 + kT128};
+    TabsA TA = tabs_a_at(tb);
     load_tabs_a(TA, tw);
     const int tid = threadIdx.x;
     const float2 wc = conjf2(__ldg(tw.w32768 + tid));
