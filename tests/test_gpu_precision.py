@@ -3,8 +3,8 @@
 Measures, on sampled 143-snapshot batches of the 3-tone stream, the relative
 RMS error of the resampled series before requantization and the 2-bit code
 agreement (GPU: FP32 series + FP32 compare with its own FP64-accumulated
-thresholds; oracle: FP64 series, FP64 thresholds).  Results are written to
-``gpurun_out/precision_fp32.json`` when that directory exists.
+thresholds; oracle: FP64 series, FP64 thresholds).  Results are written as
+JSON to the path in ``$SDBE_PRECISION_JSON`` when it is set.
 """
 import json
 import os
@@ -60,6 +60,6 @@ def test_fp32_path_rms_and_code_agreement():
     for r in results:
         assert r["rel_rms"] < RMS_TOL, r
         assert r["code_agreement"] >= AGREE_MIN, r
-    if os.path.isdir("gpurun_out"):
-        with open(os.path.join("gpurun_out", "precision_fp32.json"), "w") as f:
+    if os.environ.get("SDBE_PRECISION_JSON"):
+        with open(os.environ["SDBE_PRECISION_JSON"], "w") as f:
             json.dump({"path": "fp32", "samples_per_batch": 128 * 32768, "batches": results}, f, indent=1)
