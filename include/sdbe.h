@@ -357,7 +357,7 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
  * reference.  For callers that cannot call cudaMalloc: a thread that shares
  * the device with asynchronous packet/payload copies (a cudaMalloc or
  * cudaFree can synchronize the whole device and stall them), or a process
- * held to a fixed, pre-reserved memory budget.  Its scratch is a fixed
+ * held to a fixed, pre-reserved amount of device memory.  Its scratch is a fixed
  * 131,088-byte device array (8192 FP64 partial pairs + the result) that every
  * device loading the library holds until exit; n may be at most
  * SDBE_NOALLOC_MAX_SAMPLES (8192 partials x 16384 samples), larger n returns

@@ -1,6 +1,6 @@
 """CPU oracle for the APHIDS GPU stage (SWARM B-engine VDIF -> R2DBE 2-bit VDIF).
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` legs
 of ``bench.py`` may import it.  The product path (``sdbe_gb300``) never calls it.
 

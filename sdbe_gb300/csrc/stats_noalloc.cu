@@ -3,7 +3,7 @@
 // cudaMalloc.  In APHIDS the GPU stage shares the device with the threads that
 // copy packet groups in and payloads out; a cudaMalloc/cudaFree there can
 // synchronize the whole device and stall those copies, and some callers run
-// under a fixed pre-reserved memory budget.  This entry point uses a fixed
+// with a fixed, pre-reserved amount of device memory.  This entry point uses a fixed
 // file-scope device array instead.
 //
 // The per-block partial sums of the existing kernel (k_stats_partial, one

@@ -2,7 +2,7 @@
 
 It serves callers that cannot call cudaMalloc (threads sharing the device with
 asynchronous copies that an allocation would stall, or processes held to a
-fixed memory budget), so its scratch is a fixed device array inside the
+fixed amount of device memory), so its scratch is a fixed device array inside the
 library.  Its results must match the allocating sdbe_summary_stats within the
 tolerance of the other statistics test (1e-9 relative, FP64), on two calls in
 a row with different data (the array keeps the previous call's contents).
