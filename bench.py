@@ -106,6 +106,43 @@ def _load_peaks():
         return 6800.0, "fallback"
 
 
+def _load_tensor_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops_sustained"]), "measured (cuBLAS bf16, sustained)"
+    except (OSError, KeyError, ValueError):
+        return 1700.0, "fallback (sustained)"
+
+
+# Tensor FLOPs of one k_tc_fft transform of length 128*N2: step 1 is 8 K-steps
+# of 12 MMAs (3 split products x 4 real products) of 128 x NP x 16, step 3 is
+# ceil(N2/128) M tiles x NP/16 K-steps of 12 MMAs of 128 x 128 x 16.
+def _tc_flops(n2):
+    np_ = (n2 + 15) // 16 * 16
+    return 8 * 12 * 2 * 128 * np_ * 16 + ((n2 + 127) // 128) * (np_ // 16) * 12 * 2 * 128 * 128 * 16
+
+
+def _tc_roofline(prof, steps):
+    """Tensor roofline of the TC form: MMA FLOPs issued per span / span time.
+    Span A = pairing + TC inverse 16384 per snapshot; span BC = TC forward
+    18304 + pairings + TC inverse 16384 + 2-bit packing per chunk."""
+    peak, kind = _load_tensor_peak()
+    fa = prof.stage_a_snapshots * _tc_flops(128)
+    fbc = prof.stage_bc_chunks * (_tc_flops(143) + _tc_flops(128))
+    ta = fa / (prof.stage_a_ms * 1e-3) / 1e12 if prof.stage_a_ms else 0.0
+    tbc = fbc / (prof.stage_bc_ms * 1e-3) / 1e12 if prof.stage_bc_ms else 0.0
+    dom_bc = prof.stage_bc_ms >= prof.stage_a_ms
+    ach = tbc if dom_bc else ta
+    n = max(prof.stage_bc_launches if dom_bc else prof.stage_a_launches, 1)
+    return {"bound": "tensor", "kernel": "k_tc_fft span " + ("B+C" if dom_bc else "A"), "achieved": ach,
+            "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None, "peak_kind": kind,
+            "ms_per_launch": (prof.stage_bc_ms if dom_bc else prof.stage_a_ms) / n,
+            "flops_per_launch": (fbc if dom_bc else fa) / n,
+            "stage_ms_per_step": {"stage_a": prof.stage_a_ms / steps, "stage_bc": prof.stage_bc_ms / steps},
+            "tensor_tflops": {"span_a": ta, "span_bc": tbc}}
+
+
 def cpu_baseline(sample_frames=96, workers=None):
     """The oracle's FP32 path (numpy unpack + scipy.fft) on a bounded sample."""
     from oracle import sdbe_oracle as O
@@ -174,7 +211,11 @@ def run_ours(args):
     spec = synth.config2(stream=rank, n_frames=frames)
     pkts = synth.generate(spec)
     n_pkts = pkts.shape[0]
-    rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=args.wave)
+    from sdbe_gb300 import _native as N
+
+    tc = args.precision == "tc16"
+    rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=args.wave,
+                   precision=N.PRECISION_TC16 if tc else N.PRECISION_FP32)
     out_bytes = rs.output_bytes(frames)
     n_batches = out_bytes // (2 * 128 * 8192)
     samples_per_step = n_batches * OUT_SAMPLES_PER_BATCH * 2
@@ -274,23 +315,27 @@ def run_ours(args):
                 "stage_bc_tflops": prof.stage_bc_chunks * bc_flop / (prof.stage_bc_ms * 1e-3) / 1e12
                 if prof.stage_bc_ms else None,
                 "peak_tflops": nominal_fp32, "peak_kind": "nominal (152 SM x 128 FP32 lanes x 2 x 2.07 GHz)"}
+        roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                    "ms_per_launch": dom_ms, "algorithmic_bytes_per_launch": dom_bytes,
+                    "stage_ms_per_step": {"stage_a": prof.stage_a_ms / args.steps,
+                                          "stage_bc": prof.stage_bc_ms / args.steps},
+                    "fp32": fp32}
+        if tc:
+            roofline = _tc_roofline(prof, args.steps)
         cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f16x2 tensor (f32 accumulate)" if tc else "f32", "data": "synthetic",
             "config": {"workload": f"{frames} B-frames x 1 packet stream per GPU (2 phased sums), "
-                                   f"FP32 radix-FFT path, trim {TRIM_MHZ} MHz, first-batch thresholds per step",
+                                   f"{'FP16 tensor-core (hi+lo split) four-step' if tc else 'FP32 radix'}-FFT path, "
+                                   f"trim {TRIM_MHZ} MHz, first-batch thresholds per step",
                        "frames": frames, "batches": int(n_batches), "streams_per_gpu": 2,
                        "packets_per_step": int(n_pkts), "wave_batches": args.wave,
                        "l2": "inputs larger than L2 (packets 1.08 GB/step, payload 0.96 GB/step)"},
             "x_realtime": value / (REALTIME_GSPS * 2 * world),
-            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "ms_per_launch": dom_ms, "algorithmic_bytes_per_launch": dom_bytes,
-                         "stage_ms_per_step": {"stage_a": prof.stage_a_ms / args.steps,
-                                               "stage_bc": prof.stage_bc_ms / args.steps},
-                         "fp32": fp32},
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "GS/s", "ms_per_step": float(t.item()),
                     "h2d_bytes_per_step": int(n_pkts * 1056), "d2h_bytes_per_step": int(out_bytes),
@@ -590,6 +635,8 @@ def main():
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16"],
+                    help="group512 only: fp32 radix kernels (default) or the FP16 tensor-core form")
     ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
                     help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
                          "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")

@@ -69,6 +69,13 @@ extern "C" {
 #define SDBE_MAP_APHIDS 0          /* ((c>>1)*16 + (c&1) + 2f)*8, .cu:442                */
 #define SDBE_MAP_MAR2015 1         /* 8*(8c + f), prototyping/read_sdbe_vdif.py:193      */
 
+/* arithmetic of the three FFT stages (A: C2R 32768, B: R2C 36608, C: C2R 32768) */
+#define SDBE_PRECISION_FP32 0      /* FP32 radix kernels on the CUDA cores (default)     */
+/* FP16 tensor cores: each transform a four-step GEMM (tcgen05.mma, FP32
+ * accumulation in tensor memory) with the DFT matrix and the data split into
+ * hi + lo FP16 halves.  sdbe_process only; not with SDBE_THRESH_WINDOW. */
+#define SDBE_PRECISION_TC16 1
+
 /* sdbe_process flags */
 #define SDBE_IN_HOST 1u            /* packets are in host memory (copied in)             */
 #define SDBE_OUT_HOST 2u           /* output goes to host memory (copied out)            */
@@ -92,7 +99,8 @@ typedef struct sdbe_config {
     int32_t channel_map;       /* SDBE_MAP_*                                                */
     int32_t wave_batches;      /* batches per FFT wave (0 = default); bounds scratch        */
     int32_t threshold_window;  /* SDBE_THRESH_WINDOW: batches in the window (0 = 64)        */
-    int32_t reserved[8];
+    int32_t precision;         /* SDBE_PRECISION_*                                          */
+    int32_t reserved[7];
 } sdbe_config;
 
 typedef struct sdbe_state {

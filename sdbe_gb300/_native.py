@@ -27,6 +27,7 @@ SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED, THRESH_WINDOW = 0, 1, 2
 THRESH_BLOCK = 16
 MAP_APHIDS, MAP_MAR2015 = 0, 1
+PRECISION_FP32, PRECISION_TC16 = 0, 1
 IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED, IN_8PAC = 1, 2, 4, 8, 16, 32, 64
 PAC8_BYTES = 8504
 NOALLOC_MAX_SAMPLES = 134217728
@@ -36,7 +37,7 @@ class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("trim_mhz", C.c_int32), ("max_frames", C.c_int32),
                 ("threshold_mode", C.c_int32), ("pol1_uses_pol0_threshold", C.c_int32),
                 ("channel_map", C.c_int32), ("wave_batches", C.c_int32), ("threshold_window", C.c_int32),
-                ("reserved", C.c_int32 * 8)]
+                ("precision", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class State(C.Structure):

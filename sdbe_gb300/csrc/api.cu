@@ -75,6 +75,11 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->ipfb_tab);
     cudaFree(h->wring);
     cudaFree(h->wpart);
+    cudaFree(h->tc_f128);
+    cudaFree(h->tc_f143);
+    cudaFree(h->tc_bufx);
+    cudaFree(h->tc_bufy);
+    if (h->tc_status_host) cudaFreeHost(h->tc_status_host);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
     cudaFree(h->pay);
@@ -498,6 +503,10 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     if (cfg->channel_map != SDBE_MAP_APHIDS && cfg->channel_map != SDBE_MAP_MAR2015)
         return fail(nullptr, SDBE_ERR_ARG, "unknown channel_map");
     if (cfg->wave_batches < 0 || cfg->wave_batches > 64) return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
+    if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16)
+        return fail(nullptr, SDBE_ERR_ARG, "unknown precision");
+    if (cfg->precision == SDBE_PRECISION_TC16 && cfg->threshold_mode == SDBE_THRESH_WINDOW)
+        return fail(nullptr, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 does not take SDBE_THRESH_WINDOW");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
         cudaGetLastError();
@@ -579,8 +588,13 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     CallPlan c;
     int rc = plan_call(h, packets, n_packets, n_frames, b_zero, out, out_bytes, flags, pick(h, stream), c);
     if (!rc) rc = prepare_call(c);
-    if (!rc) rc = fft_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st,
-                            [&](int64_t lo, int64_t hi) { return c.aligned ? SDBE_OK : ship_call(c, lo, hi); });
+    if (!rc && h->cfg.precision == SDBE_PRECISION_TC16) {
+        rc = tc_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st);
+        if (!rc && !c.aligned) rc = ship_call(c, 0, c.n_out);
+    } else if (!rc) {
+        rc = fft_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st,
+                       [&](int64_t lo, int64_t hi) { return c.aligned ? SDBE_OK : ship_call(c, lo, hi); });
+    }
     if (!rc) rc = complete_call(c, result);
     return rc;
 }
@@ -591,6 +605,8 @@ int sdbe_process_multi(sdbe_resampler *const *hs, const sdbe_stream_desc *d, int
     for (int i = 0; i < n; ++i) {
         if (!hs[i]) return fail(nullptr, SDBE_ERR_ARG, "null handle");
         if (hs[i]->cfg.device != hs[0]->cfg.device) return fail(hs[i], SDBE_ERR_ARG, "handles on different devices");
+        if (hs[i]->cfg.precision != SDBE_PRECISION_FP32)
+            return fail(hs[i], SDBE_ERR_ARG, "sdbe_process_multi takes SDBE_PRECISION_FP32 handles only");
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) return fail(hs[i], SDBE_ERR_ARG, "a handle appears twice");
     }

@@ -75,6 +75,12 @@ struct sdbe_resampler {
     int window = 0;               // SDBE_THRESH_WINDOW: batches per window
     double *wring = nullptr;      // [2][window][3] batch statistics (n, mean, M2)
     double *wpart = nullptr;      // [2][wave*128][3] chunk statistics of one wave
+    // SDBE_PRECISION_TC16: pre-tiled FP16 DFT matrices and complex scratch (on first use)
+    void *tc_f128 = nullptr, *tc_f143 = nullptr;
+    float2 *tc_bufx = nullptr;    // [2][wave*143][16384]
+    float2 *tc_bufy = nullptr;    // [2][wave*128][18304]
+    int *tc_status_host = nullptr;  // 1 after a tensor-core barrier time-out (pinned, mapped)
+    int *tc_status = nullptr;       // its device address
     // Mar-2015 format: unpacked frames land here first; the last one is held
     // for the next call because output frame f needs input frame f+1.
     uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]
@@ -159,6 +165,11 @@ inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t 
     h->launches += 1;
     return SDBE_OK;
 }
+
+// The FFT chain of sdbe_process with SDBE_PRECISION_TC16 (k_tc.cu): same
+// arguments as fft_chain, payload complete when it returns (queued on st).
+int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
+             const PayloadTarget &tgt, cudaStream_t st);
 
 // First-batch threshold path (if thresholds are unset) and the FFT waves over
 // n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,

@@ -292,38 +292,6 @@ __device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
     (f(std::integral_constant<int, R>{}), ...);
 }
 
-// Packed nibble k -> (real, imag) = codes - 2.  A 2-bit code c placed in the
-// mantissa of 1.5 * 2^23 gives the float 12582912 + c exactly; subtracting
-// 12582914 leaves c - 2 (one logic op and one add, no int-to-float convert).
-__device__ __forceinline__ float2 nib_value(const uint32_t *sp, int k) {
-    const uint32_t w = sp[k >> 3] >> ((k & 7) * 4);
-    const float re = __uint_as_float(0x4B400000u | ((w >> 2) & 3u)) - 12582914.0f;
-    const float im = __uint_as_float(0x4B400000u | (w & 3u)) - 12582914.0f;
-    return make_float2(re, im);
-}
-
-// Hermitian pair of a length-32768 C2R input: from Y[k], Y[M-k] (M = 16384)
-// and we = e^{+2 pi i k/32768},
-//   Z[k]   = (Y[k] + conj Y[M-k]) + i we (Y[k] - conj Y[M-k]) =: e + i t
-//   Z[M-k] = conj(e) + i conj(t),
-// so one complex multiply serves both.
-__device__ __forceinline__ void c2r_pair(float2 y, float2 ym, float2 we, float2 &zk, float2 &zmk) {
-    const float2 e = make_float2(y.x + ym.x, y.y - ym.y);
-    const float2 t = cmul(make_float2(y.x - ym.x, y.y + ym.y), we);
-    zk = make_float2(e.x - t.y, e.y + t.x);
-    zmk = make_float2(e.x + t.y, t.x - e.y);
-}
-
-// Hermitian pair of a length-36608 R2C output: from Z[q], Z[M'-q] (M' = 18304)
-// and w = e^{-2 pi i q/36608}, with s = Z[q] + conj Z[M'-q], t = w (Z[q] - conj Z[M'-q]):
-//   X[q] = (s - i t)/2,   X[M'-q] = (conj(s) - i conj(t))/2.
-__device__ __forceinline__ void r2c_pair(float2 za, float2 zb, float2 w, float2 &xq, float2 &xmq) {
-    const float2 s = make_float2(za.x + zb.x, za.y - zb.y);
-    const float2 t = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
-    xq = make_float2(0.5f * (s.x + t.y), 0.5f * (s.y - t.x));
-    xmq = make_float2(0.5f * (s.x - t.y), -0.5f * (s.y + t.x));
-}
-
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");

@@ -1,0 +1,108 @@
+"""The tensor-core precision form (SDBE_PRECISION_TC16) against the FP64 oracle
+and against the FP32 path.
+
+Bar: 2-bit code agreement >= 99.9% against the FP64 oracle, the same bar as
+the FP32 path; thresholds within 1e-5 (relative) of the oracle's.  Per-batch
+agreement and threshold differences are written as JSON to the path in
+``$SDBE_PRECISION_TC_JSON`` when it is set.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_util import codes_of
+from oracle import sdbe_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+AGREE_MIN = 0.999
+THR_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def S():
+    import __graft_entry__ as g
+
+    g.build()
+    from sdbe_gb300 import synth
+
+    return synth
+
+
+def _agree(a, b):
+    return float(np.mean(codes_of(a) == codes_of(b)))
+
+
+def test_tc_process_vs_oracle_and_fp32(S):
+    """8 frames (7 batches) in waves of 2: first batch, two full waves and a
+    short one; codes against the oracle and against the FP32 path."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    spec = S.config1()
+    p = S.generate(spec)
+    with Resampler(trim_mhz=150, max_frames=8, wave_batches=2, precision=N.PRECISION_TC16) as tc, \
+            Resampler(trim_mhz=150, max_frames=8, wave_batches=2) as f32:
+        out, res = tc.process(p, 8, spec.b_start)
+        (th0, th1), (off0, off1), ok = tc.thresholds
+        out32, _ = f32.process(p, 8, spec.b_start)
+    assert ok and res.n_batches == 7 and out.shape == out32.shape
+    st = O.StreamState()
+    ref = O.process_group(p, spec.b_start, 8, 150, state=st)
+    rows = []
+    for pol in range(2):
+        for b in range(7):
+            sl = slice(b * 128, (b + 1) * 128)
+            rows.append({"pol": pol, "batch": b, "agree_oracle": _agree(out[pol, sl], ref[pol, sl]),
+                         "agree_fp32": _agree(out[pol, sl], out32[pol, sl])})
+    for r in rows:
+        assert r["agree_oracle"] >= AGREE_MIN, r
+    for pol, th, off in ((0, th0, off0), (1, th1, off1)):
+        assert abs(th - st.threshold[pol]) <= THR_TOL * st.threshold[pol]
+        assert abs(off - st.offset[pol]) <= THR_TOL * st.threshold[pol]
+    if os.environ.get("SDBE_PRECISION_TC_JSON"):
+        with open(os.environ["SDBE_PRECISION_TC_JSON"], "w") as f:
+            json.dump({"path": "tc16", "samples_per_batch": 128 * 32768,
+                       "threshold_rel_diff": [abs(th0 - st.threshold[0]) / st.threshold[0],
+                                              abs(th1 - st.threshold[1]) / st.threshold[1]],
+                       "batches": rows}, f, indent=1)
+
+
+def test_tc_carry_and_framed_match_single_call(S):
+    """Two calls (3 + 5 frames, snapshot carry between them) equal one call of 8
+    frames bit for bit, framed headers included."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    spec = S.config1()
+    p = S.generate(spec)
+    cut = 3 * 2048
+    with Resampler(trim_mhz=150, max_frames=8, precision=N.PRECISION_TC16) as a, \
+            Resampler(trim_mhz=150, max_frames=8, precision=N.PRECISION_TC16) as b:
+        whole, _ = a.process(p, 8, spec.b_start, framed=True)
+        o1, r1 = b.process(p[:cut], 3, spec.b_start, framed=True)
+        o2, r2 = b.process(p[cut:], 5, spec.b_start + 3, framed=True)
+    assert r1.n_batches + r2.n_batches == 7
+    assert np.array_equal(np.concatenate([o1, o2], axis=1), whole)
+
+
+def test_tc_config_errors(S):
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    with pytest.raises(N.SdbeError) as e:
+        Resampler(threshold_mode=N.THRESH_WINDOW, precision=N.PRECISION_TC16)
+    assert e.value.code == N.ERR_ARG
+    with pytest.raises(N.SdbeError) as e:
+        Resampler(precision=7)
+    assert e.value.code == N.ERR_ARG
+    spec = S.config1()
+    p = S.generate(spec, n_frames=1)
+    from sdbe_gb300 import process_multi
+
+    with Resampler(max_frames=2, precision=N.PRECISION_TC16) as rs:
+        with pytest.raises(N.SdbeError) as e:
+            process_multi([rs], [(p, 1, spec.b_start, None)])
+        assert e.value.code == N.ERR_ARG
