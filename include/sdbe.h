@@ -341,7 +341,8 @@ int sdbe_fill_missing(const uint32_t *bitmap, int32_t n_frames, int32_t channel_
 int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, void *stream);
 
 /* SwarmC2R (.cu:589-625): packed spectra [n_snapshots][2048 u32] ->
- * float [n_snapshots][32768], unnormalised C2R. */
+ * float [n_snapshots][32768], unnormalised C2R.  This and
+ * sdbe_resample_chunks compute in the handle's precision (SDBE_PRECISION_*). */
 int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out,
                    void *stream);
 

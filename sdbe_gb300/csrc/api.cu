@@ -824,6 +824,7 @@ int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, v
 int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out, void *stream) {
     if (!h || n_snapshots < 0 || (n_snapshots > 0 && (!spec || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
     DeviceGuard g(h->cfg.device);
+    if (h->cfg.precision == SDBE_PRECISION_TC16) return tc_swarm_c2r(h, spec, n_snapshots, out, pick(h, stream));
     SDBE_CK(h, launch_swarm_c2r(spec, 0, 0, n_snapshots, 1, out, 0, h->tw, pick(h, stream)));
     return SDBE_OK;
 }
@@ -847,6 +848,7 @@ int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int3
 int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, void *stream) {
     if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
     DeviceGuard g(h->cfg.device);
+    if (h->cfg.precision == SDBE_PRECISION_TC16) return tc_resample_chunks(h, in, n_chunks, out, pick(h, stream));
     ResampleOut o{};
     o.fout = out;
     SDBE_CK(h, launch_resample(2, in, 0, h->skip, n_chunks, 1, o, h->tw, pick(h, stream)));

@@ -171,6 +171,10 @@ inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t 
 int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
              const PayloadTarget &tgt, cudaStream_t st);
 
+// sdbe_swarm_c2r / sdbe_resample_chunks of a SDBE_PRECISION_TC16 handle (one pol).
+int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st);
+int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, cudaStream_t st);
+
 // First-batch threshold path (if thresholds are unset) and the FFT waves over
 // n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,
 // snapshots from 0), payload packets at tgt from packet 0.  on_wave(lo, hi)

@@ -490,4 +490,44 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
     return SDBE_OK;
 }
 
+// Stage entry points in the tensor-core form (sdbe_swarm_c2r and
+// sdbe_resample_chunks on a SDBE_PRECISION_TC16 handle), one pol, in pieces
+// that fit the handle's scratch.
+int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st) {
+    if (n_snaps <= 0) return SDBE_OK;
+    if (int rc = tc_prepare(h, st)) return rc;
+    const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
+    const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kBatchSnaps;
+    for (int64_t s0 = 0; s0 < n_snaps; s0 += cap) {
+        const int64_t n = n_snaps - s0 < cap ? n_snaps - s0 : cap;
+        k_tc_prep_a<<<static_cast<unsigned>(n), 256, 0, st>>>(spec, 0, s0, n, h->tc_bufx, h->tw.w32768);
+        SDBE_CK(h, cudaGetLastError());
+        const TcFftArgs A{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + s0 * kNA), kMA, 0,
+                          n, n, f128, f128, h->tw.w16384, h->tc_status};
+        SDBE_CK(h, (launch_tc_fft<128, true>(A, st)));
+    }
+    return SDBE_OK;
+}
+
+int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, cudaStream_t st) {
+    if (n_chunks <= 0) return SDBE_OK;
+    if (int rc = tc_prepare(h, st)) return rc;
+    const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
+    const uint8_t *f143 = static_cast<const uint8_t *>(h->tc_f143);
+    const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kChunks;
+    for (int64_t c0 = 0; c0 < n_chunks; c0 += cap) {
+        const int64_t n = n_chunks - c0 < cap ? n_chunks - c0 : cap;
+        const TcFftArgs B{reinterpret_cast<const float2 *>(in + c0 * kNB), kMB, 0, h->tc_bufy, kMB, 0,
+                          n, n, f128, f143, h->tw.w18304, h->tc_status};
+        SDBE_CK(h, (launch_tc_fft<143, false>(B, st)));
+        k_tc_pair_bc<<<static_cast<unsigned>(n), 256, 0, st>>>(h->tc_bufy, h->tc_bufx, h->skip, h->tw.w32768,
+                                                               h->tw.w36608);
+        SDBE_CK(h, cudaGetLastError());
+        const TcFftArgs C{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + c0 * kNC), kMA, 0,
+                          n, n, f128, f128, h->tw.w16384, h->tc_status};
+        SDBE_CK(h, (launch_tc_fft<128, true>(C, st)));
+    }
+    return SDBE_OK;
+}
+
 }  // namespace sdbe
