@@ -56,15 +56,26 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b,
         "l"(a), "l"(b), "r"(idesc), "r"(acc ? 1u : 0u));
 }
 
-// Eight consecutive TMEM columns of this thread's lane (warp-collective).
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
-    uint32_t r[8];
+// Eight columns at ta and eight at tb (this thread's lane), one wait for both;
+// the wait names the registers so that no use moves above it.
+__device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float *va, float *vb) {
+    uint32_t r[16];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                 : "r"(ta));
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(tb));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])::"memory");
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; ++i) {
+        va[i] = __uint_as_float(r[i]);
+        vb[i] = __uint_as_float(r[8 + i]);
+    }
 }
 
 // Bounded wait for the commit of phase `phase`; false on time-out.
@@ -81,16 +92,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
 // Byte offset of element (row, k) in a K-major operand with `kdim` columns.
 __device__ __forceinline__ uint32_t op_off(int row, int k, int kdim) {
     return static_cast<uint32_t>((row >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
-
-// v -> four FP16 components (re hi, re lo, im hi, im lo) at `off`.
-__device__ __forceinline__ void split_store(uint8_t *comp0, uint32_t comp_bytes, uint32_t off, float2 v) {
-    const __half rh = __float2half_rn(v.x), ih = __float2half_rn(v.y);
-    const __half rl = __float2half_rn(v.x - __half2float(rh)), il = __float2half_rn(v.y - __half2float(ih));
-    *reinterpret_cast<__half *>(comp0 + off) = rh;
-    *reinterpret_cast<__half *>(comp0 + comp_bytes + off) = rl;
-    *reinterpret_cast<__half *>(comp0 + 2 * comp_bytes + off) = ih;
-    *reinterpret_cast<__half *>(comp0 + 3 * comp_bytes + off) = il;
 }
 
 // 2^(14 - e) where maxabs < 2^e: the exact scale that brings |values| below 2^14.
@@ -125,27 +126,102 @@ struct TcFftArgs {
     int *status;                       // set to 1 on a barrier time-out (host-mapped)
 };
 
+__device__ __forceinline__ void mbar_init(uint64_t *mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+}
+
+// Arrival of this thread + `bytes` expected from bulk copies, then the bulk
+// copy global -> shared that delivers them.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+// The barrier completes when every tcgen05 operation this thread issued so far has.
+__device__ __forceinline__ void mma_commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t pick4(uint32_t a, uint32_t b, uint32_t c, uint32_t d, int j) {
+    const uint32_t lo = (j & 1) ? b : a, hi = (j & 1) ? d : c;
+    return (j & 2) ? hi : lo;
+}
+
+// (a, b) -> FP16 pairs hi = rn(a, b), lo = rn(a - hi, b - hi) as 32-bit words.
+__device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t &lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t *>(&h);
+    lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+template <int N2>
+struct TcGeo {
+    static constexpr int NP = (N2 + 15) / 16 * 16;  // step-1 N, step-3 K
+    static constexpr int MT = (N2 + 127) / 128;     // step-3 M tiles
+    static constexpr int KS3 = NP / 16;             // step-3 K-steps (step 1 has 8)
+    static constexpr int SPI = 8 + KS3 * MT;        // pipeline stages per item (one M tile, one K-step each)
+    static constexpr int RG = NP / 8;               // 8-row groups of the step-1 B operand
+    static constexpr int NPAIR = NP * 64 / kTcThreads;  // input element pairs per thread
+    static constexpr uint32_t COMP = NP * 128 * 2;  // bytes of one B-operand component
+    static constexpr int NRING = 4;                 // A-tile buffers
+    static constexpr uint32_t STAGE = 4 * kTile;    // bytes of one stage's A tiles
+    static constexpr size_t SMEM = 4 * static_cast<size_t>(COMP) + NRING * static_cast<size_t>(STAGE) +
+                                   (N2 + 128) * sizeof(float2);
+    static_assert(static_cast<size_t>(N2) * 1024 <= 4 * static_cast<size_t>(COMP), "output staging fits");
+};
+
 // One CTA per SM (its shared memory and all 512 TMEM columns), persistent
-// over items.
+// over items.  Thread 0 issues the MMAs and the bulk copies of the DFT tiles
+// through a ring of four 16 KB buffers (the tiles of stage g+3 load while the
+// MMAs of stage g run; a stage is one K-step of one M tile); warps 1-7 load
+// the next item's input into registers while the current item's step-3 GEMM
+// runs, warp 0 (whose lane 0 issues) after it.
+//
+// Input element pairs: thread tid holds pairs i*256 + tid, i < NPAIR; pair p
+// is row (q % RG)*8 + (p & 7) and K columns 2kp, 2kp+1 with q = p >> 5 and
+// kp = (q / RG)*4 + ((p >> 3) & 3), so one warp's 32-bit stores cover whole
+// 128-byte core-matrix rows: no bank conflicts.  Step 2 rotates the order of
+// a row's four words by its row group for the same reason.  The output is
+// staged in shared memory as [k2][k1] with the 16-byte pieces of each 128-byte
+// segment permuted by k2 & 7, and copied out with coalesced 16-byte stores.
 template <int N2, bool INV>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant__ TcFftArgs a) {
-    constexpr int NP = (N2 + 15) / 16 * 16;  // step-1 N, step-3 K
-    constexpr int MT = (N2 + 127) / 128;     // step-3 M tiles
-    constexpr int KS3 = NP / 16;
-    constexpr int NFFT = 128 * N2;
-    constexpr uint32_t COMP = NP * 128 * 2;  // bytes of one B-operand component
+    using G = TcGeo<N2>;
+    constexpr int NP = G::NP, MT = G::MT, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
+    constexpr int NRING = G::NRING;
+    constexpr uint32_t COMP = G::COMP, STAGE = G::STAGE;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *bop = smem;                     // [4 comps][COMP]
-    uint8_t *aop = smem + 4 * COMP;          // [MT][4 comps][4 KB]
-    __shared__ __align__(8) uint64_t mbar;
+    uint8_t *bop = smem;                                               // [4 comps][COMP]; output staging
+    uint8_t *aop = smem + 4 * COMP;                                    // [NRING][STAGE]
+    float2 *twh = reinterpret_cast<float2 *>(aop + NRING * STAGE);    // w^(128 i), i < N2
+    float2 *twl = twh + N2;                                            // w^j, j < 128
+    __shared__ __align__(8) uint64_t full[NRING], empty[NRING], done;
     __shared__ uint32_t tmem_base;
+    __shared__ int s_err;
     __shared__ float red[kTcThreads / 32];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int quarter = warp & 3, half = warp >> 2;
 
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        for (int b = 0; b < NRING; ++b) {
+            mbar_init(&full[b]);
+            mbar_init(&empty[b]);
+        }
+        mbar_init(&done);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_err = 0;
+    }
+    for (int i = tid; i < N2 + 128; i += kTcThreads) {  // step-2 twiddles w^e = twh[e >> 7] twl[e & 127]
+        float2 w = __ldg(a.tw + (i < N2 ? 128 * i : i - N2));
+        if (INV) w.y = -w.y;
+        twh[i] = w;  // twl = twh + N2
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -157,124 +233,202 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tb = tmem_base;
     const uint32_t lane_base = tb + (static_cast<uint32_t>(quarter * 32) << 16);
-    uint32_t phase = 0;
-    bool ok = true;
 
-    // One K-step: this step's A tiles copied in, 12 MMAs per M tile (3 split
-    // products x 4 real products), committed to the barrier, waited on.
-    auto k_step = [&](const uint8_t *atiles, int mtiles, int n, uint32_t b_kdim, int s, uint32_t dstride) -> bool {
-        const uint4 *src = reinterpret_cast<const uint4 *>(atiles);
-        uint4 *dst = reinterpret_cast<uint4 *>(aop);
-        for (int i = tid; i < mtiles * 4 * kTile / 16; i += kTcThreads) dst[i] = __ldg(src + i);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sbo_b = (b_kdim / 8) * 128;
-            for (int t = 0; t < mtiles; ++t) {
-                const uint32_t dr = tb + t * dstride, di = dr + dstride / 2;
+    // ---- issuer state (thread 0) ----------------------------------------------
+    uint32_t g = 0;                      // global stage index (items x SPI)
+    bool err = false;                    // a wait of thread 0 timed out: issue nothing more
+    uint32_t pend = 0;                   // buffers with a bulk copy in flight
+    uint32_t pend_g[NRING] = {0, 0, 0, 0};  // the stage each of those copies is for
+    uint32_t done_n = 0;                 // completions of `done` waited for (all threads)
+
+    auto issue_copy = [&](uint32_t gg) {
+        const int64_t item = blockIdx.x + static_cast<int64_t>(gg / SPI) * gridDim.x;
+        if (item >= a.n_items) return;
+        const int kk = static_cast<int>(gg % SPI), b = gg % NRING;
+        const uint8_t *src = kk < 8 ? a.f1 + kk * STAGE : a.f2 + (kk - 8) * STAGE;
+        bulk_load(aop + b * STAGE, src, STAGE, &full[b]);
+        pend |= 1u << b;
+        pend_g[b] = gg;
+    };
+    // One GEMM phase (thread 0): nst stages; step 1 (one M tile, N = NP, Dr at
+    // column 0, Di at 256) or step 3 (stage j = K-step j / MT of M tile j % MT,
+    // N = 128, Dr at 256 t, Di at 256 t + 128).
+    auto gemm = [&](int nst, bool step3) {
+        const int n = step3 ? 128 : NP;
+        const uint32_t sbo_b = step3 ? (NP / 8) * 128 : 16 * 128;
+        for (int j = 0; j < nst; ++j, ++g) {
+            const int b = g % NRING;
+            if (!err) {
+                if (mbar_wait(&full[b], (g / NRING) & 1u))
+                    pend &= ~(1u << b);
+                else
+                    err = true;
+            }
+            if (!err) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int s = step3 ? j / MT : j, t = step3 ? j % MT : 0;
+                const uint32_t dr = tb + (step3 ? t * 256 : 0), di = dr + (step3 ? 128 : 256);
+                const uint8_t *ab = aop + b * STAGE;
+#pragma unroll
                 for (int sp = 0; sp < 3; ++sp) {
                     const int ah = sp == 2 ? 1 : 0, bh = sp == 1 ? 1 : 0;  // (hi,hi) (hi,lo) (lo,hi)
-                    auto ad = [&](int comp) { return smem_desc(smem_u32(aop + (t * 4 + comp) * kTile), 128, 256); };
-                    auto bd = [&](int comp) { return smem_desc(smem_u32(bop + comp * COMP) + s * 256, 128, sbo_b); };
+                    const uint64_t ar = smem_desc(smem_u32(ab + (0 + ah) * kTile), 128, 256);
+                    const uint64_t ai = smem_desc(smem_u32(ab + (2 + ah) * kTile), 128, 256);
+                    const uint64_t br = smem_desc(smem_u32(bop + (0 + bh) * COMP) + s * 256, 128, sbo_b);
+                    const uint64_t bi = smem_desc(smem_u32(bop + (2 + bh) * COMP) + s * 256, 128, sbo_b);
                     const bool first = s == 0 && sp == 0;
                     // Dr += Fr Br -/+ Fi Bi ; Di += +/-Fi Br + Fr Bi
-                    mma_f16(dr, ad(0 + ah), bd(0 + bh), instr_desc(128, n, false), !first);
-                    mma_f16(dr, ad(2 + ah), bd(2 + bh), instr_desc(128, n, !INV), true);
-                    mma_f16(di, ad(2 + ah), bd(0 + bh), instr_desc(128, n, INV), !first);
-                    mma_f16(di, ad(0 + ah), bd(2 + bh), instr_desc(128, n, false), true);
+                    mma_f16(dr, ar, br, instr_desc(128, n, false), !first);
+                    mma_f16(dr, ai, bi, instr_desc(128, n, !INV), true);
+                    mma_f16(di, ai, br, instr_desc(128, n, INV), !first);
+                    mma_f16(di, ar, bi, instr_desc(128, n, false), true);
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(&mbar)));
+            mma_commit(&empty[b]);
+            if (j == nst - 1) mma_commit(&done);
+            if (!err) {
+                // the buffer of stage g-1 takes stage g+3 once those MMAs are done
+                if (g >= 1 && !mbar_wait(&empty[(g - 1) % NRING], ((g - 1) / NRING) & 1u)) err = true;
+                if (!err) issue_copy(g + NRING - 1);
+            }
         }
-        const bool done = mbar_wait(&mbar, phase);
-        ++phase;
+    };
+    // All threads: the GEMM phase's accumulators are final.
+    auto wait_done = [&]() {
+        if (!mbar_wait(&done, done_n & 1u)) s_err = 1;
+        ++done_n;
+        __syncwarp();  // warp 0 reconverges before the warp-collective TMEM loads
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        return __syncthreads_and(done) != 0;  // one verdict for the whole CTA
     };
 
-    for (int64_t item = blockIdx.x; item < a.n_items && ok; item += gridDim.x) {
+    float2 xv[2 * NPAIR];
+    auto load_input = [&](int64_t item) {
         const int64_t pol = item / a.per_pol, loc = item % a.per_pol;
         const float2 *x = a.in + pol * a.in_pol_stride + loc * a.in_stride;
-        float2 *y = a.out + pol * a.out_pol_stride + loc * a.out_stride;
+#pragma unroll
+        for (int i = 0; i < NPAIR; ++i) {
+            const int q = i * 8 + warp;
+            const int row = (q % RG) * 8 + (lane & 7);
+            const int k = ((q / RG) * 4 + (lane >> 3)) * 2;
+            xv[2 * i] = row < N2 ? __ldg(x + N2 * k + row) : make_float2(0.f, 0.f);
+            xv[2 * i + 1] = row < N2 ? __ldg(x + N2 * (k + 1) + row) : make_float2(0.f, 0.f);
+        }
+    };
+
+    if (tid == 0)
+        for (int i = 0; i < NRING - 1; ++i) issue_copy(i);
+    if (blockIdx.x < a.n_items) load_input(blockIdx.x);
+    for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+        float2 *y = a.out + (item / a.per_pol) * a.out_pol_stride + (item % a.per_pol) * a.out_stride;
         // ---- input: scaled below 2^14, split, B[n2][n1] -------------------------
         float m = 0.f;
-        for (int n = tid; n < NFFT; n += kTcThreads) {
-            const float2 v = __ldg(x + n);
-            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
-        }
+#pragma unroll
+        for (int i = 0; i < 2 * NPAIR; ++i) m = fmaxf(m, fmaxf(fabsf(xv[i].x), fabsf(xv[i].y)));
         const float s1 = pow2_scale(block_max(m, red));
-        for (int n = tid; n < NFFT; n += kTcThreads) {
-            const float2 v = __ldg(x + n);
-            const int n1 = n / N2, n2 = n - n1 * N2;
-            split_store(bop, COMP, op_off(n2, n1, 128), make_float2(v.x * s1, v.y * s1));
+#pragma unroll
+        for (int i = 0; i < NPAIR; ++i) {
+            const int q = i * 8 + warp;
+            const int row = (q % RG) * 8 + (lane & 7);
+            const int k = ((q / RG) * 4 + (lane >> 3)) * 2;
+            uint32_t rh, rl, ih, il;
+            split2(xv[2 * i].x * s1, xv[2 * i + 1].x * s1, rh, rl);
+            split2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1, ih, il);
+            const uint32_t off = op_off(row, k, 128);
+            *reinterpret_cast<uint32_t *>(bop + off) = rh;
+            *reinterpret_cast<uint32_t *>(bop + COMP + off) = rl;
+            *reinterpret_cast<uint32_t *>(bop + 2 * COMP + off) = ih;
+            *reinterpret_cast<uint32_t *>(bop + 3 * COMP + off) = il;
         }
-        for (int i = tid; i < (NP - N2) * 128; i += kTcThreads)  // padded rows n2 >= N2
-            split_store(bop, COMP, op_off(N2 + i / 128, i % 128, 128), make_float2(0.f, 0.f));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        // ---- step 1: D[k1][n2]; Dr at column 0, Di at 256 ------------------------
-        for (int s = 0; s < 8 && ok; ++s) ok = k_step(a.f1 + s * 4 * kTile, 1, NP, 128, s, 512);
-        if (!ok) break;
+        // ---- step 1: D[k1][n2] -----------------------------------------------------
+        if (tid == 0) gemm(8, false);
+        wait_done();
         // ---- step 2: twiddles, scale, split into B[k1][n2] -----------------------
         const int k1 = quarter * 32 + lane;
         constexpr int HALF = NP / 2;
         float m2 = 0.f;
         for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
             float dr[8], di[8];
-            tmem_ld8(lane_base + c0, dr);
-            tmem_ld8(lane_base + 256 + c0, di);
+            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
 #pragma unroll
             for (int j = 0; j < 8; ++j) m2 = fmaxf(m2, fmaxf(fabsf(dr[j]), fabsf(di[j])));
         }
         const float s2 = pow2_scale(block_max(m2, red));
+        const int rot = lane >> 3;  // = (k1 >> 3) & 3
         for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
             float dr[8], di[8];
-            tmem_ld8(lane_base + c0, dr);
-            tmem_ld8(lane_base + 256 + c0, di);
+            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
+            float2 v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int n2 = c0 + j;
-                float2 v = make_float2(0.f, 0.f);
+                v[j] = make_float2(0.f, 0.f);
                 if (n2 < N2) {
-                    int e = n2 * k1;
-                    if (e >= NFFT) e -= NFFT;
-                    float2 w = __ldg(a.tw + e);
-                    if (INV) w.y = -w.y;
-                    v = cmul(make_float2(dr[j], di[j]), w);
-                    v.x *= s2;
-                    v.y *= s2;
+                    const int e = n2 * k1;  // < 128 N2
+                    v[j] = cmul(make_float2(dr[j], di[j]), cmul(twh[e >> 7], twl[e & 127]));
                 }
-                split_store(bop, COMP, op_off(k1, n2, NP), v);
+            }
+            uint32_t w[4][4];  // [component][word: columns 2j, 2j+1]
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                split2(v[2 * j].x * s2, v[2 * j + 1].x * s2, w[0][j], w[1][j]);
+                split2(v[2 * j].y * s2, v[2 * j + 1].y * s2, w[2][j], w[3][j]);
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int j = (t + rot) & 3;
+                const uint32_t off = op_off(k1, c0 + 2 * j, NP);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    *reinterpret_cast<uint32_t *>(bop + c * COMP + off) = pick4(w[c][0], w[c][1], w[c][2], w[c][3], j);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        // ---- step 3: D[k2][k1] per M tile; Dr at 256 t, Di at 256 t + 128 ---------
-        for (int s = 0; s < KS3 && ok; ++s) ok = k_step(a.f2 + s * MT * 4 * kTile, MT, 128, NP, s, 256);
-        if (!ok) break;
+        // ---- step 3: D[k2][k1] per M tile --------------------------------------------
+        const bool more = item + gridDim.x < a.n_items;
+        if (tid == 0) gemm(KS3 * MT, true);
+        if (more && warp != 0) load_input(item + gridDim.x);  // lands during the GEMM
+        wait_done();
+        if (more && warp == 0) load_input(item + gridDim.x);  // not beside the issuing lane
+        // ---- output: TMEM -> staging [k2][k1] in shared memory -> y ------------------
         const float inv = (1.f / s1) * (1.f / s2);  // powers of two: exact
         for (int t = 0; t < MT; ++t) {
             const int k2 = t * 128 + quarter * 32 + lane;
-            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 8) {
-                float dr[8], di[8];
-                tmem_ld8(lane_base + t * 256 + c0, dr);
-                tmem_ld8(lane_base + t * 256 + 128 + c0, di);
+            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 16) {
+                float dr[16], di[16];
+                tmem_ld8x2(lane_base + t * 256 + c0, lane_base + t * 256 + 128 + c0, dr, di);
+                tmem_ld8x2(lane_base + t * 256 + c0 + 8, lane_base + t * 256 + 128 + c0 + 8, dr + 8, di + 8);
                 if (k2 < N2) {
+                    uint8_t *row = bop + k2 * 1024 + (c0 >> 4) * 128;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) y[(c0 + j) + 128 * k2] = make_float2(dr[j] * inv, di[j] * inv);
+                    for (int p = 0; p < 8; ++p)
+                        *reinterpret_cast<float4 *>(row + ((p ^ (k2 & 7)) << 4)) =
+                            make_float4(dr[2 * p] * inv, di[2 * p] * inv, dr[2 * p + 1] * inv, di[2 * p + 1] * inv);
                 }
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
+        float4 *y4 = reinterpret_cast<float4 *>(y);
+        for (int q = tid; q < N2 * 64; q += kTcThreads) {
+            const int k2 = q >> 6, piece = q & 63;
+            __stcs(y4 + q, *reinterpret_cast<const float4 *>(bop + k2 * 1024 + (piece >> 3) * 128 +
+                                                             (((piece & 7) ^ (k2 & 7)) << 4)));
+        }
+        if (tid == 0 && err) s_err = 1;
+        __syncthreads();  // staging read out before the next item's input overwrites it
+        if (s_err) break;
     }
-    if (!ok) {  // a commit never arrived: record it, give the MMAs one more bounded wait, free TMEM
-        if (tid == 0) *reinterpret_cast<volatile int *>(a.status) = 1;
-        mbar_wait(&mbar, phase - 1);
+    if (s_err && tid == 0) {  // a wait timed out: record it, let copies and MMAs in flight finish (bounded)
+        *reinterpret_cast<volatile int *>(a.status) = 1;
+        for (int b = 0; b < NRING; ++b)
+            if (pend & (1u << b)) mbar_wait(&full[b], (pend_g[b] / NRING) & 1u);
+        mma_commit(&done);
+        mbar_wait(&done, done_n & 1u);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -386,11 +540,6 @@ std::vector<__half> dft_tiles(int nf, int mtiles, int ksteps) {
     return out;
 }
 
-template <int N2>
-constexpr size_t tc_smem() {
-    return 4 * static_cast<size_t>((N2 + 15) / 16 * 16) * 128 * 2 + static_cast<size_t>((N2 + 127) / 128) * 4 * kTile;
-}
-
 template <int N2, bool INV>
 cudaError_t launch_tc_fft(const TcFftArgs &args, cudaStream_t st) {
     if (args.n_items <= 0) return cudaSuccess;
@@ -399,10 +548,10 @@ cudaError_t launch_tc_fft(const TcFftArgs &args, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)  // cheap; set each time so that every device gets it
         e = cudaFuncSetAttribute(k_tc_fft<N2, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(tc_smem<N2>()));
+                                 static_cast<int>(TcGeo<N2>::SMEM));
     if (e != cudaSuccess) return e;
     const unsigned grid = static_cast<unsigned>(args.n_items < sms ? args.n_items : sms);
-    k_tc_fft<N2, INV><<<grid, kTcThreads, tc_smem<N2>(), st>>>(args);
+    k_tc_fft<N2, INV><<<grid, kTcThreads, TcGeo<N2>::SMEM, st>>>(args);
     return cudaGetLastError();
 }
 
@@ -495,6 +644,8 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
 // that fit the handle's scratch.
 int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st) {
     if (n_snaps <= 0) return SDBE_OK;
+    if (reinterpret_cast<uintptr_t>(out) & 15u)  // the transform writes 16-byte pieces
+        return fail(h, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 needs a 16-byte aligned output buffer");
     if (int rc = tc_prepare(h, st)) return rc;
     const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
     const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kBatchSnaps;
@@ -511,6 +662,8 @@ int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float
 
 int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, cudaStream_t st) {
     if (n_chunks <= 0) return SDBE_OK;
+    if ((reinterpret_cast<uintptr_t>(in) & 7u) || (reinterpret_cast<uintptr_t>(out) & 15u))
+        return fail(h, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 needs 8-byte aligned input and 16-byte aligned output");
     if (int rc = tc_prepare(h, st)) return rc;
     const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
     const uint8_t *f143 = static_cast<const uint8_t *>(h->tc_f143);
