@@ -116,20 +116,21 @@ def _load_tensor_peak():
 
 
 # Tensor FLOPs of one k_tc_fft transform of length 128*N2: step 1 is 8 K-steps
-# of 12 MMAs (3 split products x 4 real products) of 128 x NP x 16, step 3 is
-# ceil(N2/128) M tiles x NP/16 K-steps of 12 MMAs of 128 x 128 x 16.
-def _tc_flops(n2):
+# of 4*splits MMAs (split products x 4 real products) of 128 x NP x 16, step 3
+# is ceil(N2/128) M tiles x NP/16 K-steps of 4*splits MMAs of 128 x 128 x 16.
+def _tc_flops(n2, splits=3):
     np_ = (n2 + 15) // 16 * 16
-    return 8 * 12 * 2 * 128 * np_ * 16 + ((n2 + 127) // 128) * (np_ // 16) * 12 * 2 * 128 * 128 * 16
+    m = 4 * splits  # MMAs per K-step and M tile
+    return 8 * m * 2 * 128 * np_ * 16 + ((n2 + 127) // 128) * (np_ // 16) * m * 2 * 128 * 128 * 16
 
 
-def _tc_roofline(prof, steps):
+def _tc_roofline(prof, steps, splits):
     """Tensor roofline of the TC form: MMA FLOPs issued per span / span time.
     Span A = pairing + TC inverse 16384 per snapshot; span BC = TC forward
     18304 + pairings + TC inverse 16384 + 2-bit packing per chunk."""
     peak, kind = _load_tensor_peak()
-    fa = prof.stage_a_snapshots * _tc_flops(128)
-    fbc = prof.stage_bc_chunks * (_tc_flops(143) + _tc_flops(128))
+    fa = prof.stage_a_snapshots * _tc_flops(128, splits)
+    fbc = prof.stage_bc_chunks * (_tc_flops(143, splits) + _tc_flops(128, splits))
     ta = fa / (prof.stage_a_ms * 1e-3) / 1e12 if prof.stage_a_ms else 0.0
     tbc = fbc / (prof.stage_bc_ms * 1e-3) / 1e12 if prof.stage_bc_ms else 0.0
     dom_bc = prof.stage_bc_ms >= prof.stage_a_ms
@@ -213,9 +214,10 @@ def run_ours(args):
     n_pkts = pkts.shape[0]
     from sdbe_gb300 import _native as N
 
-    tc = args.precision == "tc16"
+    tc = args.precision != "fp32"
+    prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
     rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=args.wave,
-                   precision=N.PRECISION_TC16 if tc else N.PRECISION_FP32)
+                   precision=prec)
     out_bytes = rs.output_bytes(frames)
     n_batches = out_bytes // (2 * 128 * 8192)
     samples_per_step = n_batches * OUT_SAMPLES_PER_BATCH * 2
@@ -322,14 +324,15 @@ def run_ours(args):
                                           "stage_bc": prof.stage_bc_ms / args.steps},
                     "fp32": fp32}
         if tc:
-            roofline = _tc_roofline(prof, args.steps)
+            roofline = _tc_roofline(prof, args.steps, 3 if args.precision == "tc16" else 2)
         cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f16x2 tensor (f32 accumulate)" if tc else "f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": {"fp32": "f32", "tc16": "f16 hi+lo x f16 hi+lo tensor (f32 accumulate)",
+                      "tc16fast": "f16 x f16 hi+lo tensor (f32 accumulate)"}[args.precision], "data": "synthetic",
             "config": {"workload": f"{frames} B-frames x 1 packet stream per GPU (2 phased sums), "
-                                   f"{'FP16 tensor-core (hi+lo split) four-step' if tc else 'FP32 radix'}-FFT path, "
+                                   f"{dict(fp32='FP32 radix', tc16='FP16 tensor-core (data and DFT hi+lo) four-step', tc16fast='FP16 tensor-core (DFT hi+lo, data FP16) four-step')[args.precision]}-FFT path, "
                                    f"trim {TRIM_MHZ} MHz, first-batch thresholds per step",
                        "frames": frames, "batches": int(n_batches), "streams_per_gpu": 2,
                        "packets_per_step": int(n_pkts), "wave_batches": args.wave,
@@ -635,8 +638,9 @@ def main():
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16"],
-                    help="group512 only: fp32 radix kernels (default) or the FP16 tensor-core form")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16", "tc16fast"],
+                    help="group512 only: fp32 radix kernels (default) or an FP16 tensor-core form "
+                         "(tc16: data and DFT matrix split hi+lo; tc16fast: DFT matrix split, data FP16)")
     ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
                     help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
                          "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")

@@ -72,9 +72,13 @@ extern "C" {
 /* arithmetic of the three FFT stages (A: C2R 32768, B: R2C 36608, C: C2R 32768) */
 #define SDBE_PRECISION_FP32 0      /* FP32 radix kernels on the CUDA cores (default)     */
 /* FP16 tensor cores: each transform a four-step GEMM (tcgen05.mma, FP32
- * accumulation in tensor memory) with the DFT matrix and the data split into
- * hi + lo FP16 halves.  sdbe_process only; not with SDBE_THRESH_WINDOW. */
+ * accumulation in tensor memory).  TC16 splits the DFT matrix and the data
+ * into hi + lo FP16 halves (three products per real product: FP32-like
+ * error); TC16_FAST splits only the DFT matrix and rounds the data to FP16
+ * (two products).  sdbe_process and the stage entry points only; not with
+ * SDBE_THRESH_WINDOW. */
 #define SDBE_PRECISION_TC16 1
+#define SDBE_PRECISION_TC16_FAST 2
 
 /* sdbe_process flags */
 #define SDBE_IN_HOST 1u            /* packets are in host memory (copied in)             */

@@ -27,7 +27,7 @@ SAMPLES_PER_OUT_PKT = 32768
 THRESH_FIRST_BATCH, THRESH_FIXED, THRESH_WINDOW = 0, 1, 2
 THRESH_BLOCK = 16
 MAP_APHIDS, MAP_MAR2015 = 0, 1
-PRECISION_FP32, PRECISION_TC16 = 0, 1
+PRECISION_FP32, PRECISION_TC16, PRECISION_TC16_FAST = 0, 1, 2
 IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED, IN_8PAC = 1, 2, 4, 8, 16, 32, 64
 PAC8_BYTES = 8504
 NOALLOC_MAX_SAMPLES = 134217728

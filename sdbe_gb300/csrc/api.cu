@@ -503,10 +503,11 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     if (cfg->channel_map != SDBE_MAP_APHIDS && cfg->channel_map != SDBE_MAP_MAR2015)
         return fail(nullptr, SDBE_ERR_ARG, "unknown channel_map");
     if (cfg->wave_batches < 0 || cfg->wave_batches > 64) return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
-    if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16)
+    if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16 &&
+        cfg->precision != SDBE_PRECISION_TC16_FAST)
         return fail(nullptr, SDBE_ERR_ARG, "unknown precision");
-    if (cfg->precision == SDBE_PRECISION_TC16 && cfg->threshold_mode == SDBE_THRESH_WINDOW)
-        return fail(nullptr, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 does not take SDBE_THRESH_WINDOW");
+    if (cfg->precision != SDBE_PRECISION_FP32 && cfg->threshold_mode == SDBE_THRESH_WINDOW)
+        return fail(nullptr, SDBE_ERR_ARG, "the tensor-core precisions do not take SDBE_THRESH_WINDOW");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
         cudaGetLastError();
@@ -588,7 +589,7 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     CallPlan c;
     int rc = plan_call(h, packets, n_packets, n_frames, b_zero, out, out_bytes, flags, pick(h, stream), c);
     if (!rc) rc = prepare_call(c);
-    if (!rc && h->cfg.precision == SDBE_PRECISION_TC16) {
+    if (!rc && h->cfg.precision != SDBE_PRECISION_FP32) {
         rc = tc_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st);
         if (!rc && !c.aligned) rc = ship_call(c, 0, c.n_out);
     } else if (!rc) {
@@ -824,7 +825,7 @@ int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, v
 int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out, void *stream) {
     if (!h || n_snapshots < 0 || (n_snapshots > 0 && (!spec || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
     DeviceGuard g(h->cfg.device);
-    if (h->cfg.precision == SDBE_PRECISION_TC16) return tc_swarm_c2r(h, spec, n_snapshots, out, pick(h, stream));
+    if (h->cfg.precision != SDBE_PRECISION_FP32) return tc_swarm_c2r(h, spec, n_snapshots, out, pick(h, stream));
     SDBE_CK(h, launch_swarm_c2r(spec, 0, 0, n_snapshots, 1, out, 0, h->tw, pick(h, stream)));
     return SDBE_OK;
 }
@@ -848,7 +849,7 @@ int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int3
 int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, void *stream) {
     if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
     DeviceGuard g(h->cfg.device);
-    if (h->cfg.precision == SDBE_PRECISION_TC16) return tc_resample_chunks(h, in, n_chunks, out, pick(h, stream));
+    if (h->cfg.precision != SDBE_PRECISION_FP32) return tc_resample_chunks(h, in, n_chunks, out, pick(h, stream));
     ResampleOut o{};
     o.fout = out;
     SDBE_CK(h, launch_resample(2, in, 0, h->skip, n_chunks, 1, o, h->tw, pick(h, stream)));

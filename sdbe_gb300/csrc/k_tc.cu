@@ -161,6 +161,12 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t &hi, uint32_t 
     lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
+// (a, b) -> the FP16 pair rn(a, b) as a 32-bit word.
+__device__ __forceinline__ uint32_t hi2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
 template <int N2>
 struct TcGeo {
     static constexpr int NP = (N2 + 15) / 16 * 16;  // step-1 N, step-3 K
@@ -191,7 +197,7 @@ struct TcGeo {
 // a row's four words by its row group for the same reason.  The output is
 // staged in shared memory as [k2][k1] with the 16-byte pieces of each 128-byte
 // segment permuted by k2 & 7, and copied out with coalesced 16-byte stores.
-template <int N2, bool INV>
+template <int N2, bool INV, int NS>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant__ TcFftArgs a) {
     using G = TcGeo<N2>;
     constexpr int NP = G::NP, MT = G::MT, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
@@ -270,13 +276,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                 const uint32_t dr = tb + (step3 ? t * 256 : 0), di = dr + (step3 ? 128 : 256);
                 const uint8_t *ab = aop + b * STAGE;
 #pragma unroll
-                for (int sp = 0; sp < 3; ++sp) {
-                    const int ah = sp == 2 ? 1 : 0, bh = sp == 1 ? 1 : 0;  // (hi,hi) (hi,lo) (lo,hi)
+                for (int q = 0; q < NS; ++q) {
+                    // products (F hi, x hi), (F hi, x lo), (F lo, x hi); NS = 2 leaves out the second
+                    const int sp = NS == 3 ? q : 2 * q;
+                    const int ah = sp == 2 ? 1 : 0, bh = sp == 1 ? 1 : 0;
                     const uint64_t ar = smem_desc(smem_u32(ab + (0 + ah) * kTile), 128, 256);
                     const uint64_t ai = smem_desc(smem_u32(ab + (2 + ah) * kTile), 128, 256);
                     const uint64_t br = smem_desc(smem_u32(bop + (0 + bh) * COMP) + s * 256, 128, sbo_b);
                     const uint64_t bi = smem_desc(smem_u32(bop + (2 + bh) * COMP) + s * 256, 128, sbo_b);
-                    const bool first = s == 0 && sp == 0;
+                    const bool first = s == 0 && q == 0;
                     // Dr += Fr Br -/+ Fi Bi ; Di += +/-Fi Br + Fr Bi
                     mma_f16(dr, ar, br, instr_desc(128, n, false), !first);
                     mma_f16(dr, ai, bi, instr_desc(128, n, !INV), true);
@@ -330,14 +338,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
             const int q = i * 8 + warp;
             const int row = (q % RG) * 8 + (lane & 7);
             const int k = ((q / RG) * 4 + (lane >> 3)) * 2;
-            uint32_t rh, rl, ih, il;
-            split2(xv[2 * i].x * s1, xv[2 * i + 1].x * s1, rh, rl);
-            split2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1, ih, il);
             const uint32_t off = op_off(row, k, 128);
-            *reinterpret_cast<uint32_t *>(bop + off) = rh;
-            *reinterpret_cast<uint32_t *>(bop + COMP + off) = rl;
-            *reinterpret_cast<uint32_t *>(bop + 2 * COMP + off) = ih;
-            *reinterpret_cast<uint32_t *>(bop + 3 * COMP + off) = il;
+            if constexpr (NS == 3) {
+                uint32_t rh, rl, ih, il;
+                split2(xv[2 * i].x * s1, xv[2 * i + 1].x * s1, rh, rl);
+                split2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1, ih, il);
+                *reinterpret_cast<uint32_t *>(bop + off) = rh;
+                *reinterpret_cast<uint32_t *>(bop + COMP + off) = rl;
+                *reinterpret_cast<uint32_t *>(bop + 2 * COMP + off) = ih;
+                *reinterpret_cast<uint32_t *>(bop + 3 * COMP + off) = il;
+            } else {
+                *reinterpret_cast<uint32_t *>(bop + off) = hi2(xv[2 * i].x * s1, xv[2 * i + 1].x * s1);
+                *reinterpret_cast<uint32_t *>(bop + 2 * COMP + off) = hi2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1);
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -382,7 +395,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                 const uint32_t off = op_off(k1, c0 + 2 * j, NP);
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
-                    *reinterpret_cast<uint32_t *>(bop + c * COMP + off) = pick4(w[c][0], w[c][1], w[c][2], w[c][3], j);
+                    if (NS == 3 || (c & 1) == 0)  // NS = 2 keeps the data's hi halves only
+                        *reinterpret_cast<uint32_t *>(bop + c * COMP + off) =
+                            pick4(w[c][0], w[c][1], w[c][2], w[c][3], j);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -540,22 +555,30 @@ std::vector<__half> dft_tiles(int nf, int mtiles, int ksteps) {
     return out;
 }
 
-template <int N2, bool INV>
-cudaError_t launch_tc_fft(const TcFftArgs &args, cudaStream_t st) {
-    if (args.n_items <= 0) return cudaSuccess;
+template <int N2, bool INV, int NS>
+cudaError_t launch_tc_fft_ns(const TcFftArgs &args, cudaStream_t st) {
     int dev = 0, sms = 1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)  // cheap; set each time so that every device gets it
-        e = cudaFuncSetAttribute(k_tc_fft<N2, INV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(k_tc_fft<N2, INV, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(TcGeo<N2>::SMEM));
     if (e != cudaSuccess) return e;
     const unsigned grid = static_cast<unsigned>(args.n_items < sms ? args.n_items : sms);
-    k_tc_fft<N2, INV><<<grid, kTcThreads, TcGeo<N2>::SMEM, st>>>(args);
+    k_tc_fft<N2, INV, NS><<<grid, kTcThreads, TcGeo<N2>::SMEM, st>>>(args);
     return cudaGetLastError();
 }
 
+// ns = split products per complex product: 3 (SDBE_PRECISION_TC16) or 2 (SDBE_PRECISION_TC16_FAST).
+template <int N2, bool INV>
+cudaError_t launch_tc_fft(const TcFftArgs &args, int ns, cudaStream_t st) {
+    if (args.n_items <= 0) return cudaSuccess;
+    return ns == 3 ? launch_tc_fft_ns<N2, INV, 3>(args, st) : launch_tc_fft_ns<N2, INV, 2>(args, st);
+}
+
 }  // namespace
+
+static int tc_splits(const sdbe_resampler *h) { return h->cfg.precision == SDBE_PRECISION_TC16 ? 3 : 2; }
 
 // Tables and scratch of the tensor-core path, on first use.
 int tc_prepare(sdbe_resampler *h, cudaStream_t st) {
@@ -605,7 +628,7 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
         float2 *ts = reinterpret_cast<float2 *>(h->ts);
         const TcFftArgs A{h->tc_bufx, kMA, snaps * kMA, ts, kMA, h->ts_pol_stride / 2,
                           snaps, 2 * snaps, f128, f128, tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(A, st)));
+        SDBE_CK(h, (launch_tc_fft<128, true>(A, tc_splits(h), st)));
         if (!first) {
             SDBE_CK(h, timed_end(h, slot, st));
             SDBE_CK(h, timed_begin(h, 1, 2 * chunks, st, &slot));
@@ -613,7 +636,7 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
         // stage B: chunks of 18304 complex -> Z (bufy)
         const TcFftArgs B{ts, kMB, h->ts_pol_stride / 2, h->tc_bufy, kMB, chunks * kMB,
                           chunks, 2 * chunks, f128, f143, tw.w18304, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<143, false>(B, st)));
+        SDBE_CK(h, (launch_tc_fft<143, false>(B, tc_splits(h), st)));
         // pairings: bufy -> Z' (bufx)
         k_tc_pair_bc<<<static_cast<unsigned>(2 * chunks), 256, 0, st>>>(h->tc_bufy, h->tc_bufx, h->skip, tw.w32768,
                                                                         tw.w36608);
@@ -621,7 +644,7 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
         // stage C: Z' -> floats (bufy, 32768 per chunk)
         const TcFftArgs C{h->tc_bufx, kMA, chunks * kMA, h->tc_bufy, kMA, chunks * kMA,
                           chunks, 2 * chunks, f128, f128, tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(C, st)));
+        SDBE_CK(h, (launch_tc_fft<128, true>(C, tc_splits(h), st)));
         const float *yf = reinterpret_cast<const float *>(h->tc_bufy);
         if (first) {
             k_tc_chunk_stats<<<dim3(kChunks, 2), 256, 0, st>>>(yf, chunks * kNC, kChunks, h->partials);
@@ -655,7 +678,7 @@ int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float
         SDBE_CK(h, cudaGetLastError());
         const TcFftArgs A{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + s0 * kNA), kMA, 0,
                           n, n, f128, f128, h->tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(A, st)));
+        SDBE_CK(h, (launch_tc_fft<128, true>(A, tc_splits(h), st)));
     }
     return SDBE_OK;
 }
@@ -672,13 +695,13 @@ int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, flo
         const int64_t n = n_chunks - c0 < cap ? n_chunks - c0 : cap;
         const TcFftArgs B{reinterpret_cast<const float2 *>(in + c0 * kNB), kMB, 0, h->tc_bufy, kMB, 0,
                           n, n, f128, f143, h->tw.w18304, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<143, false>(B, st)));
+        SDBE_CK(h, (launch_tc_fft<143, false>(B, tc_splits(h), st)));
         k_tc_pair_bc<<<static_cast<unsigned>(n), 256, 0, st>>>(h->tc_bufy, h->tc_bufx, h->skip, h->tw.w32768,
                                                                h->tw.w36608);
         SDBE_CK(h, cudaGetLastError());
         const TcFftArgs C{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + c0 * kNC), kMA, 0,
                           n, n, f128, f128, h->tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(C, st)));
+        SDBE_CK(h, (launch_tc_fft<128, true>(C, tc_splits(h), st)));
     }
     return SDBE_OK;
 }
