@@ -121,7 +121,7 @@ struct TcFftArgs {
     int64_t out_stride, out_pol_stride;
     int64_t per_pol, n_items;          // items per pol, items in all
     const uint8_t *f1;                 // DFT-128 tiles [8 K-steps][4 comps][4 KB]
-    const uint8_t *f2;                 // DFT-N2 tiles [K-steps][M tiles][4 comps][4 KB]
+    const uint8_t *f2;                 // DFT-N2 tiles [K-steps][4 comps][NP rows x 16 k]
     const float2 *tw;                  // e^{-2 pi i e / (128 N2)}, e < 128 N2
     int *status;                       // set to 1 on a barrier time-out (host-mapped)
 };
@@ -169,24 +169,28 @@ __device__ __forceinline__ uint32_t hi2(float a, float b) {
 
 template <int N2>
 struct TcGeo {
-    static constexpr int NP = (N2 + 15) / 16 * 16;  // step-1 N, step-3 K
-    static constexpr int MT = (N2 + 127) / 128;     // step-3 M tiles
+    static constexpr int NP = (N2 + 15) / 16 * 16;  // N of both GEMMs, step-3 K
     static constexpr int KS3 = NP / 16;             // step-3 K-steps (step 1 has 8)
-    static constexpr int SPI = 8 + KS3 * MT;        // pipeline stages per item (one M tile, one K-step each)
+    static constexpr int SPI = 8 + KS3;             // pipeline stages (K-steps) per item
     static constexpr int RG = NP / 8;               // 8-row groups of the step-1 B operand
     static constexpr int NPAIR = NP * 64 / kTcThreads;  // input element pairs per thread
     static constexpr uint32_t COMP = NP * 128 * 2;  // bytes of one B-operand component
-    static constexpr int NRING = 4;                 // A-tile buffers
-    static constexpr uint32_t STAGE = 4 * kTile;    // bytes of one stage's A tiles
+    static constexpr int NRING = 4;                 // DFT-tile buffers
+    static constexpr uint32_t STAGE1 = 4 * kTile;   // bytes of a step-1 stage: DFT-128 [128 rows][16 k] x 4
+    static constexpr uint32_t STAGE3 = 4 * NP * 32; // bytes of a step-3 stage: DFT-N2 [NP rows][16 k] x 4
+    static constexpr uint32_t STAGE = STAGE3 > STAGE1 ? STAGE3 : STAGE1;
     static constexpr size_t SMEM = 4 * static_cast<size_t>(COMP) + NRING * static_cast<size_t>(STAGE) +
                                    (N2 + 128) * sizeof(float2);
-    static_assert(static_cast<size_t>(N2) * 1024 <= 4 * static_cast<size_t>(COMP), "output staging fits");
 };
 
 // One CTA per SM (its shared memory and all 512 TMEM columns), persistent
-// over items.  Thread 0 issues the MMAs and the bulk copies of the DFT tiles
-// through a ring of four 16 KB buffers (the tiles of stage g+3 load while the
-// MMAs of stage g run; a stage is one K-step of one M tile); warps 1-7 load
+// over items.  Step 1 is D[k1][n2] = F128 (A) x B[n2][n1] (B operand); step 3
+// is D[k1][k2] = B2[k1][n2] (A) x F_N2[k2][n2] (B operand), so both GEMMs are
+// 128 x NP and step 3 leaves y[k1 + 128 k2] in TMEM lane k1, column k2, which
+// a warp stores as 32 consecutive complex values.  Accumulators: Dr at column
+// 0, Di at 256.  Thread 0 issues the MMAs and the bulk copies of the DFT tiles
+// through a ring of four buffers (the tiles of K-step g+3 load while the MMAs
+// of K-step g run); warps 1-7 load
 // the next item's input into registers while the current item's step-3 GEMM
 // runs, warp 0 (whose lane 0 issues) after it.
 //
@@ -194,17 +198,15 @@ struct TcGeo {
 // is row (q % RG)*8 + (p & 7) and K columns 2kp, 2kp+1 with q = p >> 5 and
 // kp = (q / RG)*4 + ((p >> 3) & 3), so one warp's 32-bit stores cover whole
 // 128-byte core-matrix rows: no bank conflicts.  Step 2 rotates the order of
-// a row's four words by its row group for the same reason.  The output is
-// staged in shared memory as [k2][k1] with the 16-byte pieces of each 128-byte
-// segment permuted by k2 & 7, and copied out with coalesced 16-byte stores.
+// a row's four words by its row group for the same reason.
 template <int N2, bool INV, int NS>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant__ TcFftArgs a) {
     using G = TcGeo<N2>;
-    constexpr int NP = G::NP, MT = G::MT, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
+    constexpr int NP = G::NP, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
     constexpr int NRING = G::NRING;
-    constexpr uint32_t COMP = G::COMP, STAGE = G::STAGE;
+    constexpr uint32_t COMP = G::COMP, STAGE = G::STAGE, STAGE1 = G::STAGE1, STAGE3 = G::STAGE3;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *bop = smem;                                               // [4 comps][COMP]; output staging
+    uint8_t *bop = smem;                                               // [4 comps][COMP]
     uint8_t *aop = smem + 4 * COMP;                                    // [NRING][STAGE]
     float2 *twh = reinterpret_cast<float2 *>(aop + NRING * STAGE);    // w^(128 i), i < N2
     float2 *twl = twh + N2;                                            // w^j, j < 128
@@ -251,18 +253,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         const int64_t item = blockIdx.x + static_cast<int64_t>(gg / SPI) * gridDim.x;
         if (item >= a.n_items) return;
         const int kk = static_cast<int>(gg % SPI), b = gg % NRING;
-        const uint8_t *src = kk < 8 ? a.f1 + kk * STAGE : a.f2 + (kk - 8) * STAGE;
-        bulk_load(aop + b * STAGE, src, STAGE, &full[b]);
+        const uint8_t *src = kk < 8 ? a.f1 + kk * STAGE1 : a.f2 + (kk - 8) * STAGE3;
+        bulk_load(aop + b * STAGE, src, kk < 8 ? STAGE1 : STAGE3, &full[b]);
         pend |= 1u << b;
         pend_g[b] = gg;
     };
-    // One GEMM phase (thread 0): nst stages; step 1 (one M tile, N = NP, Dr at
-    // column 0, Di at 256) or step 3 (stage j = K-step j / MT of M tile j % MT,
-    // N = 128, Dr at 256 t, Di at 256 t + 128).
+    // One GEMM phase (thread 0), nst K-steps: step 1 (A = DFT-128 tiles from
+    // the ring, B = the data in bop with K = 128) or step 3 (A = the data in
+    // bop with K = NP, B = DFT-N2 tiles from the ring).
     auto gemm = [&](int nst, bool step3) {
-        const int n = step3 ? 128 : NP;
-        const uint32_t sbo_b = step3 ? (NP / 8) * 128 : 16 * 128;
-        for (int j = 0; j < nst; ++j, ++g) {
+        const uint32_t dr = tb, di = tb + 256;
+        const uint32_t idesc = instr_desc(128, NP, false), idesc_m = instr_desc(128, NP, true);
+        for (int s = 0; s < nst; ++s, ++g) {
             const int b = g % NRING;
             if (!err) {
                 if (mbar_wait(&full[b], (g / NRING) & 1u))
@@ -272,30 +274,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
             }
             if (!err) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const int s = step3 ? j / MT : j, t = step3 ? j % MT : 0;
-                const uint32_t dr = tb + (step3 ? t * 256 : 0), di = dr + (step3 ? 128 : 256);
                 const uint8_t *ab = aop + b * STAGE;
 #pragma unroll
                 for (int q = 0; q < NS; ++q) {
                     // products (F hi, x hi), (F hi, x lo), (F lo, x hi); NS = 2 leaves out the second
                     const int sp = NS == 3 ? q : 2 * q;
-                    const int ah = sp == 2 ? 1 : 0, bh = sp == 1 ? 1 : 0;
-                    const uint64_t ar = smem_desc(smem_u32(ab + (0 + ah) * kTile), 128, 256);
-                    const uint64_t ai = smem_desc(smem_u32(ab + (2 + ah) * kTile), 128, 256);
-                    const uint64_t br = smem_desc(smem_u32(bop + (0 + bh) * COMP) + s * 256, 128, sbo_b);
-                    const uint64_t bi = smem_desc(smem_u32(bop + (2 + bh) * COMP) + s * 256, 128, sbo_b);
+                    const int fh = sp == 2 ? 1 : 0, xh = sp == 1 ? 1 : 0;
                     const bool first = s == 0 && q == 0;
-                    // Dr += Fr Br -/+ Fi Bi ; Di += +/-Fi Br + Fr Bi
-                    mma_f16(dr, ar, br, instr_desc(128, n, false), !first);
-                    mma_f16(dr, ai, bi, instr_desc(128, n, !INV), true);
-                    mma_f16(di, ai, br, instr_desc(128, n, INV), !first);
-                    mma_f16(di, ar, bi, instr_desc(128, n, false), true);
+                    if (!step3) {
+                        const uint64_t fr = smem_desc(smem_u32(ab + (0 + fh) * kTile), 128, 256);
+                        const uint64_t fi = smem_desc(smem_u32(ab + (2 + fh) * kTile), 128, 256);
+                        const uint64_t xr = smem_desc(smem_u32(bop + (0 + xh) * COMP) + s * 256, 128, 16 * 128);
+                        const uint64_t xi = smem_desc(smem_u32(bop + (2 + xh) * COMP) + s * 256, 128, 16 * 128);
+                        // Dr += Fr Xr -/+ Fi Xi ; Di += +/-Fi Xr + Fr Xi
+                        mma_f16(dr, fr, xr, idesc, !first);
+                        mma_f16(dr, fi, xi, INV ? idesc : idesc_m, true);
+                        mma_f16(di, fi, xr, INV ? idesc_m : idesc, !first);
+                        mma_f16(di, fr, xi, idesc, true);
+                    } else {
+                        const uint64_t xr = smem_desc(smem_u32(bop + (0 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
+                        const uint64_t xi = smem_desc(smem_u32(bop + (2 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
+                        const uint64_t fr = smem_desc(smem_u32(ab + (0 + fh) * (NP * 32)), 128, 256);
+                        const uint64_t fi = smem_desc(smem_u32(ab + (2 + fh) * (NP * 32)), 128, 256);
+                        mma_f16(dr, xr, fr, idesc, !first);
+                        mma_f16(dr, xi, fi, INV ? idesc : idesc_m, true);
+                        mma_f16(di, xr, fi, INV ? idesc_m : idesc, !first);
+                        mma_f16(di, xi, fr, idesc, true);
+                    }
                 }
             }
             mma_commit(&empty[b]);
-            if (j == nst - 1) mma_commit(&done);
+            if (s == nst - 1) mma_commit(&done);
             if (!err) {
-                // the buffer of stage g-1 takes stage g+3 once those MMAs are done
+                // the buffer of K-step g-1 takes K-step g+3 once those MMAs are done
                 if (g >= 1 && !mbar_wait(&empty[(g - 1) % NRING], ((g - 1) / NRING) & 1u)) err = true;
                 if (!err) issue_copy(g + NRING - 1);
             }
@@ -403,39 +414,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
-        // ---- step 3: D[k2][k1] per M tile --------------------------------------------
+        // ---- step 3: D[k1][k2] -----------------------------------------------------
         const bool more = item + gridDim.x < a.n_items;
-        if (tid == 0) gemm(KS3 * MT, true);
+        if (tid == 0) gemm(KS3, true);
         if (more && warp != 0) load_input(item + gridDim.x);  // lands during the GEMM
         wait_done();
         if (more && warp == 0) load_input(item + gridDim.x);  // not beside the issuing lane
-        // ---- output: TMEM -> staging [k2][k1] in shared memory -> y ------------------
+        // ---- output: y[k1 + 128 k2], a warp's stores 32 consecutive values ----------
         const float inv = (1.f / s1) * (1.f / s2);  // powers of two: exact
-        for (int t = 0; t < MT; ++t) {
-            const int k2 = t * 128 + quarter * 32 + lane;
-            for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 16) {
-                float dr[16], di[16];
-                tmem_ld8x2(lane_base + t * 256 + c0, lane_base + t * 256 + 128 + c0, dr, di);
-                tmem_ld8x2(lane_base + t * 256 + c0 + 8, lane_base + t * 256 + 128 + c0 + 8, dr + 8, di + 8);
-                if (k2 < N2) {
-                    uint8_t *row = bop + k2 * 1024 + (c0 >> 4) * 128;
+        for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
+            float dr[8], di[8];
+            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
 #pragma unroll
-                    for (int p = 0; p < 8; ++p)
-                        *reinterpret_cast<float4 *>(row + ((p ^ (k2 & 7)) << 4)) =
-                            make_float4(dr[2 * p] * inv, di[2 * p] * inv, dr[2 * p + 1] * inv, di[2 * p + 1] * inv);
-                }
-            }
+            for (int j = 0; j < 8; ++j)
+                if (c0 + j < N2) __stcs(y + k1 + 128 * (c0 + j), make_float2(dr[j] * inv, di[j] * inv));
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        float4 *y4 = reinterpret_cast<float4 *>(y);
-        for (int q = tid; q < N2 * 64; q += kTcThreads) {
-            const int k2 = q >> 6, piece = q & 63;
-            __stcs(y4 + q, *reinterpret_cast<const float4 *>(bop + k2 * 1024 + (piece >> 3) * 128 +
-                                                             (((piece & 7) ^ (k2 & 7)) << 4)));
-        }
         if (tid == 0 && err) s_err = 1;
-        __syncthreads();  // staging read out before the next item's input overwrites it
+        __syncthreads();  // TMEM read out before the next item's MMAs
         if (s_err) break;
     }
     if (s_err && tid == 0) {  // a wait timed out: record it, let copies and MMAs in flight finish (bounded)
@@ -524,34 +520,33 @@ __global__ void k_tc_chunk_stats(const float *__restrict__ y, int64_t y_pol_stri
     }
 }
 
-// Pre-tiled DFT matrices for the tensor cores: tile (K-step s, M tile t,
-// component c) holds F[128 t + r][16 s + kk] in core-matrix order, F[m][k] =
-// e^{-2 pi i m k / nf} (zero outside nf x nf); components re hi, re lo, im
-// hi, im lo.  Layout [s][t][c]: one K-step's tiles are contiguous.
-std::vector<__half> dft_tiles(int nf, int mtiles, int ksteps) {
-    std::vector<__half> out(static_cast<size_t>(mtiles) * ksteps * 4 * (kTile / 2));
-    for (int t = 0; t < mtiles; ++t)
-        for (int s = 0; s < ksteps; ++s)
-            for (int r = 0; r < 128; ++r)
-                for (int kk = 0; kk < 16; ++kk) {
-                    const int mrow = 128 * t + r, k = 16 * s + kk;
-                    double re = 0.0, im = 0.0;
-                    if (mrow < nf && k < nf) {
-                        const long long e = static_cast<long long>(mrow) * k % nf;
-                        const double ang = -2.0 * 3.14159265358979323846 * static_cast<double>(e) / nf;
-                        re = std::cos(ang);
-                        im = std::sin(ang);
-                    }
-                    const float rh = __half2float(__float2half_rn(static_cast<float>(re)));
-                    const float ih = __half2float(__float2half_rn(static_cast<float>(im)));
-                    const __half vals[4] = {__float2half_rn(static_cast<float>(re)),
-                                            __float2half_rn(static_cast<float>(re - rh)),
-                                            __float2half_rn(static_cast<float>(im)),
-                                            __float2half_rn(static_cast<float>(im - ih))};
-                    const size_t off = (r >> 3) * 128 + (kk >> 3) * 64 + (r & 7) * 8 + (kk & 7);  // in halves
-                    for (int c = 0; c < 4; ++c)
-                        out[((static_cast<size_t>(s) * mtiles + t) * 4 + c) * (kTile / 2) + off] = vals[c];
+// Pre-tiled DFT matrices for the tensor cores: K-step s, component c (re hi,
+// re lo, im hi, im lo) holds F[r][16 s + kk], r < rows, kk < 16, in
+// core-matrix order (8 rows x 16 bytes; K step 128 bytes, row-group step 256
+// bytes); F[m][k] = e^{-2 pi i m k / nf}, zero outside nf x nf.  Layout
+// [s][c][rows x 16]: one K-step's tiles are contiguous.
+std::vector<__half> dft_tiles(int nf, int rows, int ksteps) {
+    std::vector<__half> out(static_cast<size_t>(ksteps) * 4 * rows * 16);
+    for (int s = 0; s < ksteps; ++s)
+        for (int r = 0; r < rows; ++r)
+            for (int kk = 0; kk < 16; ++kk) {
+                const int k = 16 * s + kk;
+                double re = 0.0, im = 0.0;
+                if (r < nf && k < nf) {
+                    const long long e = static_cast<long long>(r) * k % nf;
+                    const double ang = -2.0 * 3.14159265358979323846 * static_cast<double>(e) / nf;
+                    re = std::cos(ang);
+                    im = std::sin(ang);
                 }
+                const float rh = __half2float(__float2half_rn(static_cast<float>(re)));
+                const float ih = __half2float(__float2half_rn(static_cast<float>(im)));
+                const __half vals[4] = {__float2half_rn(static_cast<float>(re)),
+                                        __float2half_rn(static_cast<float>(re - rh)),
+                                        __float2half_rn(static_cast<float>(im)),
+                                        __float2half_rn(static_cast<float>(im - ih))};
+                const size_t off = (r >> 3) * 128 + (kk >> 3) * 64 + (r & 7) * 8 + (kk & 7);  // in halves
+                for (int c = 0; c < 4; ++c) out[(static_cast<size_t>(s) * 4 + c) * rows * 16 + off] = vals[c];
+            }
     return out;
 }
 
@@ -583,7 +578,7 @@ static int tc_splits(const sdbe_resampler *h) { return h->cfg.precision == SDBE_
 // Tables and scratch of the tensor-core path, on first use.
 int tc_prepare(sdbe_resampler *h, cudaStream_t st) {
     if (h->tc_f128) return SDBE_OK;
-    const std::vector<__half> f128 = dft_tiles(128, 1, 8), f143 = dft_tiles(143, 2, 9);
+    const std::vector<__half> f128 = dft_tiles(128, 128, 8), f143 = dft_tiles(143, 144, 9);
     const size_t wave_snaps = static_cast<size_t>(h->wave) * kBatchSnaps;
     const size_t wave_chunks = static_cast<size_t>(h->wave) * kChunks;
     if (cudaMalloc(&h->tc_f128, f128.size() * sizeof(__half)) != cudaSuccess ||
