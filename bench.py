@@ -115,13 +115,12 @@ def _load_tensor_peak():
         return 1700.0, "fallback (sustained)"
 
 
-# Tensor FLOPs of one k_tc_fft transform of length 128*N2: step 1 is 8 K-steps
-# of 4*splits MMAs (split products x 4 real products) of 128 x NP x 16, step 3
-# is ceil(N2/128) M tiles x NP/16 K-steps of 4*splits MMAs of 128 x 128 x 16.
+# Tensor FLOPs one k_tc_fft transform of length 128*N2 issues: step 1 is 8
+# K-steps and step 3 is NP/16 K-steps (NP = N2 rounded up to 16), each of
+# 4*splits MMAs (split products x 4 real products) of 128 x NP x 16.
 def _tc_flops(n2, splits=3):
     np_ = (n2 + 15) // 16 * 16
-    m = 4 * splits  # MMAs per K-step and M tile
-    return 8 * m * 2 * 128 * np_ * 16 + ((n2 + 127) // 128) * (np_ // 16) * m * 2 * 128 * 128 * 16
+    return (8 + np_ // 16) * 4 * splits * 2 * 128 * np_ * 16
 
 
 def _tc_roofline(prof, steps, splits):
