@@ -106,6 +106,12 @@ def _load_peaks():
         return 6800.0, "fallback"
 
 
+_DTYPE = {"fp32": "f32", "tc16": "f16 hi+lo x f16 hi+lo tensor (f32 accumulate)",
+          "tc16fast": "f16 x f16 hi+lo tensor (f32 accumulate)"}
+_PATH = {"fp32": "FP32 radix", "tc16": "FP16 tensor-core (data and DFT hi+lo) four-step",
+         "tc16fast": "FP16 tensor-core (DFT hi+lo, data FP16) four-step"}
+
+
 def _load_tensor_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -328,10 +334,9 @@ def run_ours(args):
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp32": "f32", "tc16": "f16 hi+lo x f16 hi+lo tensor (f32 accumulate)",
-                      "tc16fast": "f16 x f16 hi+lo tensor (f32 accumulate)"}[args.precision], "data": "synthetic",
+            "vs_baseline": None, "dtype": _DTYPE[args.precision], "data": "synthetic",
             "config": {"workload": f"{frames} B-frames x 1 packet stream per GPU (2 phased sums), "
-                                   f"{dict(fp32='FP32 radix', tc16='FP16 tensor-core (data and DFT hi+lo) four-step', tc16fast='FP16 tensor-core (DFT hi+lo, data FP16) four-step')[args.precision]}-FFT path, "
+                                   f"{_PATH[args.precision]}-FFT path, "
                                    f"trim {TRIM_MHZ} MHz, first-batch thresholds per step",
                        "frames": frames, "batches": int(n_batches), "streams_per_gpu": 2,
                        "packets_per_step": int(n_pkts), "wave_batches": args.wave,
@@ -367,6 +372,10 @@ def run_streams(args):
         return 0
     from sdbe_gb300 import Resampler, autotune, host_buffer, process_multi, synth
 
+    from sdbe_gb300 import _native as N
+
+    tc = args.precision != "fp32"
+    prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
     specs = synth.config4(n_packet_streams=4)
     pk = [synth.generate(sp) for sp in specs]
     frames = [sp.n_frames for sp in specs]
@@ -374,7 +383,8 @@ def run_streams(args):
     stream = torch.cuda.Stream()
 
     def make(wave):
-        hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=f, wave_batches=wave) for f in frames]
+        hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=f, wave_batches=wave, precision=prec)
+              for f in frames]
         outs = [torch.empty(h.output_bytes(f), dtype=torch.uint8, device="cuda") for h, f in zip(hs, frames)]
         return hs, outs
 
@@ -398,7 +408,7 @@ def run_streams(args):
             h.close()
         return e0.elapsed_time(e1) / 2
 
-    key = "streams8|" + ",".join(map(str, frames))
+    key = "streams8|" + ("" if not tc else args.precision + "|") + ",".join(map(str, frames))
     wave, table = (args.wave, {}) if args.wave else autotune.tune(key, measure)
     hs, outs = make(wave)
     n_batches = [h.output_bytes(f) // (2 * 128 * 8192) for h, f in zip(hs, frames)]
@@ -478,20 +488,24 @@ def run_streams(args):
     bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
     bc_bytes = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) * (36608 * 4 + 8192)
     achieved = bc_bytes / (bc_ms * 1e-3) / 1e9 if bc_ms else None
+    roofline = {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
+                "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes}
+    if tc:
+        roofline = _tc_roofline(prof, 1, 3 if args.precision == "tc16" else 2)
     line = {
         "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": 1, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": _DTYPE[args.precision], "data": "synthetic",
         "config": {"workload": "8 streams (4 packet streams x 2 phased sums), uneven seeded lengths, per-stream "
-                               "sigma; one sdbe_process_multi pass per step, CUDA-graph replay",
+                               "sigma; one sdbe_process_multi pass per step, CUDA-graph replay; "
+                               + _PATH[args.precision] + "-FFT path",
                    "frames_per_packet_stream": frames, "batches_per_packet_stream": n_batches,
                    "wave_batches": wave, "autotune_ms_per_pass": table,
                    "l2": "inputs larger than L2"},
         "x_realtime": value / (REALTIME_GSPS * 8),
         "direct_ms_per_step": ms_direct,
-        "roofline": {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                     "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes},
+        "roofline": roofline,
         "e2e": {"value": samples / (e2e_ms * 1e-3) / 1e9, "unit": "GS/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(sum(p.nbytes for p in pk)),
                 "d2h_bytes_per_step": int(sum(o.numel() for o in outs)),
@@ -638,12 +652,14 @@ def main():
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16", "tc16fast"],
-                    help="group512 only: fp32 radix kernels (default) or an FP16 tensor-core form "
+                    help="group512 and streams8: fp32 radix kernels (default) or an FP16 tensor-core form "
                          "(tc16: data and DFT matrix split hi+lo; tc16fast: DFT matrix split, data FP16)")
     ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
                     help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
                          "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")
     args = ap.parse_args()
+    if args.workload == "stress32" and args.precision != "fp32":
+        ap.error("stress32 uses windowed thresholds, which the tensor-core precisions do not take")
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "streams8":

@@ -379,10 +379,55 @@ int complete_call(CallPlan &c, sdbe_result *result) {
     return SDBE_OK;
 }
 
+// fft_chain_multi for tensor-core handles (all of one precision): the first
+// batches of every handle that needs thresholds in one wave, then waves of up
+// to the smallest handle wave, each transform one launch over all handles.
+int tc_chain_multi(std::vector<CallPlan> &cs) {
+    cudaStream_t st = cs[0].st;
+    const int n = static_cast<int>(cs.size());
+    std::vector<int64_t> b(static_cast<size_t>(n), 0);
+    std::vector<TcWaveItem> w;
+    for (int i = 0; i < n; ++i) {
+        sdbe_resampler *h = cs[i].h;
+        if (cs[i].n_batches == 0 || h->thresholds_set) continue;
+        w.push_back(TcWaveItem{h, h->spec, h->spec_pol_stride, 0, 1, cs[i].pt});
+    }
+    if (int rc = tc_wave_multi(w, true, st)) return rc;
+    for (const auto &it : w)
+        for (int i = 0; i < n; ++i)
+            if (cs[i].h == it.h) {
+                b[i] = 1;
+                if (!cs[i].aligned)
+                    if (int rc = ship_call(cs[i], 0, kChunks)) return rc;
+            }
+    int wave = cs[0].h->wave;
+    for (const auto &c : cs) wave = std::min(wave, c.h->wave);
+    while (true) {
+        w.clear();
+        std::vector<int> act;
+        for (int i = 0; i < n; ++i) {
+            if (b[i] >= cs[i].n_batches) continue;
+            const int64_t nb = std::min<int64_t>(wave, cs[i].n_batches - b[i]);
+            w.push_back(TcWaveItem{cs[i].h, cs[i].h->spec, cs[i].h->spec_pol_stride, b[i], nb, cs[i].pt});
+            act.push_back(i);
+        }
+        if (w.empty()) break;
+        if (int rc = tc_wave_multi(w, false, st)) return rc;
+        for (size_t k = 0; k < act.size(); ++k) {
+            const int i = act[k];
+            if (!cs[i].aligned)
+                if (int rc = ship_call(cs[i], b[i] * kChunks, (b[i] + w[k].nb) * kChunks)) return rc;
+            b[i] += w[k].nb;
+        }
+    }
+    return SDBE_OK;
+}
+
 // The FFT chain of several handles on one stream: the first-batch threshold
 // path of every handle that needs it in one pair of launches, then waves in
 // which one stage-A and one stage-BC launch cover every handle's batches.
 int fft_chain_multi(std::vector<CallPlan> &cs) {
+    if (cs[0].h->cfg.precision != SDBE_PRECISION_FP32) return tc_chain_multi(cs);
     sdbe_resampler *h0 = cs[0].h;
     cudaStream_t st = cs[0].st;
     const int n = static_cast<int>(cs.size());
@@ -606,8 +651,8 @@ int sdbe_process_multi(sdbe_resampler *const *hs, const sdbe_stream_desc *d, int
     for (int i = 0; i < n; ++i) {
         if (!hs[i]) return fail(nullptr, SDBE_ERR_ARG, "null handle");
         if (hs[i]->cfg.device != hs[0]->cfg.device) return fail(hs[i], SDBE_ERR_ARG, "handles on different devices");
-        if (hs[i]->cfg.precision != SDBE_PRECISION_FP32)
-            return fail(hs[i], SDBE_ERR_ARG, "sdbe_process_multi takes SDBE_PRECISION_FP32 handles only");
+        if (hs[i]->cfg.precision != hs[0]->cfg.precision)
+            return fail(hs[i], SDBE_ERR_ARG, "sdbe_process_multi needs handles of one precision");
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) return fail(hs[i], SDBE_ERR_ARG, "a handle appears twice");
     }

@@ -166,10 +166,21 @@ inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t 
     return SDBE_OK;
 }
 
-// The FFT chain of sdbe_process with SDBE_PRECISION_TC16 (k_tc.cu): same
+// The FFT chain of sdbe_process on a tensor-core handle (k_tc.cu): same
 // arguments as fft_chain, payload complete when it returns (queued on st).
 int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
              const PayloadTarget &tgt, cudaStream_t st);
+
+// Batches [b0, b0 + nb) of one handle's packed spectra in a tensor-core wave.
+struct TcWaveItem {
+    sdbe_resampler *h;
+    const uint32_t *spec;
+    int64_t spec_pol_stride, b0, nb;
+    PayloadTarget tgt;
+};
+// One wave over several tensor-core handles of the same precision, the three
+// transforms in shared launches; `first`: each item is its handle's first batch.
+int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st);
 
 // sdbe_swarm_c2r / sdbe_resample_chunks of a SDBE_PRECISION_TC16 handle (one pol).
 int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st);

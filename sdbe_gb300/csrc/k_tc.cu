@@ -114,17 +114,31 @@ __device__ __forceinline__ float block_max(float v, float *red) {
     return m;
 }
 
-struct TcFftArgs {
+// One stream pair's transforms in a launch: 2 x per_pol items, pol-major,
+// global items item0 .. item0 + 2 per_pol.
+struct TcSeg {
     const float2 *in;
     int64_t in_stride, in_pol_stride;  // complex elements between items / between pols
     float2 *out;
     int64_t out_stride, out_pol_stride;
-    int64_t per_pol, n_items;          // items per pol, items in all
+    int64_t per_pol, item0;
+};
+
+struct TcFftArgs {
+    int64_t n_items;                   // items of all segments
+    int n;                             // segments
+    TcSeg s[kMaxSegs];
     const uint8_t *f1;                 // DFT-128 tiles [8 K-steps][4 comps][4 KB]
     const uint8_t *f2;                 // DFT-N2 tiles [K-steps][4 comps][NP rows x 16 k]
     const float2 *tw;                  // e^{-2 pi i e / (128 N2)}, e < 128 N2
     int *status;                       // set to 1 on a barrier time-out (host-mapped)
 };
+
+__device__ __forceinline__ const TcSeg &seg_of(const TcFftArgs &a, int64_t item) {
+    int j = 0;
+    while (j + 1 < a.n && item >= a.s[j + 1].item0) ++j;
+    return a.s[j];
+}
 
 __device__ __forceinline__ void mbar_init(uint64_t *mbar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
@@ -322,8 +336,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
 
     float2 xv[2 * NPAIR];
     auto load_input = [&](int64_t item) {
-        const int64_t pol = item / a.per_pol, loc = item % a.per_pol;
-        const float2 *x = a.in + pol * a.in_pol_stride + loc * a.in_stride;
+        const TcSeg &sg = seg_of(a, item);
+        const int64_t local = item - sg.item0, pol = local / sg.per_pol, loc = local % sg.per_pol;
+        const float2 *x = sg.in + pol * sg.in_pol_stride + loc * sg.in_stride;
 #pragma unroll
         for (int i = 0; i < NPAIR; ++i) {
             const int q = i * 8 + warp;
@@ -338,7 +353,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         for (int i = 0; i < NRING - 1; ++i) issue_copy(i);
     if (blockIdx.x < a.n_items) load_input(blockIdx.x);
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        float2 *y = a.out + (item / a.per_pol) * a.out_pol_stride + (item % a.per_pol) * a.out_stride;
+        const TcSeg &sg = seg_of(a, item);
+        const int64_t local = item - sg.item0;
+        float2 *y = sg.out + (local / sg.per_pol) * sg.out_pol_stride + (local % sg.per_pol) * sg.out_stride;
         // ---- input: scaled below 2^14, split, B[n2][n1] -------------------------
         float m = 0.f;
 #pragma unroll
@@ -573,6 +590,19 @@ cudaError_t launch_tc_fft(const TcFftArgs &args, int ns, cudaStream_t st) {
 
 }  // namespace
 
+// A launch of one segment: n = per_pol items (one pol).
+static TcFftArgs one_seg(const TcSeg &g, const uint8_t *f1, const uint8_t *f2, const float2 *tw, int *status) {
+    TcFftArgs a{};
+    a.n_items = g.per_pol;
+    a.n = 1;
+    a.s[0] = g;
+    a.f1 = f1;
+    a.f2 = f2;
+    a.tw = tw;
+    a.status = status;
+    return a;
+}
+
 static int tc_splits(const sdbe_resampler *h) { return h->cfg.precision == SDBE_PRECISION_TC16 ? 3 : 2; }
 
 // Tables and scratch of the tensor-core path, on first use.
@@ -597,61 +627,97 @@ int tc_prepare(sdbe_resampler *h, cudaStream_t st) {
     return SDBE_OK;
 }
 
-// The FFT chain of sdbe_process in the tensor-core form: per wave, stage A
-// (pairing, TC inverse 16384), stage B (TC forward 18304), the pairings, stage
-// C (TC inverse 16384) and the 2-bit packing; the first batch of a stream sets
-// the thresholds from its FP64 statistics as the FP32 path does.
-int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
-             const PayloadTarget &tgt, cudaStream_t st) {
-    if (n_batches <= 0) return SDBE_OK;
-    if (int rc = tc_prepare(h, st)) return rc;
-    if (*reinterpret_cast<volatile int *>(h->tc_status_host))  // written by an earlier call's kernels
-        return fail(h, SDBE_ERR_CUDA, "a tensor-core transform timed out on its mbarrier wait");
-    const Twiddles &tw = h->tw;
-    const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
-    const uint8_t *f143 = static_cast<const uint8_t *>(h->tc_f143);
-    for (int64_t b = 0; b < n_batches;) {
-        const bool first = !h->thresholds_set;
-        const int64_t nb = first ? 1 : (n_batches - b < h->wave ? n_batches - b : h->wave);
-        const int64_t snaps = nb * kBatchSnaps, chunks = nb * kChunks;
-        size_t slot = 0;
-        if (!first) SDBE_CK(h, timed_begin(h, 0, 2 * snaps, st, &slot));
-        // stage A: Z (bufx) -> time series (ts: complex 16384 per snapshot)
-        k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(spec, spec_pol_stride, b * kBatchSnaps, snaps,
-                                                                      h->tc_bufx, tw.w32768);
-        SDBE_CK(h, cudaGetLastError());
+// One wave of the tensor-core chain over several handles (one stream pair
+// each): per handle the stage-A pairing, then one launch of each transform
+// covering every handle's items (stage A inverse 16384, stage B forward 18304,
+// stage C inverse 16384) with the B->C pairing per handle in between, then per
+// handle the 2-bit packing into its payload.  With `first` each item is its
+// handle's first batch (nb = 1): its FP64 statistics set the thresholds
+// before it is packed, as the FP32 path does.
+int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st) {
+    if (w.empty()) return SDBE_OK;
+    sdbe_resampler *h0 = w[0].h;
+    for (const auto &it : w) {
+        if (int rc = tc_prepare(it.h, st)) return rc;
+        if (*reinterpret_cast<volatile int *>(it.h->tc_status_host))  // written by an earlier call's kernels
+            return fail(it.h, SDBE_ERR_CUDA, "a tensor-core transform timed out on its mbarrier wait");
+    }
+    const Twiddles &tw = h0->tw;
+    const uint8_t *f128 = static_cast<const uint8_t *>(h0->tc_f128);
+    const uint8_t *f143 = static_cast<const uint8_t *>(h0->tc_f143);
+    TcFftArgs A{}, B{}, C{};
+    for (TcFftArgs *x : {&A, &B, &C}) {
+        x->f1 = f128;
+        x->f2 = x == &B ? f143 : f128;
+        x->tw = x == &B ? tw.w18304 : tw.w16384;
+        x->status = h0->tc_status;
+    }
+    int64_t units_a = 0, units_bc = 0;
+    for (const auto &it : w) {
+        sdbe_resampler *h = it.h;
+        const int64_t snaps = it.nb * kBatchSnaps, chunks = it.nb * kChunks;
         float2 *ts = reinterpret_cast<float2 *>(h->ts);
-        const TcFftArgs A{h->tc_bufx, kMA, snaps * kMA, ts, kMA, h->ts_pol_stride / 2,
-                          snaps, 2 * snaps, f128, f128, tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(A, tc_splits(h), st)));
-        if (!first) {
-            SDBE_CK(h, timed_end(h, slot, st));
-            SDBE_CK(h, timed_begin(h, 1, 2 * chunks, st, &slot));
-        }
-        // stage B: chunks of 18304 complex -> Z (bufy)
-        const TcFftArgs B{ts, kMB, h->ts_pol_stride / 2, h->tc_bufy, kMB, chunks * kMB,
-                          chunks, 2 * chunks, f128, f143, tw.w18304, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<143, false>(B, tc_splits(h), st)));
-        // pairings: bufy -> Z' (bufx)
-        k_tc_pair_bc<<<static_cast<unsigned>(2 * chunks), 256, 0, st>>>(h->tc_bufy, h->tc_bufx, h->skip, tw.w32768,
-                                                                        tw.w36608);
-        SDBE_CK(h, cudaGetLastError());
-        // stage C: Z' -> floats (bufy, 32768 per chunk)
-        const TcFftArgs C{h->tc_bufx, kMA, chunks * kMA, h->tc_bufy, kMA, chunks * kMA,
-                          chunks, 2 * chunks, f128, f128, tw.w16384, h->tc_status};
-        SDBE_CK(h, (launch_tc_fft<128, true>(C, tc_splits(h), st)));
+        A.s[A.n++] = TcSeg{h->tc_bufx, kMA, snaps * kMA, ts, kMA, h->ts_pol_stride / 2, snaps, A.n_items};
+        A.n_items += 2 * snaps;
+        B.s[B.n++] = TcSeg{ts, kMB, h->ts_pol_stride / 2, h->tc_bufy, kMB, chunks * kMB, chunks, B.n_items};
+        B.n_items += 2 * chunks;
+        C.s[C.n++] = TcSeg{h->tc_bufx, kMA, chunks * kMA, h->tc_bufy, kMA, chunks * kMA, chunks, C.n_items};
+        C.n_items += 2 * chunks;
+        units_a += 2 * snaps;
+        units_bc += 2 * chunks;
+    }
+    const int ns = tc_splits(h0);
+    size_t slot = 0;
+    if (!first) SDBE_CK(h0, timed_begin(h0, 0, units_a, st, &slot));
+    for (const auto &it : w) {  // stage A pairing: packed spectra -> Z (bufx)
+        const int64_t snaps = it.nb * kBatchSnaps;
+        k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(it.spec, it.spec_pol_stride,
+                                                                      it.b0 * kBatchSnaps, snaps, it.h->tc_bufx,
+                                                                      tw.w32768);
+        SDBE_CK(it.h, cudaGetLastError());
+    }
+    SDBE_CK(h0, (launch_tc_fft<128, true>(A, ns, st)));  // -> time series (ts)
+    if (!first) {
+        SDBE_CK(h0, timed_end(h0, slot, st));
+        SDBE_CK(h0, timed_begin(h0, 1, units_bc, st, &slot));
+    }
+    SDBE_CK(h0, (launch_tc_fft<143, false>(B, ns, st)));  // chunks of 18304 -> Z (bufy)
+    for (const auto &it : w) {  // pairings: bufy -> Z' (bufx)
+        k_tc_pair_bc<<<static_cast<unsigned>(2 * it.nb * kChunks), 256, 0, st>>>(it.h->tc_bufy, it.h->tc_bufx,
+                                                                                it.h->skip, tw.w32768, tw.w36608);
+        SDBE_CK(it.h, cudaGetLastError());
+    }
+    SDBE_CK(h0, (launch_tc_fft<128, true>(C, ns, st)));  // -> floats (bufy, 32768 per chunk)
+    for (const auto &it : w) {
+        sdbe_resampler *h = it.h;
+        const int64_t chunks = it.nb * kChunks;
         const float *yf = reinterpret_cast<const float *>(h->tc_bufy);
         if (first) {
             k_tc_chunk_stats<<<dim3(kChunks, 2), 256, 0, st>>>(yf, chunks * kNC, kChunks, h->partials);
             SDBE_CK(h, cudaGetLastError());
             SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
             h->thresholds_set = true;
+            h->launches += 2;
         }
-        SDBE_CK(h, launch_quantize_chunks(yf, chunks * kNC, chunks, h->thr, tgt.base, tgt.pol_stride, tgt.pkt_stride,
-                                          tgt.payload_off, b * kChunks, st));
-        if (!first) SDBE_CK(h, timed_end(h, slot, st));
-        h->stream_batch = (first ? 0 : h->stream_batch) + nb;
-        h->launches += first ? 8 : 6;
+        const PayloadTarget &t = it.tgt;
+        SDBE_CK(h, launch_quantize_chunks(yf, chunks * kNC, chunks, h->thr, t.base, t.pol_stride, t.pkt_stride,
+                                          t.payload_off, it.b0 * kChunks, st));
+        h->stream_batch = (first ? 0 : h->stream_batch) + it.nb;
+        h->launches += 3;  // pairing A, pairing BC, packing
+    }
+    if (!first) SDBE_CK(h0, timed_end(h0, slot, st));
+    h0->launches += 3;  // the three transforms
+    return SDBE_OK;
+}
+
+// The FFT chain of sdbe_process in the tensor-core form: the first batch of a
+// stream alone (it sets the thresholds), then waves of up to `wave` batches.
+int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
+             const PayloadTarget &tgt, cudaStream_t st) {
+    for (int64_t b = 0; b < n_batches;) {
+        const bool first = !h->thresholds_set;
+        const int64_t nb = first ? 1 : (n_batches - b < h->wave ? n_batches - b : h->wave);
+        if (int rc = tc_wave_multi({TcWaveItem{h, spec, spec_pol_stride, b, nb, tgt}}, first, st)) return rc;
         b += nb;
     }
     return SDBE_OK;
@@ -671,8 +737,8 @@ int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float
         const int64_t n = n_snaps - s0 < cap ? n_snaps - s0 : cap;
         k_tc_prep_a<<<static_cast<unsigned>(n), 256, 0, st>>>(spec, 0, s0, n, h->tc_bufx, h->tw.w32768);
         SDBE_CK(h, cudaGetLastError());
-        const TcFftArgs A{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + s0 * kNA), kMA, 0,
-                          n, n, f128, f128, h->tw.w16384, h->tc_status};
+        const TcFftArgs A = one_seg(TcSeg{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + s0 * kNA), kMA, 0, n, 0},
+                                    f128, f128, h->tw.w16384, h->tc_status);
         SDBE_CK(h, (launch_tc_fft<128, true>(A, tc_splits(h), st)));
     }
     return SDBE_OK;
@@ -688,14 +754,15 @@ int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, flo
     const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kChunks;
     for (int64_t c0 = 0; c0 < n_chunks; c0 += cap) {
         const int64_t n = n_chunks - c0 < cap ? n_chunks - c0 : cap;
-        const TcFftArgs B{reinterpret_cast<const float2 *>(in + c0 * kNB), kMB, 0, h->tc_bufy, kMB, 0,
-                          n, n, f128, f143, h->tw.w18304, h->tc_status};
+        const TcFftArgs B = one_seg(TcSeg{reinterpret_cast<const float2 *>(in + c0 * kNB), kMB, 0, h->tc_bufy, kMB, 0,
+                                          n, 0},
+                                    f128, f143, h->tw.w18304, h->tc_status);
         SDBE_CK(h, (launch_tc_fft<143, false>(B, tc_splits(h), st)));
         k_tc_pair_bc<<<static_cast<unsigned>(n), 256, 0, st>>>(h->tc_bufy, h->tc_bufx, h->skip, h->tw.w32768,
                                                                h->tw.w36608);
         SDBE_CK(h, cudaGetLastError());
-        const TcFftArgs C{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + c0 * kNC), kMA, 0,
-                          n, n, f128, f128, h->tw.w16384, h->tc_status};
+        const TcFftArgs C = one_seg(TcSeg{h->tc_bufx, kMA, 0, reinterpret_cast<float2 *>(out + c0 * kNC), kMA, 0, n, 0},
+                                    f128, f128, h->tw.w16384, h->tc_status);
         SDBE_CK(h, (launch_tc_fft<128, true>(C, tc_splits(h), st)));
     }
     return SDBE_OK;

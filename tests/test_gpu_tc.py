@@ -96,7 +96,52 @@ def test_tc_config_errors(S):
     p = S.generate(spec, n_frames=1)
     from sdbe_gb300 import process_multi
 
-    with Resampler(max_frames=2, precision=N.PRECISION_TC16) as rs:
+    with Resampler(max_frames=2, precision=N.PRECISION_TC16) as a, Resampler(max_frames=2) as b:
         with pytest.raises(N.SdbeError) as e:
-            process_multi([rs], [(p, 1, spec.b_start, None)])
+            process_multi([a, b], [(p, 1, spec.b_start, None), (p, 1, spec.b_start, None)])
         assert e.value.code == N.ERR_ARG
+
+
+def _rebase(p, b_from, b_to):
+    """The same packets with B-counters shifted from b_from to b_to."""
+    q = p.copy()
+    w = q.view("<u4").reshape(q.shape[0], -1)
+    b = ((w[:, 4].astype(np.int64) << 8) | (w[:, 5].astype(np.int64) >> 24)) - b_from + b_to
+    w[:, 4] = (b >> 8).astype(np.uint32)
+    w[:, 5] = (w[:, 5] & np.uint32(0x00FFFFFF)) | ((b & 0xFF).astype(np.uint32) << 24)
+    return q
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_tc_multi_equals_one_by_one(S, fast):
+    """sdbe_process_multi over three tensor-core handles (uneven lengths,
+    trims 150 / 0 / 240 MHz, waves 4 / 8 / 16) equals sdbe_process one handle
+    at a time, bit for bit, over two calls: first batches, then carried
+    snapshots with the thresholds set."""
+    from sdbe_gb300 import Resampler, process_multi
+    from sdbe_gb300 import _native as N
+
+    prec = N.PRECISION_TC16_FAST if fast else N.PRECISION_TC16
+    cfg = [dict(trim_mhz=150, wave_batches=4), dict(trim_mhz=0, wave_batches=8), dict(trim_mhz=240, wave_batches=16)]
+    frames = [5, 2, 9]
+    st = []
+    for f, seed in zip(frames, [0, 1, 2]):
+        spec = S.config1(stream=seed)
+        spec.b_start = 1_000_000 + 5000 * seed
+        st.append((spec, S.generate(spec, frame_offset=0, n_frames=f)))
+    ms = [Resampler(max_frames=10, precision=prec, **c) for c in cfg]
+    ss = [Resampler(max_frames=10, precision=prec, **c) for c in cfg]
+    try:
+        for call in range(2):
+            items = [(p if call == 0 else _rebase(p, spec.b_start, spec.b_start + f), f, spec.b_start + call * f, None)
+                     for (spec, p), f in zip(st, frames)]
+            got, res = process_multi(ms, items, want_results=True)
+            for i, (r, it) in enumerate(zip(ss, items)):
+                want, wres = r.process(it[0], it[1], it[2])
+                assert np.array_equal(got[i], want), (call, i)
+                assert res[i] == wres, (call, i)
+        for a, b in zip(ms, ss):
+            assert a.thresholds == b.thresholds
+    finally:
+        for r in ms + ss:
+            r.close()
