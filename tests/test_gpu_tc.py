@@ -145,3 +145,28 @@ def test_tc_multi_equals_one_by_one(S, fast):
     finally:
         for r in ms + ss:
             r.close()
+
+
+def test_tc_aligned_and_mar2015_match_fp32(S):
+    """Time-aligned output and the Mar-2015 channel map run the tensor-core
+    chain too: headers equal to the FP32 path's, payload codes >= 99.9% equal."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    spec = S.config1()
+    p = S.generate(spec, frame_offset=0, n_frames=4)
+    for kw in (dict(), dict(channel_map=N.MAP_MAR2015)):
+        outs = []
+        for prec in (N.PRECISION_FP32, N.PRECISION_TC16):
+            with Resampler(trim_mhz=150, max_frames=4, precision=prec, **kw) as rs:
+                if not kw:
+                    rs.align_start(1_234_567, 285_800_000, ref_epoch=30)
+                    o, _ = rs.process(p, 4, spec.b_start, aligned=True)
+                else:
+                    o, _ = rs.process(p, 4, spec.b_start, framed=True)
+                outs.append(o)
+        f32, tc = outs
+        assert f32.shape == tc.shape and f32.shape[1] > 0, kw
+        assert np.array_equal(f32[:, :, :32], tc[:, :, :32]), kw  # VDIF headers
+        agree = float(np.mean(codes_of(f32[:, :, 32:]) == codes_of(tc[:, :, 32:])))
+        assert agree >= AGREE_MIN, (kw, agree)
