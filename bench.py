@@ -544,8 +544,10 @@ def run_stress(args):
     pool = [[synth.generate(sp, frame_offset=g * G, n_frames=G) for g in range(2)] for sp in specs]
     d_pool = [[torch.from_numpy(p).cuda() for p in row] for row in pool]
     wave = args.wave or 16
+    tc = args.precision != "fp32"
+    prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
     hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=G, wave_batches=wave,
-                    threshold_mode=N.THRESH_WINDOW, threshold_window=64) for _ in specs]
+                    threshold_mode=N.THRESH_WINDOW, threshold_window=64, precision=prec) for _ in specs]
     out_bytes = hs[0].output_bytes(G)
     outs = [torch.empty(out_bytes, dtype=torch.uint8, device="cuda") for _ in hs]
     stream = torch.cuda.Stream()
@@ -615,19 +617,21 @@ def run_stress(args):
     line = {
         "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": 1, "steps": n_passes,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_total / n_passes, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": _DTYPE[args.precision], "data": "synthetic",
         "config": {"workload": "32 streams (16 packet streams x 2 phased sums) x 2048 B-frames in 143-frame "
                                "groups; 1% dropped, 0.5% displaced (<= 64) packets, sigma x4 bursts on 1% of "
-                               "snapshots; windowed thresholds (64 batches); one sdbe_process_multi pass per group",
+                               "snapshots; windowed thresholds (64 batches); one sdbe_process_multi pass per group; "
+                               + _PATH[args.precision] + "-FFT path",
                    "packet_streams": n_streams, "frames_per_stream": n_passes * G, "wave_batches": wave,
                    "packets_accepted_first_pass": int(accepted), "frames_incomplete_first_pass": int(incomplete),
                    "l2": "inputs larger than L2 (4.9 GB of packets per pass)"},
         "x_realtime": value / (REALTIME_GSPS * 2 * n_streams),
         "whole_pipeline_hbm": {"algorithmic_gbs": whole_bytes / (ms_total * 1e-3) / 1e9, "peak": peak,
                                "frac": whole_bytes / (ms_total * 1e-3) / 1e9 / peak},
-        "roofline": {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                     "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes},
+        "roofline": (_tc_roofline(prof, n_passes, 3 if args.precision == "tc16" else 2) if tc else
+                     {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                      "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
+                      "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes}),
         "thresholds_after_run": {"pol0": float(st.threshold[0]), "pol1": float(st.threshold[1])},
         "stage_ms_per_step": {"stage_a": prof.stage_a_ms / n_passes, "stage_bc": prof.stage_bc_ms / n_passes},
         "e2e": {"value": n_passes * samples / e2e_s / 1e9, "unit": "GS/s", "ms_per_step": e2e_s / n_passes * 1e3,
@@ -652,14 +656,12 @@ def main():
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16", "tc16fast"],
-                    help="group512 and streams8: fp32 radix kernels (default) or an FP16 tensor-core form "
+                    help="fp32 radix kernels (default) or an FP16 tensor-core form "
                          "(tc16: data and DFT matrix split hi+lo; tc16fast: DFT matrix split, data FP16)")
     ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
                     help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
                          "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")
     args = ap.parse_args()
-    if args.workload == "stress32" and args.precision != "fp32":
-        ap.error("stress32 uses windowed thresholds, which the tensor-core precisions do not take")
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "streams8":

@@ -75,8 +75,7 @@ extern "C" {
  * accumulation in tensor memory).  TC16 splits the DFT matrix and the data
  * into hi + lo FP16 halves (three products per real product: FP32-like
  * error); TC16_FAST splits only the DFT matrix and rounds the data to FP16
- * (two products).  sdbe_process and the stage entry points only; not with
- * SDBE_THRESH_WINDOW. */
+ * (two products).  All entry points and threshold modes. */
 #define SDBE_PRECISION_TC16 1
 #define SDBE_PRECISION_TC16_FAST 2
 

@@ -407,7 +407,7 @@ int tc_chain_multi(std::vector<CallPlan> &cs) {
         std::vector<int> act;
         for (int i = 0; i < n; ++i) {
             if (b[i] >= cs[i].n_batches) continue;
-            const int64_t nb = std::min<int64_t>(wave, cs[i].n_batches - b[i]);
+            const int64_t nb = wave_len(cs[i].h, wave, cs[i].n_batches - b[i]);
             w.push_back(TcWaveItem{cs[i].h, cs[i].h->spec, cs[i].h->spec_pol_stride, b[i], nb, cs[i].pt});
             act.push_back(i);
         }
@@ -551,8 +551,6 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16 &&
         cfg->precision != SDBE_PRECISION_TC16_FAST)
         return fail(nullptr, SDBE_ERR_ARG, "unknown precision");
-    if (cfg->precision != SDBE_PRECISION_FP32 && cfg->threshold_mode == SDBE_THRESH_WINDOW)
-        return fail(nullptr, SDBE_ERR_ARG, "the tensor-core precisions do not take SDBE_THRESH_WINDOW");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
         cudaGetLastError();

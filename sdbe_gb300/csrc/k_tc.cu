@@ -688,10 +688,12 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
         SDBE_CK(it.h, cudaGetLastError());
     }
     SDBE_CK(h0, (launch_tc_fft<128, true>(C, ns, st)));  // -> floats (bufy, 32768 per chunk)
+    WinUpds U{};
     for (const auto &it : w) {
         sdbe_resampler *h = it.h;
         const int64_t chunks = it.nb * kChunks;
         const float *yf = reinterpret_cast<const float *>(h->tc_bufy);
+        const bool win = h->cfg.threshold_mode == SDBE_THRESH_WINDOW;
         if (first) {
             k_tc_chunk_stats<<<dim3(kChunks, 2), 256, 0, st>>>(yf, chunks * kNC, kChunks, h->partials);
             SDBE_CK(h, cudaGetLastError());
@@ -702,8 +704,20 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
         const PayloadTarget &t = it.tgt;
         SDBE_CK(h, launch_quantize_chunks(yf, chunks * kNC, chunks, h->thr, t.base, t.pol_stride, t.pkt_stride,
                                           t.payload_off, it.b0 * kChunks, st));
-        h->stream_batch = (first ? 0 : h->stream_batch) + it.nb;
         h->launches += 3;  // pairing A, pairing BC, packing
+        if (first) h->stream_batch = 0;
+        if (win && !first) {  // windowed thresholds: this wave's FP64 chunk statistics
+            k_tc_chunk_stats<<<dim3(static_cast<unsigned>(chunks), 2), 256, 0, st>>>(yf, chunks * kNC,
+                                                                                  static_cast<int>(chunks), h->wpart);
+            SDBE_CK(h, cudaGetLastError());
+            h->launches += 1;
+        }
+        // the window ring takes the wave's statistics after it was packed with the old thresholds
+        window_step(h, first ? h->partials : h->wpart, it.nb, true, U);
+    }
+    if (U.n) {
+        SDBE_CK(h0, launch_window_update(U, st));
+        h0->launches += 1;
     }
     if (!first) SDBE_CK(h0, timed_end(h0, slot, st));
     h0->launches += 3;  // the three transforms
@@ -716,7 +730,7 @@ int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, i
              const PayloadTarget &tgt, cudaStream_t st) {
     for (int64_t b = 0; b < n_batches;) {
         const bool first = !h->thresholds_set;
-        const int64_t nb = first ? 1 : (n_batches - b < h->wave ? n_batches - b : h->wave);
+        const int64_t nb = first ? 1 : wave_len(h, h->wave, n_batches - b);
         if (int rc = tc_wave_multi({TcWaveItem{h, spec, spec_pol_stride, b, nb, tgt}}, first, st)) return rc;
         b += nb;
     }

@@ -87,9 +87,6 @@ def test_tc_config_errors(S):
     from sdbe_gb300 import _native as N
 
     with pytest.raises(N.SdbeError) as e:
-        Resampler(threshold_mode=N.THRESH_WINDOW, precision=N.PRECISION_TC16)
-    assert e.value.code == N.ERR_ARG
-    with pytest.raises(N.SdbeError) as e:
         Resampler(precision=7)
     assert e.value.code == N.ERR_ARG
     spec = S.config1()

@@ -2,8 +2,9 @@
 on a stream whose noise power steps up: the first-batch thresholds of the
 reference stay where the first batch put them, the windowed ones follow.
 
-Bar: >= 99.9% 2-bit code agreement with the oracle (FP32 path), thresholds
-within 1e-5 relative, outputs independent of the wave size."""
+Bar: >= 99.9% 2-bit code agreement with the oracle, thresholds within 1e-5
+relative (FP32 path; 3e-5 for the tensor-core paths), outputs independent of
+the wave size."""
 import os
 
 import numpy as np
@@ -71,3 +72,29 @@ def test_window_thresholds_match_oracle_and_adapt(step_stream):
         f_ref = _outer(codes_of(out_r[pol, last]))
         assert abs(f_win - f_first) < 0.04, (f_first, f_win)
         assert f_ref > f_win + 0.1, (f_ref, f_win)
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_window_thresholds_tensor_core_paths(step_stream, fast):
+    """The tensor-core chains with windowed thresholds, against the oracle."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    b0, p = step_stream
+    W = 16
+    prec = N.PRECISION_TC16_FAST if fast else N.PRECISION_TC16
+    kw = dict(max_frames=40, threshold_mode=N.THRESH_WINDOW, threshold_window=W, precision=prec)
+    with Resampler(wave_batches=4, **kw) as a, Resampler(wave_batches=16, **kw) as b:
+        out_a, res = a.process(p, 40, b0)
+        out_b, _ = b.process(p, 40, b0)
+        (th0, th1), _, _ = a.thresholds
+    assert res.n_batches == 35
+    assert np.array_equal(out_a, out_b)
+    st = O.StreamState()
+    ref = O.process_group(p, b0, 40, 150, state=st, precision="f32", workers=os.cpu_count() or 1,
+                          threshold_window=W)
+    for pol in range(2):
+        agree = float(np.mean(codes_of(out_a[pol]) == codes_of(ref[pol])))
+        assert agree >= 0.999, (pol, agree)
+    assert abs(th0 - st.threshold[0]) <= 3e-5 * st.threshold[0]
+    assert abs(th1 - st.threshold[1]) <= 3e-5 * st.threshold[1]
