@@ -185,6 +185,9 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
 // sdbe_swarm_c2r / sdbe_resample_chunks of a SDBE_PRECISION_TC16 handle (one pol).
 int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st);
 int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, cudaStream_t st);
+// C2R 32768 of complex spectra [n][spec_stride] in the tensor-core form (z: n x 16384 complex scratch).
+int tc_c2r_spectra(sdbe_resampler *h, const float2 *spec, int64_t spec_stride, int64_t n, float2 *z, float *out,
+                   cudaStream_t st);
 
 // First-batch threshold path (if thresholds are unset) and the FFT waves over
 // n_batches 143-snapshot batches of packed spectra (spec + pol*spec_pol_stride,

@@ -180,7 +180,18 @@ extern "C" int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t
     double *scr = nullptr;
     SDBE_CK(h, cudaMallocAsync(reinterpret_cast<void **>(&y), static_cast<size_t>(nblock) * kNA * sizeof(float), st));
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&scr), static_cast<size_t>(nblock) * ntap * kNA * sizeof(double), st);
-    if (e == cudaSuccess) e = launch_r2dbe_c2r(spec_c64, kMA + 1, nblock, 0, y, h->tw, st);
+    if (e == cudaSuccess && h->cfg.precision != SDBE_PRECISION_FP32) {
+        // the pseudo time stream on the tensor cores; scr holds the paired spectra
+        // first (n x 16384 complex fits its n x ntap x 32768 doubles)
+        if (int rc = tc_c2r_spectra(h, static_cast<const float2 *>(spec_c64), kMA + 1, nblock,
+                                    reinterpret_cast<float2 *>(scr), y, st)) {
+            cudaFreeAsync(scr, st);
+            cudaFreeAsync(y, st);
+            return rc;
+        }
+    } else if (e == cudaSuccess) {
+        e = launch_r2dbe_c2r(spec_c64, kMA + 1, nblock, 0, y, h->tw, st);
+    }
     if (e == cudaSuccess) {
         switch (ntap) {
             case 2: e = launch_solve<2>(y, nblock, h->ipfb_tab, scr, out, st); break;

@@ -515,6 +515,27 @@ __global__ void k_tc_pair_bc(const float2 *__restrict__ zb, float2 *__restrict__
     }
 }
 
+// C2R pairing of complex spectra X[0..16384] (row stride spec_stride): Z[j],
+// Z[16384 - j] from X[j], X[16384 - j], the imaginary parts of X[0] and
+// X[16384] dropped (as k_r2dbe_c2r with skip 0).
+__global__ void k_tc_pair_c2r(const float2 *__restrict__ spec, int64_t spec_stride, float2 *__restrict__ z,
+                              const float2 *__restrict__ w32768) {
+    const int64_t item = blockIdx.x;
+    const float2 *sp = spec + item * spec_stride;
+    float2 *zo = z + item * kMA;
+    for (int j = threadIdx.x; j <= kMA / 2; j += blockDim.x) {
+        float2 y = sp[j], ym = sp[kMA - j];
+        if (j == 0) {
+            y.y = 0.f;
+            ym.y = 0.f;
+        }
+        float2 zk, zmk;
+        c2r_pair(y, ym, conjf2(__ldg(w32768 + j)), zk, zmk);
+        zo[j] = zk;
+        if (j != 0 && j != kMA / 2) zo[kMA - j] = zmk;
+    }
+}
+
 // Per-chunk (n, mean, M2) of the first batch's floats in FP64 (as k_resample<1>).
 __global__ void k_tc_chunk_stats(const float *__restrict__ y, int64_t y_pol_stride, int n_chunks,
                                  double *__restrict__ partials) {
@@ -779,6 +800,28 @@ int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, flo
                                     f128, f128, h->tw.w16384, h->tc_status);
         SDBE_CK(h, (launch_tc_fft<128, true>(C, tc_splits(h), st)));
     }
+    return SDBE_OK;
+}
+
+// C2R 32768 of n complex spectra [n][spec_stride >= 16385] into out [n][32768]
+// floats in the tensor-core form (the inverse PFB's transform); z is caller
+// scratch of n x 16384 complex values.
+int tc_c2r_spectra(sdbe_resampler *h, const float2 *spec, int64_t spec_stride, int64_t n, float2 *z, float *out,
+                   cudaStream_t st) {
+    if (n <= 0) return SDBE_OK;
+    if (reinterpret_cast<uintptr_t>(out) & 15u)
+        return fail(h, SDBE_ERR_ARG, "the tensor-core precisions need a 16-byte aligned output buffer");
+    if (int rc = tc_prepare(h, st)) return rc;
+    const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
+    for (int64_t i0 = 0; i0 < n; i0 += (int64_t(1) << 30)) {  // grid limit of the pairing kernel
+        const int64_t m = n - i0 < (int64_t(1) << 30) ? n - i0 : (int64_t(1) << 30);
+        k_tc_pair_c2r<<<static_cast<unsigned>(m), 256, 0, st>>>(spec + i0 * spec_stride, spec_stride, z + i0 * kMA,
+                                                               h->tw.w32768);
+        SDBE_CK(h, cudaGetLastError());
+    }
+    const TcFftArgs A =
+        one_seg(TcSeg{z, kMA, 0, reinterpret_cast<float2 *>(out), kMA, 0, n, 0}, f128, f128, h->tw.w16384, h->tc_status);
+    SDBE_CK(h, (launch_tc_fft<128, true>(A, tc_splits(h), st)));
     return SDBE_OK;
 }
 

@@ -48,3 +48,26 @@ def test_inverse_pfb_matches_oracle(rs, ntap, nb):
     if ntap == 4 and nb == 48:
         rho_in = np.corrcoef(got[8:-8].ravel(), xb[8:-8].ravel())[0, 1]
         assert rho_in > 0.985, rho_in  # 48 blocks; the 0.5% loss figure needs ~400 (CPU test)
+
+
+# The pseudo time stream on the tensor cores: its relative error (1.8e-6 for
+# SDBE_PRECISION_TC16, 2.9e-4 for SDBE_PRECISION_TC16_FAST per transform)
+# is amplified by the inverse as above.  Measured at 48 blocks: 1.1e-5 and
+# 9.2e-3.
+TOL_TC = {"tc16": 4e-5, "tc16fast": 3e-2}
+
+
+@pytest.mark.parametrize("path", ["tc16", "tc16fast"])
+def test_inverse_pfb_tensor_core_transform(path):
+    from sdbe_gb300 import Resampler, pfb
+    from sdbe_gb300 import _native as N
+
+    prec = N.PRECISION_TC16 if path == "tc16" else N.PRECISION_TC16_FAST
+    ntap, nb = 4, 48
+    xb, S = _case(ntap, nb, 10 + ntap + nb)
+    with Resampler(max_frames=1, precision=prec) as r:
+        got = pfb.inverse_pfb(r, S.astype(np.complex64), ntap=ntap).cpu().numpy().astype(np.float64)
+    ref = O.inverse_pfb(S, ntap)
+    err = np.sqrt(np.mean((got - ref) ** 2) / np.mean(ref ** 2))
+    print(f"{path}: inverse PFB relative RMS {err:.3e}")
+    assert err < TOL_TC[path], err
