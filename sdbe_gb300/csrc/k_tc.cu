@@ -155,6 +155,19 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
         : "memory");
 }
 
+// A bulk copy global -> shared that reports its bytes to mbar (whose expected
+// bytes were set by one arrive.expect_tx for several copies).
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+
 // The barrier completes when every tcgen05 operation this thread issued so far has.
 __device__ __forceinline__ void mma_commit(uint64_t *mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
@@ -181,7 +194,7 @@ __device__ __forceinline__ uint32_t hi2(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-template <int N2>
+template <int N2, int NS>
 struct TcGeo {
     static constexpr int NP = (N2 + 15) / 16 * 16;  // N of both GEMMs, step-3 K
     static constexpr int KS3 = NP / 16;             // step-3 K-steps (step 1 has 8)
@@ -189,11 +202,16 @@ struct TcGeo {
     static constexpr int RG = NP / 8;               // 8-row groups of the step-1 B operand
     static constexpr int NPAIR = NP * 64 / kTcThreads;  // input element pairs per thread
     static constexpr uint32_t COMP = NP * 128 * 2;  // bytes of one B-operand component
-    static constexpr int NRING = 4;                 // DFT-tile buffers
+    // 16384 points with FP16 data (NS = 2): the data operand takes two
+    // components (64 KB), so all eight DFT-128 stages stay resident (128 KB),
+    // loaded once per CTA and read by both GEMMs
+    static constexpr bool RES = N2 == 128 && NS == 2;
+    static constexpr int NCOMP = NS == 3 ? 4 : 2;   // data components kept: re/im x hi/lo, or hi only
+    static constexpr int NRING = RES ? 8 : 4;       // DFT-tile buffers
     static constexpr uint32_t STAGE1 = 4 * kTile;   // bytes of a step-1 stage: DFT-128 [128 rows][16 k] x 4
     static constexpr uint32_t STAGE3 = 4 * NP * 32; // bytes of a step-3 stage: DFT-N2 [NP rows][16 k] x 4
     static constexpr uint32_t STAGE = STAGE3 > STAGE1 ? STAGE3 : STAGE1;
-    static constexpr size_t SMEM = 4 * static_cast<size_t>(COMP) + NRING * static_cast<size_t>(STAGE) +
+    static constexpr size_t SMEM = NCOMP * static_cast<size_t>(COMP) + NRING * static_cast<size_t>(STAGE) +
                                    (N2 + 128) * sizeof(float2);
 };
 
@@ -215,13 +233,16 @@ struct TcGeo {
 // a row's four words by its row group for the same reason.
 template <int N2, bool INV, int NS>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant__ TcFftArgs a) {
-    using G = TcGeo<N2>;
+    using G = TcGeo<N2, NS>;
+    constexpr bool RES = G::RES;
+    // physical slot of data component c (0 re hi, 1 re lo, 2 im hi, 3 im lo)
+    auto cslot = [](int c) { return NS == 3 ? c : c >> 1; };
     constexpr int NP = G::NP, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
     constexpr int NRING = G::NRING;
     constexpr uint32_t COMP = G::COMP, STAGE = G::STAGE, STAGE1 = G::STAGE1, STAGE3 = G::STAGE3;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *bop = smem;                                               // [4 comps][COMP]
-    uint8_t *aop = smem + 4 * COMP;                                    // [NRING][STAGE]
+    uint8_t *bop = smem;                                               // [NCOMP][COMP]
+    uint8_t *aop = smem + G::NCOMP * COMP;                             // [NRING][STAGE]
     float2 *twh = reinterpret_cast<float2 *>(aop + NRING * STAGE);    // w^(128 i), i < N2
     float2 *twl = twh + N2;                                            // w^j, j < 128
     __shared__ __align__(8) uint64_t full[NRING], empty[NRING], done;
@@ -260,7 +281,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
     uint32_t g = 0;                      // global stage index (items x SPI)
     bool err = false;                    // a wait of thread 0 timed out: issue nothing more
     uint32_t pend = 0;                   // buffers with a bulk copy in flight
-    uint32_t pend_g[NRING] = {0, 0, 0, 0};  // the stage each of those copies is for
+    uint32_t pend_g[NRING] = {};            // the stage each of those copies is for
     uint32_t done_n = 0;                 // completions of `done` waited for (all threads)
 
     auto issue_copy = [&](uint32_t gg) {
@@ -279,8 +300,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         const uint32_t dr = tb, di = tb + 256;
         const uint32_t idesc = instr_desc(128, NP, false), idesc_m = instr_desc(128, NP, true);
         for (int s = 0; s < nst; ++s, ++g) {
-            const int b = g % NRING;
-            if (!err) {
+            const int b = RES ? s : g % NRING;  // resident tiles: K-step s in buffer s
+            if (!RES && !err) {
                 if (mbar_wait(&full[b], (g / NRING) & 1u))
                     pend &= ~(1u << b);
                 else
@@ -298,16 +319,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                     if (!step3) {
                         const uint64_t fr = smem_desc(smem_u32(ab + (0 + fh) * kTile), 128, 256);
                         const uint64_t fi = smem_desc(smem_u32(ab + (2 + fh) * kTile), 128, 256);
-                        const uint64_t xr = smem_desc(smem_u32(bop + (0 + xh) * COMP) + s * 256, 128, 16 * 128);
-                        const uint64_t xi = smem_desc(smem_u32(bop + (2 + xh) * COMP) + s * 256, 128, 16 * 128);
+                        const uint64_t xr = smem_desc(smem_u32(bop + cslot(0 + xh) * COMP) + s * 256, 128, 16 * 128);
+                        const uint64_t xi = smem_desc(smem_u32(bop + cslot(2 + xh) * COMP) + s * 256, 128, 16 * 128);
                         // Dr += Fr Xr -/+ Fi Xi ; Di += +/-Fi Xr + Fr Xi
                         mma_f16(dr, fr, xr, idesc, !first);
                         mma_f16(dr, fi, xi, INV ? idesc : idesc_m, true);
                         mma_f16(di, fi, xr, INV ? idesc_m : idesc, !first);
                         mma_f16(di, fr, xi, idesc, true);
                     } else {
-                        const uint64_t xr = smem_desc(smem_u32(bop + (0 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
-                        const uint64_t xi = smem_desc(smem_u32(bop + (2 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
+                        const uint64_t xr = smem_desc(smem_u32(bop + cslot(0 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
+                        const uint64_t xi = smem_desc(smem_u32(bop + cslot(2 + xh) * COMP) + s * 256, 128, (NP / 8) * 128);
                         const uint64_t fr = smem_desc(smem_u32(ab + (0 + fh) * (NP * 32)), 128, 256);
                         const uint64_t fi = smem_desc(smem_u32(ab + (2 + fh) * (NP * 32)), 128, 256);
                         mma_f16(dr, xr, fr, idesc, !first);
@@ -317,9 +338,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                     }
                 }
             }
-            mma_commit(&empty[b]);
+            if (!RES) mma_commit(&empty[b]);
             if (s == nst - 1) mma_commit(&done);
-            if (!err) {
+            if (!RES && !err) {
                 // the buffer of K-step g-1 takes K-step g+3 once those MMAs are done
                 if (g >= 1 && !mbar_wait(&empty[(g - 1) % NRING], ((g - 1) / NRING) & 1u)) err = true;
                 if (!err) issue_copy(g + NRING - 1);
@@ -349,8 +370,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         }
     };
 
-    if (tid == 0)
-        for (int i = 0; i < NRING - 1; ++i) issue_copy(i);
+    if (tid == 0) {
+        if constexpr (RES) {  // all eight K-step stages once; wait before the first GEMM
+            arrive_expect_tx(&full[0], 8 * STAGE);
+            for (int k = 0; k < 8; ++k) bulk_copy(aop + k * STAGE, a.f1 + k * STAGE, STAGE, &full[0]);
+            pend = 1u;
+            pend_g[0] = 0;
+            if (blockIdx.x < a.n_items) {
+                if (mbar_wait(&full[0], 0))
+                    pend = 0;
+                else
+                    err = true;
+            }
+        } else {
+            for (int i = 0; i < NRING - 1; ++i) issue_copy(i);
+        }
+    }
     if (blockIdx.x < a.n_items) load_input(blockIdx.x);
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const TcSeg &sg = seg_of(a, item);
@@ -377,7 +412,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                 *reinterpret_cast<uint32_t *>(bop + 3 * COMP + off) = il;
             } else {
                 *reinterpret_cast<uint32_t *>(bop + off) = hi2(xv[2 * i].x * s1, xv[2 * i + 1].x * s1);
-                *reinterpret_cast<uint32_t *>(bop + 2 * COMP + off) = hi2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1);
+                *reinterpret_cast<uint32_t *>(bop + COMP + off) = hi2(xv[2 * i].y * s1, xv[2 * i + 1].y * s1);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -424,7 +459,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
                     if (NS == 3 || (c & 1) == 0)  // NS = 2 keeps the data's hi halves only
-                        *reinterpret_cast<uint32_t *>(bop + c * COMP + off) =
+                        *reinterpret_cast<uint32_t *>(bop + cslot(c) * COMP + off) =
                             pick4(w[c][0], w[c][1], w[c][2], w[c][3], j);
             }
         }
@@ -595,10 +630,10 @@ cudaError_t launch_tc_fft_ns(const TcFftArgs &args, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)  // cheap; set each time so that every device gets it
         e = cudaFuncSetAttribute(k_tc_fft<N2, INV, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(TcGeo<N2>::SMEM));
+                                 static_cast<int>(TcGeo<N2, NS>::SMEM));
     if (e != cudaSuccess) return e;
     const unsigned grid = static_cast<unsigned>(args.n_items < sms ? args.n_items : sms);
-    k_tc_fft<N2, INV, NS><<<grid, kTcThreads, TcGeo<N2>::SMEM, st>>>(args);
+    k_tc_fft<N2, INV, NS><<<grid, kTcThreads, TcGeo<N2, NS>::SMEM, st>>>(args);
     return cudaGetLastError();
 }
 
