@@ -78,6 +78,27 @@ __device__ __forceinline__ void tmem_ld8x2(uint32_t ta, uint32_t tb, float *va, 
     }
 }
 
+// Eight TMEM columns of this thread's lane into r, no wait (see tmem_wait_tied).
+__device__ __forceinline__ void tmem_ld8_nw(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
+// Waits for this thread's TMEM loads; then ties each register of a[0..N) and
+// b[0..N) to an (empty) asm after the wait, so that no use moves above it.
+template <int N>
+__device__ __forceinline__ void tmem_wait_tied(uint32_t *a, uint32_t *b) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < N; i += 8) {
+        asm volatile("" : "+r"(a[i]), "+r"(a[i + 1]), "+r"(a[i + 2]), "+r"(a[i + 3]), "+r"(a[i + 4]), "+r"(a[i + 5]),
+                     "+r"(a[i + 6]), "+r"(a[i + 7]));
+        asm volatile("" : "+r"(b[i]), "+r"(b[i + 1]), "+r"(b[i + 2]), "+r"(b[i + 3]), "+r"(b[i + 4]), "+r"(b[i + 5]),
+                     "+r"(b[i + 6]), "+r"(b[i + 7]));
+    }
+}
+
 // Bounded wait for the commit of phase `phase`; false on time-out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
     uint32_t done = 0;
@@ -422,20 +443,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         if (tid == 0) gemm(8, false);
         wait_done();
         // ---- step 2: twiddles, scale, split into B[k1][n2] -----------------------
+        // The scaled input is below 2^14 per component, so |D| < 128 sqrt(2) 2^14
+        // < 2^21.5 and the twiddles keep magnitudes: the fixed scale 2^-8 keeps
+        // every FP16 half below 2^14 without a pass for the maximum.  TMEM is
+        // read GC chunks of 8 columns per wait.
         const int k1 = quarter * 32 + lane;
-        constexpr int HALF = NP / 2;
-        float m2 = 0.f;
-        for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
-            float dr[8], di[8];
-            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) m2 = fmaxf(m2, fmaxf(fabsf(dr[j]), fabsf(di[j])));
-        }
-        const float s2 = pow2_scale(block_max(m2, red));
+        constexpr int HALF = NP / 2, NCH = HALF / 8, GC = G::RES ? 4 : 1;  // one chunk where registers are short
+        static_assert(NCH % GC == 0, "chunk groups");
+        constexpr float s2 = 1.f / 256.f;
         const int rot = lane >> 3;  // = (k1 >> 3) & 3
-        for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
-            float dr[8], di[8];
-            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
+#pragma unroll 1
+        for (int cg = 0; cg < NCH; cg += GC) {
+        uint32_t ur[8 * GC], ui[8 * GC];
+#pragma unroll
+        for (int q = 0; q < GC; ++q) {
+            tmem_ld8_nw(lane_base + half * HALF + 8 * (cg + q), ur + 8 * q);
+            tmem_ld8_nw(lane_base + 256 + half * HALF + 8 * (cg + q), ui + 8 * q);
+        }
+        tmem_wait_tied<8 * GC>(ur, ui);
+#pragma unroll
+        for (int q = 0; q < GC; ++q) {
+            const int c0 = half * HALF + 8 * (cg + q);
             float2 v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -443,7 +471,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                 v[j] = make_float2(0.f, 0.f);
                 if (n2 < N2) {
                     const int e = n2 * k1;  // < 128 N2
-                    v[j] = cmul(make_float2(dr[j], di[j]), cmul(twh[e >> 7], twl[e & 127]));
+                    v[j] = cmul(make_float2(__uint_as_float(ur[8 * q + j]), __uint_as_float(ui[8 * q + j])),
+                                cmul(twh[e >> 7], twl[e & 127]));
                 }
             }
             uint32_t w[4][4];  // [component][word: columns 2j, 2j+1]
@@ -463,15 +492,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
                             pick4(w[c][0], w[c][1], w[c][2], w[c][3], j);
             }
         }
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         // ---- step 3: D[k1][k2] -----------------------------------------------------
-        const bool more = item + gridDim.x < a.n_items;
+        // the next item's input (the current one again after the last, so that the
+        // registers are always reloaded and stay free from the input stage to here)
+        const int64_t next = item + gridDim.x < a.n_items ? item + gridDim.x : item;
         if (tid == 0) gemm(KS3, true);
-        if (more && warp != 0) load_input(item + gridDim.x);  // lands during the GEMM
+        if (warp != 0) load_input(next);  // lands during the GEMM
         wait_done();
-        if (more && warp == 0) load_input(item + gridDim.x);  // not beside the issuing lane
+        if (warp == 0) load_input(next);  // not beside the issuing lane
         // ---- output: y[k1 + 128 k2], a warp's stores 32 consecutive values ----------
         const float inv = (1.f / s1) * (1.f / s2);  // powers of two: exact
         for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
