@@ -149,6 +149,50 @@ def _tc_roofline(prof, steps, splits):
             "tensor_tflops": {"span_a": ta, "span_bc": tbc}}
 
 
+def cufft_library_baseline(n_batches, samples_per_step, skip):
+    """The reference's GPU transforms through the library it calls (cuFFT, via
+    torch.fft) on one 16-batch wave of both phased sums, scaled to the step:
+    int8 -> complex64 with a zero Nyquist bin (beng_int8_to_cufftComplex), C2R
+    32768 x 143 per batch, R2C 36608 x 128, C2R 32768 x 128 from bin `skip`,
+    then a 2-bit quantize and 16-per-word pack in torch elementwise ops.  The
+    packet unpack is left out.  A comparison for the hand-written kernels,
+    not the reference arm."""
+    import torch
+
+    n_snap, n_chunk = 2 * 16 * 143, 2 * 16 * 128
+    g = torch.Generator(device="cuda").manual_seed(5)
+    beng = torch.randint(-2, 2, (n_snap, 16384, 2), dtype=torch.int8, device="cuda", generator=g)
+    shifts = (2 * torch.arange(16, device="cuda", dtype=torch.int32))
+
+    def wave():
+        X = torch.zeros(n_snap, 16385, dtype=torch.complex64, device="cuda")
+        X[:, :16384] = torch.complex(beng[..., 1].float(), beng[..., 0].float())
+        ts = torch.fft.irfft(X, n=32768)
+        Y = torch.fft.rfft(ts.reshape(-1)[: n_chunk * 36608].reshape(n_chunk, 36608))
+        y = torch.fft.irfft(Y[:, skip:skip + 16385], n=32768)
+        th = y.std()
+        codes = ((y >= 0).int() * 2 + (y.abs() >= th).int() * (2 * (y >= 0).int() - 1)
+                 + (y < 0).int()).reshape(-1, 16)
+        return (codes << shifts).sum(dim=1, dtype=torch.int32)
+
+    for _ in range(3):
+        wave()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 5
+    for _ in range(reps):
+        wave()
+    e1.record()
+    torch.cuda.synchronize()
+    wave_ms = e0.elapsed_time(e1) / reps
+    step_ms = wave_ms * n_batches / 16
+    return {"value": samples_per_step / (step_ms * 1e-3) / 1e9, "unit": "GS/s", "ms_per_step": step_ms,
+            "ms_per_16_batch_wave": wave_ms,
+            "what": "cuFFT (torch.fft) C2R 32768 + R2C 36608 + C2R 32768 per batch as the reference plans them, "
+                    "with int8->complex conversion and a torch 2-bit quantize/pack; packet unpack not included"}
+
+
 def cpu_baseline(sample_frames=96, workers=None):
     """The oracle's FP32 path (numpy unpack + scipy.fft) on a bounded sample."""
     from oracle import sdbe_oracle as O
@@ -331,6 +375,7 @@ def run_ours(args):
         if tc:
             roofline = _tc_roofline(prof, args.steps, 3 if args.precision == "tc16" else 2)
         cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
+        lib = cufft_library_baseline(int(n_batches), samples_per_step, rs.skip_chan) if world == 1 else None
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -344,6 +389,7 @@ def run_ours(args):
             "x_realtime": value / (REALTIME_GSPS * 2 * world),
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "gpu_library_baseline": lib,
             "e2e": {"value": e2e_value, "unit": "GS/s", "ms_per_step": float(t.item()),
                     "h2d_bytes_per_step": int(n_pkts * 1056), "d2h_bytes_per_step": int(out_bytes),
                     "api": "Resampler.process(host pinned buffers) -> sdbe_process(SDBE_IN_HOST|SDBE_OUT_HOST|"
