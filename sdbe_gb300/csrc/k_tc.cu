@@ -256,6 +256,11 @@ template <int N2, bool INV, int NS>
 __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant__ TcFftArgs a) {
     using G = TcGeo<N2, NS>;
     constexpr bool RES = G::RES;
+    // 16384 points: step 3 gets its own TMEM columns (Dr at 256, Di at 384;
+    // step 1 at 0 and 128), so that one transform's output is stored while
+    // the next one's step-1 GEMM runs.  18304 points need 288 columns a step.
+    constexpr bool OVL = N2 == 128;
+    constexpr uint32_t DI1 = OVL ? 128 : 256, D3 = OVL ? 256 : 0, DI3 = OVL ? 128 : 256;
     // physical slot of data component c (0 re hi, 1 re lo, 2 im hi, 3 im lo)
     auto cslot = [](int c) { return NS == 3 ? c : c >> 1; };
     constexpr int NP = G::NP, KS3 = G::KS3, SPI = G::SPI, RG = G::RG, NPAIR = G::NPAIR;
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
     // the ring, B = the data in bop with K = 128) or step 3 (A = the data in
     // bop with K = NP, B = DFT-N2 tiles from the ring).
     auto gemm = [&](int nst, bool step3) {
-        const uint32_t dr = tb, di = tb + 256;
+        const uint32_t dr = tb + (step3 ? D3 : 0), di = dr + (step3 ? DI3 : DI1);
         const uint32_t idesc = instr_desc(128, NP, false), idesc_m = instr_desc(128, NP, true);
         for (int s = 0; s < nst; ++s, ++g) {
             const int b = RES ? s : g % NRING;  // resident tiles: K-step s in buffer s
@@ -407,6 +412,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
             for (int i = 0; i < NRING - 1; ++i) issue_copy(i);
         }
     }
+    // y[k1 + 128 k2] = step-3 result x inv, a warp's stores 32 consecutive values
+    constexpr int HALF_OUT = NP / 2;
+    auto store_out = [&](float2 *yo, float inv) {
+        const int k1 = quarter * 32 + lane;
+        for (int c0 = half * HALF_OUT; c0 < (half + 1) * HALF_OUT; c0 += 8) {
+            float dr[8], di[8];
+            tmem_ld8x2(lane_base + D3 + c0, lane_base + D3 + DI3 + c0, dr, di);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (c0 + j < N2) __stcs(yo + k1 + 128 * (c0 + j), make_float2(dr[j] * inv, di[j] * inv));
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    };
+    float2 *y_prev = nullptr;  // OVL: the transform whose output is still in TMEM
+    float inv_prev = 0.f;
+
     if (blockIdx.x < a.n_items) load_input(blockIdx.x);
     for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
         const TcSeg &sg = seg_of(a, item);
@@ -441,6 +462,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         __syncthreads();
         // ---- step 1: D[k1][n2] -----------------------------------------------------
         if (tid == 0) gemm(8, false);
+        if (OVL && y_prev) {  // the previous transform's output, beside this step-1 GEMM
+            __syncwarp();     // warp 0 reconverges after its lane 0 issued
+            store_out(y_prev, inv_prev);
+        }
         wait_done();
         // ---- step 2: twiddles, scale, split into B[k1][n2] -----------------------
         // The scaled input is below 2^14 per component, so |D| < 128 sqrt(2) 2^14
@@ -458,7 +483,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
 #pragma unroll
         for (int q = 0; q < GC; ++q) {
             tmem_ld8_nw(lane_base + half * HALF + 8 * (cg + q), ur + 8 * q);
-            tmem_ld8_nw(lane_base + 256 + half * HALF + 8 * (cg + q), ui + 8 * q);
+            tmem_ld8_nw(lane_base + DI1 + half * HALF + 8 * (cg + q), ui + 8 * q);
         }
         tmem_wait_tied<8 * GC>(ur, ui);
 #pragma unroll
@@ -504,20 +529,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
         if (warp != 0) load_input(next);  // lands during the GEMM
         wait_done();
         if (warp == 0) load_input(next);  // not beside the issuing lane
-        // ---- output: y[k1 + 128 k2], a warp's stores 32 consecutive values ----------
+        // ---- output --------------------------------------------------------------
         const float inv = (1.f / s1) * (1.f / s2);  // powers of two: exact
-        for (int c0 = half * HALF; c0 < (half + 1) * HALF; c0 += 8) {
-            float dr[8], di[8];
-            tmem_ld8x2(lane_base + c0, lane_base + 256 + c0, dr, di);
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (c0 + j < N2) __stcs(y + k1 + 128 * (c0 + j), make_float2(dr[j] * inv, di[j] * inv));
+        if (OVL) {
+            y_prev = y;
+            inv_prev = inv;
+        } else {
+            store_out(y, inv);
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         if (tid == 0 && err) s_err = 1;
         __syncthreads();  // TMEM read out before the next item's MMAs
         if (s_err) break;
     }
+    if (OVL && y_prev && !s_err) store_out(y_prev, inv_prev);
     if (s_err && tid == 0) {  // a wait timed out: record it, let copies and MMAs in flight finish (bounded)
         *reinterpret_cast<volatile int *>(a.status) = 1;
         for (int b = 0; b < NRING; ++b)
