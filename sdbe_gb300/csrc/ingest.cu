@@ -193,8 +193,10 @@ int run_device(sdbe_resampler *h, const Policy &after, const uint8_t *dev_pkts, 
                 h->psn += static_cast<uint64_t>(kGroupPkts);
             }
             PayloadTarget pt{gout, gbytes / 2, framed ? kOutPkt : kOutPktData, framed ? 32 : 0};
-            int rc = fft_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st,
-                               [](int64_t, int64_t) { return SDBE_OK; });
+            int rc = h->cfg.precision != SDBE_PRECISION_FP32
+                         ? tc_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st)
+                         : fft_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st,
+                                     [](int64_t, int64_t) { return SDBE_OK; });
             if (rc) return rc;
             SDBE_CK(h, cudaMemsetAsync(bmp, 0, size_t(kGroupFrames) * 256, st));
             h->launches += 1;

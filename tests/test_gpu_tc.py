@@ -167,3 +167,25 @@ def test_tc_aligned_and_mar2015_match_fp32(S):
         assert np.array_equal(f32[:, :, :32], tc[:, :, :32]), kw  # VDIF headers
         agree = float(np.mean(codes_of(f32[:, :, 32:]) == codes_of(tc[:, :, 32:])))
         assert agree >= AGREE_MIN, (kw, agree)
+
+
+def test_tc_ingest_group_equals_process(S):
+    """Group assembly (sdbe_ingest) on a tensor-core handle resamples in the
+    handle's precision: the shipped group equals sdbe_process of the same
+    packets on another tensor-core handle, bit for bit."""
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    G = 143
+    spec = S.config1()
+    batch = S.generate(spec, frame_offset=0, n_frames=1 + G)
+    with Resampler(max_frames=G, precision=N.PRECISION_TC16_FAST) as rs, \
+            Resampler(max_frames=G, precision=N.PRECISION_TC16_FAST) as ref, \
+            Resampler(max_frames=G) as f32:
+        groups, n = rs.ingest(batch)
+        assert n == 1
+        pk = S.generate(spec, frame_offset=1, n_frames=G)
+        want, _ = ref.process(pk, G, spec.b_start + 1)
+        assert np.array_equal(groups[0], want)
+        got32, _ = f32.process(pk, G, spec.b_start + 1)
+        assert float(np.mean(codes_of(groups[0]) == codes_of(got32))) >= AGREE_MIN
