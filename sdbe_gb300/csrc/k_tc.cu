@@ -1,22 +1,24 @@
 // Precision form of the resampling stage on the 5th-generation tensor cores:
 // every DFT block is a batched FP16 GEMM with FP32 accumulation in tensor
-// memory (tcgen05.mma, operands in shared memory), with both the DFT matrix
-// and the data split into hi + lo FP16 halves (a compensated product:
-// hi*hi + hi*lo + lo*hi).
+// memory (tcgen05.mma, operands in shared memory).  The DFT matrix is split
+// into hi + lo FP16 halves; with SDBE_PRECISION_TC16 the data too (three
+// products: hi*hi + hi*lo + lo*hi), with SDBE_PRECISION_TC16_FAST the data is
+// rounded to FP16 (two products).
 //
 // A complex transform of length 128*N2 (16384 = 128*128 for the inverse
 // transforms of stages A and C, 18304 = 128*143 for the forward transform of
 // stage B) runs as the four-step factorisation, with n = N2*n1 + n2 and
-// k = k1 + 128*k2:
-//   step 1  A[k1][n2] = sum_n1 F128[k1][n1] x[N2 n1 + n2]        GEMM, M=128 K=128 N=N2
-//   step 2  B[k1][n2] = A[k1][n2] w^(n2 k1)                      twiddles, FP32
-//   step 3  X[k1 + 128 k2] = sum_n2 F_N2[k2][n2] B[k1][n2]        GEMM, M=N2 K=N2 N=128
+// k = k1 + 128*k2 (NP = N2 rounded up to 16):
+//   step 1  A[k1][n2] = sum_n1 F128[k1][n1] x[N2 n1 + n2]     GEMM 128 x NP, K = 128
+//   step 2  B[k1][n2] = A[k1][n2] w^(n2 k1)                   twiddles, FP32
+//   step 3  X[k1 + 128 k2] = sum_n2 B[k1][n2] F_N2[k2][n2]     GEMM 128 x NP, K = NP
 // Complex products are real GEMMs accumulated into two TMEM accumulators
 // (Dr = Fr Br - Fi Bi, Di = Fi Br + Fr Bi; the inverse flips the signs of
 // the Fi terms through the instruction descriptor's negate-A bit).  Each
-// transform's input and step-1 output are scaled by powers of two (exact)
-// so that every FP16 half stays below 2^14.  The Hermitian pairings, the
-// statistics and the 2-bit packing stay on the CUDA cores.
+// transform's input is scaled by a power of two from its maximum and the
+// step-1 output by a fixed power of two (exact) so that every FP16 half
+// stays below 2^14.  The Hermitian pairings, the statistics and the 2-bit
+// packing stay on the CUDA cores.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -241,11 +243,13 @@ struct TcGeo {
 // is D[k1][k2] = B2[k1][n2] (A) x F_N2[k2][n2] (B operand), so both GEMMs are
 // 128 x NP and step 3 leaves y[k1 + 128 k2] in TMEM lane k1, column k2, which
 // a warp stores as 32 consecutive complex values.  Accumulators: Dr at column
-// 0, Di at 256.  Thread 0 issues the MMAs and the bulk copies of the DFT tiles
-// through a ring of four buffers (the tiles of K-step g+3 load while the MMAs
-// of K-step g run); warps 1-7 load
-// the next item's input into registers while the current item's step-3 GEMM
-// runs, warp 0 (whose lane 0 issues) after it.
+// 0, Di at 256 (at 16384 points step 1 at 0 and 128, step 3 at 256 and 384,
+// so that an output is stored while the next step-1 GEMM runs).  Thread 0
+// issues the MMAs and the bulk copies of the DFT tiles through a ring of four
+// buffers (the tiles of K-step g+3 load while the MMAs of K-step g run; all
+// resident at 16384 points with FP16 data); warps 1-7 load the next item's
+// input into registers while the current item's step-3 GEMM runs, warp 0
+// (whose lane 0 issues) after it.
 //
 // Input element pairs: thread tid holds pairs i*256 + tid, i < NPAIR; pair p
 // is row (q % RG)*8 + (p & 7) and K columns 2kp, 2kp+1 with q = p >> 5 and
@@ -307,7 +311,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_fft(const __grid_constant_
     uint32_t g = 0;                      // global stage index (items x SPI)
     bool err = false;                    // a wait of thread 0 timed out: issue nothing more
     uint32_t pend = 0;                   // buffers with a bulk copy in flight
-    uint32_t pend_g[NRING] = {};            // the stage each of those copies is for
+    uint32_t pend_g[NRING] = {};         // the stage each of those copies is for
     uint32_t done_n = 0;                 // completions of `done` waited for (all threads)
 
     auto issue_copy = [&](uint32_t gg) {
