@@ -188,6 +188,14 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
 // outputs to slots 16*rho(j) + r, rho = digit reversal of j over (8, 11, 13);
 // every later butterfly reads and writes the same slots g*Ns*R + k + Ns*r
 // with twiddles W_{Ns*R}^{k r}, so passes need no staging.
+//
+// R2C: the last pass also applies the R2C pairing, leaving X[q] (q <= 18304,
+// X[18304] in the spare slot padb(18304)) instead of Z.  Its butterfly k
+// holds Z[k + 2288 r] and butterfly 2288 - k holds their mirrors Z[18304 - q]
+// at r' = 7 - r, so one thread takes both (k = 0 and k = 1144 are their own
+// mirrors) and pairs in registers: one pass and one barrier fewer.  Each pair
+// is formed from its side with q <= 9152, the range of the W_36608 table.
+template <bool R2C>
 __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *__restrict__ z, const TabsB &T) {
     constexpr int NB1 = kMB / 16;  // 1144 = 143 groups of 8
     for (int h = threadIdx.x >> 4; h < 72; h += blockDim.x >> 4) {
@@ -233,9 +241,8 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
     }
     __syncthreads();
     // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
-    for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
-        float2 v[8];
-        float2 *p = sm + padb(k);  // padb(k + 2288 r) = padb(k) + 2431 r
+    auto bfly8 = [&](int k, float2 *v) {
+        const float2 *p = sm + padb(k);  // padb(k + 2288 r) = padb(k) + 2431 r
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[r] = p[2431 * r];
         float2 S[4];
@@ -248,8 +255,60 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
             v[r] = cmul(v[r], w);
         }
         dft<8, false>(v);
+    };
+    if constexpr (!R2C) {
+        for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
+            float2 v[8];
+            bfly8(k, v);
+            float2 *p = sm + padb(k);
 #pragma unroll
-        for (int r = 0; r < 8; ++r) p[2431 * r] = v[r];
+            for (int r = 0; r < 8; ++r) p[2431 * r] = v[r];
+        }
+    } else {
+        constexpr int K = kMB / 8;  // 2288
+        for (int u = threadIdx.x; u <= K / 2; u += blockDim.x) {
+            float2 a[8];
+            bfly8(u, a);
+            float2 *pa = sm + padb(u);
+            if (u == 0) {  // q = 2288 r pairs with 2288 (8 - r); X[0], X[18304] from Z[0]
+                pa[0] = make_float2(a[0].x + a[0].y, 0.f);
+                sm[padb(kMB)] = make_float2(a[0].x - a[0].y, 0.f);
+#pragma unroll
+                for (int r = 1; r <= 4; ++r) {
+                    float2 xq, xmq;
+                    r2c_pair(a[r], a[8 - r], tw2(T.h36608, T.l36608, K * r), xq, xmq);
+                    pa[2431 * r] = xq;
+                    if (r != 4) pa[2431 * (8 - r)] = xmq;
+                }
+            } else if (u == K / 2) {  // q = 1144 + 2288 r pairs with r' = 7 - r
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    float2 xq, xmq;
+                    r2c_pair(a[r], a[7 - r], tw2(T.h36608, T.l36608, u + K * r), xq, xmq);
+                    pa[2431 * r] = xq;
+                    pa[2431 * (7 - r)] = xmq;
+                }
+            } else {  // butterflies u and 2288 - u
+                float2 b[8];
+                bfly8(K - u, b);
+                float2 *pb = sm + padb(K - u);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    // pair from the side with q <= 9152 (the twiddle table's range):
+                    // q = u + 2288 r for r < 4, its mirror (2288 - u) + 2288 (7 - r) for r >= 4
+                    float2 xq, xmq;
+                    if (r < 4) {
+                        r2c_pair(a[r], b[7 - r], tw2(T.h36608, T.l36608, u + K * r), xq, xmq);
+                        pa[2431 * r] = xq;
+                        pb[2431 * (7 - r)] = xmq;
+                    } else {
+                        r2c_pair(b[7 - r], a[r], tw2(T.h36608, T.l36608, K - u + K * (7 - r)), xq, xmq);
+                        pb[2431 * (7 - r)] = xq;
+                        pa[2431 * r] = xmq;
+                    }
+                }
+            }
+        }
     }
     __syncthreads();
 }
@@ -397,22 +456,8 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         const int64_t c = local % n_chunks;
         __syncthreads();  // tables loaded / previous item's last smem reads done
         const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
-        fft18304_from_global(sm, z, TB);
-        // R2C post-processing in place: X[q], X[M'-q] from Z[q], Z[M'-q];
-        // X[0] and X[18304] (both real) from Z[0], X[18304] in the spare slot.
-        for (int q = tid; q <= kMB / 2; q += kNTB) {
-            if (q == 0) {
-                const float2 z0 = sm[0];
-                sm[0] = make_float2(z0.x + z0.y, 0.f);
-                sm[padb(kMB)] = make_float2(z0.x - z0.y, 0.f);
-            } else {
-                float2 xq, xmq;
-                r2c_pair(sm[padb(q)], sm[padb(kMB - q)], tw2(TB.h36608, TB.l36608, q), xq, xmq);
-                sm[padb(q)] = xq;
-                if (q != kMB / 2) sm[padb(kMB - q)] = xmq;
-            }
-        }
-        __syncthreads();
+        // forward 18304 with the R2C pairing in its last pass: X[q], q <= 18304
+        fft18304_from_global<true>(sm, z, TB);
         // C2R pre-processing in place on the window Y[j] = X[skip + j], j = 0..16384:
         // Z'[j] is stored in the slot of Y[j].
         for (int j = tid; j <= kMA / 2; j += kNTB) {
@@ -504,7 +549,7 @@ __global__ void __launch_bounds__(kNTB, 1)
     load_tabs_b(TB, tw);
     for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         __syncthreads();
-        fft18304_from_global(sm, reinterpret_cast<const float2 *>(in + c * kNB), TB);
+        fft18304_from_global<false>(sm, reinterpret_cast<const float2 *>(in + c * kNB), TB);
         float2 *dst = out + c * (kMB + 1);
         for (int q = threadIdx.x; q <= kMB; q += kNTB) dst[q] = r2c_bin(sm, q, __ldg(tw.w36608 + q));
     }
