@@ -458,24 +458,31 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
         // forward 18304 with the R2C pairing in its last pass: X[q], q <= 18304
         fft18304_from_global<true>(sm, z, TB);
-        // C2R pre-processing in place on the window Y[j] = X[skip + j], j = 0..16384:
-        // Z'[j] is stored in the slot of Y[j].
-        for (int j = tid; j <= kMA / 2; j += kNTB) {
-            float2 y = sm[padb(skip + j)], ym = sm[padb(skip + kMA - j)];
-            if (j == 0) {
-                y.y = 0.f;
-                ym.y = 0.f;
-            }
-            float2 zk, zmk;
-            c2r_pair(y, ym, conjf2(tw2(TA.h32768, TA.l32768, j)), zk, zmk);
-            sm[padb(skip + j)] = zk;
-            if (j != 0 && j != kMA / 2) sm[padb(skip + kMA - j)] = zmk;
-        }
-        __syncthreads();
+        // The inverse's first pass loads Z'[j], j = tid + 512 r, computed on the
+        // fly by the C2R pairing of the window Y[j] = X[skip + j], j = 0..16384
+        // (no pass of its own; ifft16384 syncs before its first stores):
+        //   j <= 8192: Z'[j] = zk of (Y[j], Y[16384 - j]) with W_32768^j;
+        //   j >  8192: Z'[j] = zmk of (Y[16384 - j], Y[j]) with W_32768^(16384 - j),
+        // so the twiddle stays in the table's range; Im Y[0] and Im Y[16384] are dropped.
         auto zin = [&](float2 *v) {
-            const float2 *src = sm + padb(skip + tid);  // padb(a + 512 r) = padb(a) + 544 r
+            const float2 *lo = sm + padb(skip + tid);          // Y[tid + 512 r] = lo[544 r]
+            const float2 *hi = sm + padb(skip + kMA - tid);    // Y[16384 - tid - 512 r] = hi[-544 r]
 #pragma unroll
-            for (int r = 0; r < 32; ++r) v[r] = src[544 * r];
+            for (int r = 0; r < 32; ++r) {
+                float2 y = lo[544 * r], ym = hi[-544 * r];
+                float2 zk, zmk;
+                if (r < 16) {
+                    if (r == 0 && tid == 0) {
+                        y.y = 0.f;
+                        ym.y = 0.f;
+                    }
+                    c2r_pair(y, ym, conjf2(tw2(TA.h32768, TA.l32768, tid + 512 * r)), zk, zmk);
+                    v[r] = zk;
+                } else {
+                    c2r_pair(ym, y, conjf2(tw2(TA.h32768, TA.l32768, kMA - tid - 512 * r)), zk, zmk);
+                    v[r] = zmk;
+                }
+            }
         };
         if constexpr (MODE == 0 || MODE == 3) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
