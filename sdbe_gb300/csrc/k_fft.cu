@@ -446,6 +446,7 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
     load_tabs_a(TA, tw);
     load_tabs_b(TB, tw);
     const int tid = threadIdx.x;
+    const float2 wc = conjf2(__ldg(tw.w32768 + tid));  // W_32768^-tid
     const int64_t n_items = S.n_items;
     for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x) {
         const SegB &g = S.s[seg_of(S, item)];
@@ -460,29 +461,16 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         fft18304_from_global<true>(sm, z, TB);
         // The inverse's first pass loads Z'[j], j = tid + 512 r, computed on the
         // fly by the C2R pairing of the window Y[j] = X[skip + j], j = 0..16384
-        // (no pass of its own; ifft16384 syncs before its first stores):
-        //   j <= 8192: Z'[j] = zk of (Y[j], Y[16384 - j]) with W_32768^j;
-        //   j >  8192: Z'[j] = zmk of (Y[16384 - j], Y[j]) with W_32768^(16384 - j),
-        // so the twiddle stays in the table's range; Im Y[0] and Im Y[16384] are dropped.
+        // (no pass of its own; ifft16384 syncs before its first stores), with
+        // W_32768^-j = wc e^{2 pi i r/64} (wc per thread, the rest compile-time);
+        // Im Y[0] and Im Y[16384] are dropped.
         auto zin = [&](float2 *v) {
-            const float2 *lo = sm + padb(skip + tid);          // Y[tid + 512 r] = lo[544 r]
-            const float2 *hi = sm + padb(skip + kMA - tid);    // Y[16384 - tid - 512 r] = hi[-544 r]
-#pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                float2 y = lo[544 * r], ym = hi[-544 * r];
-                float2 zk, zmk;
-                if (r < 16) {
-                    if (r == 0 && tid == 0) {
-                        y.y = 0.f;
-                        ym.y = 0.f;
-                    }
-                    c2r_pair(y, ym, conjf2(tw2(TA.h32768, TA.l32768, tid + 512 * r)), zk, zmk);
-                    v[r] = zk;
-                } else {
-                    c2r_pair(ym, y, conjf2(tw2(TA.h32768, TA.l32768, kMA - tid - 512 * r)), zk, zmk);
-                    v[r] = zmk;
-                }
-            }
+            const float2 *lo = sm + padb(skip + tid);        // Y[tid + 512 r] = lo[544 r]
+            const float2 *hi = sm + padb(skip + kMA - tid);  // Y[16384 - tid - 512 r] = hi[-544 r]
+            for_r(std::make_integer_sequence<int, 32>{}, [&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                v[r] = c2r_pre(lo[544 * r], hi[-544 * r], tid + 512 * r, c2r_tw<r>(wc));
+            });
         };
         if constexpr (MODE == 0 || MODE == 3) {
             uint32_t *words = reinterpret_cast<uint32_t *>(o.out + pol * o.out_pol_stride +
