@@ -375,6 +375,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
     TabsA T = tabs_a_at(sm + kPadA);
     load_tabs_a(T, tw);
+    const float2 wc = conjf2(__ldg(tw.w32768 + threadIdx.x));  // W_32768^-tid
     const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
         const SegA &g = S.s[seg_of(S, item)];
@@ -398,18 +399,23 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
         float2 *dst = reinterpret_cast<float2 *>(g.out + pol * g.out_pol_stride + s * kNA);
         // Hermitian pairing: Z[k], Z[M-k] for k = 0..8192 from X[k], X[M-k];
         // X[16384] (Nyquist) = 0 and the imaginary part of X[0] are dropped.
-        for (int k = threadIdx.x; k <= kMA / 2; k += kNTA) {
-            float2 a = nib_value(cur, k);
-            float2 b = make_float2(0.f, 0.f);
-            if (k == 0)
-                a.y = 0.f;
-            else
-                b = nib_value(cur, kMA - k);
-            float2 zk, zmk;
-            c2r_pair(a, b, conjf2(tw2(T.h32768, T.l32768, k)), zk, zmk);
-            sm[pad(k)] = zk;
-            if (k != 0 && k != kMA / 2) sm[pad(kMA - k)] = zmk;
-        }
+        // k = tid + 512 i; W_32768^-k = wc e^{2 pi i i/64} (wc per thread).
+        for_r(std::make_integer_sequence<int, 17>{}, [&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const int k = threadIdx.x + kNTA * i;
+            if (i < 16 || k == kMA / 2) {
+                float2 a = nib_value(cur, k);
+                float2 b = make_float2(0.f, 0.f);
+                if (k == 0)
+                    a.y = 0.f;
+                else
+                    b = nib_value(cur, kMA - k);
+                float2 zk, zmk;
+                c2r_pair(a, b, c2r_tw<i>(wc), zk, zmk);
+                sm[pad(k)] = zk;
+                if (k != 0 && k != kMA / 2) sm[pad(kMA - k)] = zmk;
+            }
+        });
         __syncthreads();
         auto zin = [&](float2 *v) {
             const float2 *src = sm + pad(threadIdx.x);
