@@ -181,6 +181,12 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
 }
 
+// f(integral_constant<int, R>) for each R: a loop over compile-time indices.
+template <int... R, class F>
+__device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
+    (f(std::integral_constant<int, R>{}), ...);
+}
+
 // Forward 18304-point FFT of z[m] = x[2m] + i x[2m+1] read from global memory;
 // result Z in natural order in `sm` (padded with padb).  In-place decimation
 // in time, radices 16 (from global) x 13 x 11 x 8: the first pass reads
@@ -193,8 +199,7 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
 // X[18304] in the spare slot padb(18304)) instead of Z.  Its butterfly k
 // holds Z[k + 2288 r] and butterfly 2288 - k holds their mirrors Z[18304 - q]
 // at r' = 7 - r, so one thread takes both (k = 0 and k = 1144 are their own
-// mirrors) and pairs in registers: one pass and one barrier fewer.  Each pair
-// is formed from its side with q <= 9152, the range of the W_36608 table.
+// mirrors) and pairs in registers: one pass and one barrier fewer.
 template <bool R2C>
 __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *__restrict__ z, const TabsB &T) {
     constexpr int NB1 = kMB / 16;  // 1144 = 143 groups of 8
@@ -266,47 +271,41 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         }
     } else {
         constexpr int K = kMB / 8;  // 2288
+        // W_36608^(u + 2288 r) = W_36608^u W_16^r: one table value per unit
         for (int u = threadIdx.x; u <= K / 2; u += blockDim.x) {
             float2 a[8];
             bfly8(u, a);
             float2 *pa = sm + padb(u);
+            const float2 wu = tw2(T.h36608, T.l36608, u);
             if (u == 0) {  // q = 2288 r pairs with 2288 (8 - r); X[0], X[18304] from Z[0]
                 pa[0] = make_float2(a[0].x + a[0].y, 0.f);
                 sm[padb(kMB)] = make_float2(a[0].x - a[0].y, 0.f);
-#pragma unroll
-                for (int r = 1; r <= 4; ++r) {
+                for_r(std::integer_sequence<int, 1, 2, 3, 4>{}, [&](auto rc) {
+                    constexpr int r = decltype(rc)::value;
                     float2 xq, xmq;
-                    r2c_pair(a[r], a[8 - r], tw2(T.h36608, T.l36608, K * r), xq, xmq);
+                    r2c_pair(a[r], a[8 - r], mul_tc<16, r, false>(make_float2(1.f, 0.f)), xq, xmq);
                     pa[2431 * r] = xq;
                     if (r != 4) pa[2431 * (8 - r)] = xmq;
-                }
+                });
             } else if (u == K / 2) {  // q = 1144 + 2288 r pairs with r' = 7 - r
-#pragma unroll
-                for (int r = 0; r < 4; ++r) {
+                for_r(std::make_integer_sequence<int, 4>{}, [&](auto rc) {
+                    constexpr int r = decltype(rc)::value;
                     float2 xq, xmq;
-                    r2c_pair(a[r], a[7 - r], tw2(T.h36608, T.l36608, u + K * r), xq, xmq);
+                    r2c_pair(a[r], a[7 - r], mul_tc<16, r, false>(wu), xq, xmq);
                     pa[2431 * r] = xq;
                     pa[2431 * (7 - r)] = xmq;
-                }
+                });
             } else {  // butterflies u and 2288 - u
                 float2 b[8];
                 bfly8(K - u, b);
                 float2 *pb = sm + padb(K - u);
-#pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    // pair from the side with q <= 9152 (the twiddle table's range):
-                    // q = u + 2288 r for r < 4, its mirror (2288 - u) + 2288 (7 - r) for r >= 4
+                for_r(std::make_integer_sequence<int, 8>{}, [&](auto rc) {
+                    constexpr int r = decltype(rc)::value;
                     float2 xq, xmq;
-                    if (r < 4) {
-                        r2c_pair(a[r], b[7 - r], tw2(T.h36608, T.l36608, u + K * r), xq, xmq);
-                        pa[2431 * r] = xq;
-                        pb[2431 * (7 - r)] = xmq;
-                    } else {
-                        r2c_pair(b[7 - r], a[r], tw2(T.h36608, T.l36608, K - u + K * (7 - r)), xq, xmq);
-                        pb[2431 * (7 - r)] = xq;
-                        pa[2431 * r] = xmq;
-                    }
-                }
+                    r2c_pair(a[r], b[7 - r], mul_tc<16, r, false>(wu), xq, xmq);
+                    pa[2431 * r] = xq;
+                    pb[2431 * (7 - r)] = xmq;
+                });
             }
         }
     }
@@ -346,10 +345,6 @@ __device__ __forceinline__ float2 c2r_tw(float2 base) {
     return mul_tc<64, R, true>(base);
 }
 
-template <int... R, class F>
-__device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
-    (f(std::integral_constant<int, R>{}), ...);
-}
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
