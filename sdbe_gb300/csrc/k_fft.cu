@@ -246,20 +246,23 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
     }
     __syncthreads();
     // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
-    auto bfly8 = [&](int k, float2 *v) {
+    // butterfly k with its twiddles S[q] = W^(k q), q = 1..3, and A1 = W^(4 k)
+    auto bfly8w = [&](int k, float2 *v, const float2 *S, float2 A1) {
         const float2 *p = sm + padb(k);  // padb(k + 2288 r) = padb(k) + 2431 r
 #pragma unroll
         for (int r = 0; r < 8; ++r) v[r] = p[2431 * r];
-        float2 S[4];
-#pragma unroll
-        for (int q = 1; q < 4; ++q) S[q] = tw2(T.h18304, T.l18304, k * q);
-        const float2 A1 = tw2(T.h18304, T.l18304, 4 * k);
 #pragma unroll
         for (int r = 1; r < 8; ++r) {
             const float2 w = r < 4 ? S[r] : (r == 4 ? A1 : cmul(A1, S[r - 4]));
             v[r] = cmul(v[r], w);
         }
         dft<8, false>(v);
+    };
+    auto bfly8 = [&](int k, float2 *v) {
+        float2 S[4];
+#pragma unroll
+        for (int q = 1; q < 4; ++q) S[q] = tw2(T.h18304, T.l18304, k * q);
+        bfly8w(k, v, S, tw2(T.h18304, T.l18304, 4 * k));
     };
     if constexpr (!R2C) {
         for (int k = threadIdx.x; k < kMB / 8; k += blockDim.x) {
@@ -271,12 +274,29 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         }
     } else {
         constexpr int K = kMB / 8;  // 2288
-        // W_36608^(u + 2288 r) = W_36608^u W_16^r: one table value per unit
-        for (int u = threadIdx.x; u <= K / 2; u += blockDim.x) {
+        // Units u = tid + 512 i (i < 3, u <= 1144).  Twiddles from per-thread
+        // bases and compile-time factors: W_18304^(u q) = W^(tid q) W^(512 i q);
+        // the mirror butterfly's W^((2288 - u) q) = W^(2288 q) conj(W^(u q));
+        // W_36608^(u + 2288 r) = W_36608^u W_16^r.
+        static_assert(kNTB == 512, "units u = tid + 512 i");
+        const int tid = threadIdx.x;
+        float2 B[5];
+#pragma unroll
+        for (int q = 1; q <= 4; ++q) B[q] = tw2(T.h18304, T.l18304, tid * q);
+        const float2 wt = tw2(T.h36608, T.l36608, tid);
+        for_r(std::make_integer_sequence<int, 3>{}, [&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const int u = tid + 512 * i;
+            if (u > K / 2) return;
+            float2 S[4];
+            S[1] = mul_tc<kMB, 512 * i, false>(B[1]);
+            S[2] = mul_tc<kMB, 1024 * i, false>(B[2]);
+            S[3] = mul_tc<kMB, 1536 * i, false>(B[3]);
+            const float2 A1 = mul_tc<kMB, 2048 * i, false>(B[4]);
             float2 a[8];
-            bfly8(u, a);
+            bfly8w(u, a, S, A1);
             float2 *pa = sm + padb(u);
-            const float2 wu = tw2(T.h36608, T.l36608, u);
+            const float2 wu = mul_tc<kNB, 512 * i, false>(wt);
             if (u == 0) {  // q = 2288 r pairs with 2288 (8 - r); X[0], X[18304] from Z[0]
                 pa[0] = make_float2(a[0].x + a[0].y, 0.f);
                 sm[padb(kMB)] = make_float2(a[0].x - a[0].y, 0.f);
@@ -296,8 +316,12 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
                     pa[2431 * (7 - r)] = xmq;
                 });
             } else {  // butterflies u and 2288 - u
+                float2 Sm[4];
+                Sm[1] = mul_tc<kMB, K, false>(conjf2(S[1]));
+                Sm[2] = mul_tc<kMB, 2 * K, false>(conjf2(S[2]));
+                Sm[3] = mul_tc<kMB, 3 * K, false>(conjf2(S[3]));
                 float2 b[8];
-                bfly8(K - u, b);
+                bfly8w(K - u, b, Sm, mul_tc<kMB, 4 * K, false>(conjf2(A1)));
                 float2 *pb = sm + padb(K - u);
                 for_r(std::make_integer_sequence<int, 8>{}, [&](auto rc) {
                     constexpr int r = decltype(rc)::value;
@@ -307,7 +331,7 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
                     pb[2431 * (7 - r)] = xmq;
                 });
             }
-        }
+        });
     }
     __syncthreads();
 }
