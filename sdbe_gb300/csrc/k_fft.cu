@@ -114,7 +114,7 @@ __constant__ uint8_t kFirstPassGroups[144] = {
 // Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(r) gives
 // input element tid + 512 r of this thread (it may read `sm`: a barrier
 // separates those reads from the writes); epi(jj, u) receives outputs
-// z[jj + 1024 r], r < 16.  blockDim.x is a multiple of 32 and >= 512.
+// z[jj + 1024 r], r < 16.  blockDim.x is 512.
 template <class In, class Epi>
 __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi) {
     const int tid = threadIdx.x;
@@ -159,17 +159,27 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
         for (int r = 0; r < 32; ++r) dst[33 * r] = v[r];
     }
     __syncthreads();
-    for (int jj = tid; jj < 1024; jj += blockDim.x) {
+    // last pass: jj = tid + 512 i, i = 0, 1; W_16384^(jj s) = W^(tid s) W^(512 i s)
+    float2 S0[4], A0[4];
+#pragma unroll
+    for (int s = 1; s < 4; ++s) S0[s] = tw2(T.h16384, T.l16384, tid * s);
+#pragma unroll
+    for (int a = 1; a < 4; ++a) A0[a] = tw2(T.h16384, T.l16384, tid * 4 * a);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int jj = tid + 512 * i;
         float2 u[16];
         const float2 *src = sm + pad(jj);
 #pragma unroll
         for (int r = 0; r < 16; ++r) u[r] = src[1056 * r];
         // W_16384^{jj r} = A[r/4] * S[r%4]
         float2 S[4], A[4];
-#pragma unroll
-        for (int s = 1; s < 4; ++s) S[s] = tw2(T.h16384, T.l16384, jj * s);
-#pragma unroll
-        for (int a = 1; a < 4; ++a) A[a] = tw2(T.h16384, T.l16384, jj * 4 * a);
+        S[1] = i ? mul_tc<kMA, 512, false>(S0[1]) : S0[1];
+        S[2] = i ? mul_tc<kMA, 1024, false>(S0[2]) : S0[2];
+        S[3] = i ? mul_tc<kMA, 1536, false>(S0[3]) : S0[3];
+        A[1] = i ? mul_tc<kMA, 2048, false>(A0[1]) : A0[1];
+        A[2] = i ? mul_tc<kMA, 4096, false>(A0[2]) : A0[2];
+        A[3] = i ? mul_tc<kMA, 6144, false>(A0[3]) : A0[3];
 #pragma unroll
         for (int r = 1; r < 16; ++r) {
             const int a = r >> 2, s = r & 3;
