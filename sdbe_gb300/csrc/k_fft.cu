@@ -227,18 +227,24 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         for (int r = 0; r < 16; ++r) d[r] = v[r];
     }
     __syncthreads();
-    // radix 13, Ns = 16: twiddles W_208^{k r}
-    for (int b = threadIdx.x; b < kMB / 13; b += blockDim.x) {
-        const int k = b & 15;
-        float2 *p = sm + padb((b >> 4) * 208 + k);  // padb(base + 16 r) = padb(base) + 17 r
-        float2 v[13];
+    // radix 13, Ns = 16: twiddles W_208^{k r}; k = b & 15 = tid & 15 for all of a
+    // thread's butterflies (blockDim.x is a multiple of 16), so they load once
+    {
+        const int k = threadIdx.x & 15;
+        float2 w13[13];
 #pragma unroll
-        for (int r = 0; r < 13; ++r) v[r] = p[17 * r];
+        for (int r = 1; r < 13; ++r) w13[r] = T.t13[16 * (r - 1) + k];
+        for (int b = threadIdx.x; b < kMB / 13; b += blockDim.x) {
+            float2 *p = sm + padb((b >> 4) * 208 + k);  // padb(base + 16 r) = padb(base) + 17 r
+            float2 v[13];
 #pragma unroll
-        for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], T.t13[16 * (r - 1) + k]);
-        dft<13, false>(v);
+            for (int r = 0; r < 13; ++r) v[r] = p[17 * r];
 #pragma unroll
-        for (int r = 0; r < 13; ++r) p[17 * r] = v[r];
+            for (int r = 1; r < 13; ++r) v[r] = cmul(v[r], w13[r]);
+            dft<13, false>(v);
+#pragma unroll
+            for (int r = 0; r < 13; ++r) p[17 * r] = v[r];
+        }
     }
     __syncthreads();
     // radix 11, Ns = 208: twiddles W_2288^{k r}
