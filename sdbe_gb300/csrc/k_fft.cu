@@ -247,18 +247,27 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         }
     }
     __syncthreads();
-    // radix 11, Ns = 208: twiddles W_2288^{k r}
-    for (int b = threadIdx.x; b < kMB / 11; b += blockDim.x) {
-        const int k = b % 208;
-        float2 *p = sm + padb((b / 208) * 2288 + k);  // padb(base + 208 r) = padb(base) + 221 r
-        float2 v[11];
+    // radix 11, Ns = 208: twiddles W_2288^{k r}.  Butterfly (m, k) is at base
+    // 2288 m + k, m < 8, k < 208; thread t takes k = t % 208 and m = t / 208
+    // + j nk, nk = the threads sharing its k, so its twiddles load once (at
+    // most 4 butterflies a thread, as with b = t + 512 j).
+    {
+        static_assert(kNTB == 512, "512 threads share 208 x 8 butterflies");
+        const int t = threadIdx.x, k = t % 208, nk = k < 512 - 2 * 208 ? 3 : 2;
+        float2 w11[11];
 #pragma unroll
-        for (int r = 0; r < 11; ++r) v[r] = p[221 * r];
+        for (int r = 1; r < 11; ++r) w11[r] = T.t11[208 * (r - 1) + k];
+        for (int m = t / 208; m < 8; m += nk) {
+            float2 *p = sm + padb(2288 * m + k);  // padb(base + 208 r) = padb(base) + 221 r
+            float2 v[11];
 #pragma unroll
-        for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], T.t11[208 * (r - 1) + k]);
-        dft<11, false>(v);
+            for (int r = 0; r < 11; ++r) v[r] = p[221 * r];
 #pragma unroll
-        for (int r = 0; r < 11; ++r) p[221 * r] = v[r];
+            for (int r = 1; r < 11; ++r) v[r] = cmul(v[r], w11[r]);
+            dft<11, false>(v);
+#pragma unroll
+            for (int r = 0; r < 11; ++r) p[221 * r] = v[r];
+        }
     }
     __syncthreads();
     // radix 8, Ns = 2288: twiddles W_18304^{k r} = A[r/4] * S[r%4]
