@@ -191,6 +191,11 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
 }
 
+// Brings the L2 line holding p in from HBM; no register or shared-memory cost.
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // f(integral_constant<int, R>) for each R: a loop over compile-time indices.
 template <int... R, class F>
 __device__ __forceinline__ void for_r(std::integer_sequence<int, R...>, F f) {
@@ -509,6 +514,18 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
         // forward 18304 with the R2C pairing in its last pass: X[q], q <= 18304
         fft18304_from_global<true>(sm, z, TB);
+        // The next item's 146 KB chunk to L2 while this chunk's inverse runs:
+        // pass 1 of the next forward then waits on L2, not HBM (one 32-B
+        // sector per thread and step).  Prefetching the later rounds of the
+        // current pass 1 instead was slower: it delays the first round's loads.
+        if (item + gridDim.x < n_items) {
+            const int64_t nx = item + gridDim.x;
+            const SegB &gn = S.s[seg_of(S, nx)];
+            const int64_t ln = nx - gn.item0;
+            const char *zn = reinterpret_cast<const char *>(gn.in + (ln / gn.n_chunks) * gn.in_pol_stride +
+                                                            (ln % gn.n_chunks) * kNB);
+            for (int o = tid * 32; o < kNB * 4; o += kNTB * 32) prefetch_l2(zn + o);
+        }
         // The inverse's first pass loads Z'[j], j = tid + 512 r, computed on the
         // fly by the C2R pairing of the window Y[j] = X[skip + j], j = 0..16384
         // (no pass of its own; ifft16384 syncs before its first stores), with
