@@ -111,12 +111,14 @@ __constant__ uint8_t kFirstPassGroups[144] = {
     65,  57,  71,  85,  77,  91,  105, 119, 111, 125, 139, 255};
 
 // ---------------------------------------------------------------------------
-// Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(r) gives
-// input element tid + 512 r of this thread (it may read `sm`: a barrier
-// separates those reads from the writes); epi(jj, u) receives outputs
-// z[jj + 1024 r], r < 16.  blockDim.x is 512.
+// Inverse 16384-point FFT, radices 32 x 32 x 16 (Stockham).  zin(v) gives
+// input elements col + 512 r, r < 32, of this thread's first-pass column
+// `col` (a permutation of the thread index whose 16 values in each half-warp
+// are distinct mod 16; zin may read `sm`: a barrier separates those reads
+// from the writes); epi(jj, u) receives outputs z[jj + 1024 r], r < 16.
+// blockDim.x is 512.
 template <class In, class Epi>
-__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi) {
+__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col = threadIdx.x) {
     const int tid = threadIdx.x;
     float2 v[32];
     if (tid < 512) {
@@ -128,7 +130,7 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     // pad(t + 512 r) = pad(t) + 528 r, pad(b + 32 r) = pad(b) + 33 r (b % 32 + r < 32 not
     // needed: b is a multiple of 1024 plus a lane), pad(j + 1024 r) = pad(j) + 1056 r.
     if (tid < 512) {
-        float2 *dst = sm + 33 * tid;
+        float2 *dst = sm + 33 * col;
 #pragma unroll
         for (int r = 0; r < 32; ++r) dst[r] = v[r];
     }
@@ -399,6 +401,67 @@ __device__ __forceinline__ float2 c2r_tw(float2 base) {
     return mul_tc<64, R, true>(base);
 }
 
+// First-pass column of thread t for the paired C2R input below: lanes l < 16
+// of warp w take b = 16 w + l, lanes l >= 16 take 512 - (16 w + l - 16), so
+// lanes l and l ^ 16 hold mirror columns (b + b' = 512); warp 0's lane 16
+// takes 256.  The 16 columns of each half-warp are distinct mod 16.
+__device__ __forceinline__ int c2r_col(int t) {
+    const int w = t >> 5, l = t & 31;
+    if (l < 16) return 16 * w + l;
+    return (w == 0 && l == 16) ? 256 : 512 - 16 * w - (l - 16);
+}
+
+// The C2R 32768 input Z[col + 512 r], r < 32, from the bins Y[0..16384]
+// (M = 16384): Z[k] = (Y[k] + conj Y[M-k]) + i e^{2 pi i k/32768}
+// (Y[k] - conj Y[M-k]), Im Y[0] and Im Y[M] dropped (Y[M] = 0 if NYQ_ZERO).
+// Each pair (k, M - k) is formed once: for p < 16 the thread pairs its
+// k = col + 512 p with M - k, which is element 31 - p of the mirror column
+// 512 - col, held by lane l ^ 16; one shuffle swaps the halves.  Columns 0
+// and 256 are their own mirrors (M - 512 p = 512 (32 - p); M - 256 - 512 p
+// = 256 + 512 (31 - p)) and keep both halves; column 0 forms Z[8192] alone.
+// lo(p) = Y[col + 512 p] (p <= 16), hi(p) = Y[M - col - 512 p] (p < 16);
+// wcol = e^{2 pi i col/32768}.
+template <bool NYQ_ZERO, class Lo, class Hi>
+__device__ __forceinline__ void c2r_paired(float2 *v, int col, float2 wcol, Lo lo, Hi hi) {
+    const int lane = threadIdx.x & 31;
+    auto pairs = [&](auto w0c) {
+        constexpr bool W0 = decltype(w0c)::value;
+        for_r(std::make_integer_sequence<int, 16>{}, [&](auto pc) {
+            constexpr int p = decltype(pc)::value;
+            float2 y = lo(pc), ym = hi(pc);
+            if (W0 && p == 0 && col == 0) {
+                y.y = 0.f;
+                ym = NYQ_ZERO ? make_float2(0.f, 0.f) : make_float2(ym.x, 0.f);
+            }
+            float2 zk, zmk;
+            c2r_pair(y, ym, c2r_tw<p>(wcol), zk, zmk);
+            v[p] = zk;
+            const float2 x = make_float2(__shfl_xor_sync(0xffffffffu, zmk.x, 16), __shfl_xor_sync(0xffffffffu, zmk.y, 16));
+            if constexpr (!W0) {
+                v[31 - p] = x;
+            } else {  // selects, not branches: warp 0 must not fall behind
+                const bool own = lane == 16;
+                v[31 - p] = make_float2(own ? zmk.x : x.x, own ? zmk.y : x.y);
+                if constexpr (p >= 1) {
+                    const bool c0 = lane == 0;
+                    v[32 - p] = make_float2(c0 ? zmk.x : v[32 - p].x, c0 ? zmk.y : v[32 - p].y);
+                }
+            }
+        });
+    };
+    if (threadIdx.x >= 32) {
+        pairs(std::false_type{});
+    } else {
+        pairs(std::true_type{});
+        // column 0: Z[8192] = Y[8192] + conj Y[8192] + i e^{i pi/2} (Y[8192] - conj Y[8192]);
+        // the other lanes' lo(16) is in range and discarded
+        const float2 y = lo(std::integral_constant<int, 16>{});
+        const float2 z = c2r_pre(y, y, 8192, c2r_tw<16>(wcol));
+        const bool c0 = lane == 0;
+        v[16] = make_float2(c0 ? z.x : v[16].x, c0 ? z.y : v[16].y);
+    }
+}
+
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -424,7 +487,8 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     float2 *sm = reinterpret_cast<float2 *>(smem_raw + 2 * kGroups * sizeof(uint32_t));
     TabsA T = tabs_a_at(sm + kPadA);
     load_tabs_a(T, tw);
-    const float2 wc = conjf2(__ldg(tw.w32768 + threadIdx.x));  // W_32768^-tid
+    const int col = c2r_col(threadIdx.x);               // the inverse's first-pass column
+    const float2 wc = conjf2(__ldg(tw.w32768 + col));  // W_32768^-col
     const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
         const SegA &g = S.s[seg_of(S, item)];
@@ -446,36 +510,24 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
         const int64_t local = item - g.item0;
         const int64_t pol = local / g.n_snaps, s = local % g.n_snaps;
         float2 *dst = reinterpret_cast<float2 *>(g.out + pol * g.out_pol_stride + s * kNA);
-        // Hermitian pairing: Z[k], Z[M-k] for k = 0..8192 from X[k], X[M-k];
-        // X[16384] (Nyquist) = 0 and the imaginary part of X[0] are dropped.
-        // k = tid + 512 i; W_32768^-k = wc e^{2 pi i i/64} (wc per thread).
-        for_r(std::make_integer_sequence<int, 17>{}, [&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            const int k = threadIdx.x + kNTA * i;
-            if (i < 16 || k == kMA / 2) {
-                float2 a = nib_value(cur, k);
-                float2 b = make_float2(0.f, 0.f);
-                if (k == 0)
-                    a.y = 0.f;
-                else
-                    b = nib_value(cur, kMA - k);
-                float2 zk, zmk;
-                c2r_pair(a, b, c2r_tw<i>(wc), zk, zmk);
-                sm[pad(k)] = zk;
-                if (k != 0 && k != kMA / 2) sm[pad(kMA - k)] = zmk;
-            }
-        });
-        __syncthreads();
+        // The inverse's first pass forms Z[col + 512 r] from the packed bins
+        // X[k] (k < 16384; the Nyquist bin X[16384] = 0, Im X[0] dropped), each
+        // Hermitian pair once with its mirror half from lane ^ 16: no pairing
+        // pass, no barrier of its own.
         auto zin = [&](float2 *v) {
-            const float2 *src = sm + pad(threadIdx.x);
-#pragma unroll
-            for (int r = 0; r < 32; ++r) v[r] = src[528 * r];
+            c2r_paired<true>(
+                v, col, wc, [&](auto pc) { return nib_value(cur, col + kNTA * decltype(pc)::value); },
+                [&](auto pc) {
+                    constexpr int p = decltype(pc)::value;
+                    const int k = kMA - col - kNTA * p;  // 16384 only for col = 0, p = 0 (replaced by 0)
+                    return nib_value(cur, p == 0 ? (k & (kMA - 1)) : k);
+                });
         };
         auto epi = [&](int jj, const float2 *u) {
 #pragma unroll
             for (int r = 0; r < 16; ++r) __stcs(dst + jj + 1024 * r, u[r]);
         };
-        ifft16384(sm, T, zin, epi);
+        ifft16384(sm, T, zin, epi, col);
     }
 }
 
