@@ -401,6 +401,21 @@ __device__ __forceinline__ float2 c2r_tw(float2 base) {
     return mul_tc<64, R, true>(base);
 }
 
+// 8 x 8 transpose of 4-bit nibbles over the aligned groups of 8 lanes: on
+// return, nibble r of lane c is nibble c of lane r (c = lane & 7).  Step m
+// (1, 2, 4) swaps, between lanes c and c ^ m, the nibbles whose index bit m
+// differs from the lane's own bit m.
+__device__ __forceinline__ uint32_t nib_transpose8(uint32_t x, int c) {
+    constexpr uint32_t kKeep[3] = {0x0F0F0F0Fu, 0x00FF00FFu, 0x0000FFFFu};  // nibbles with index bit m clear
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int m = 1 << s, sh = 4 << s;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, m);
+        x = (c & m) ? ((x & ~kKeep[s]) | ((y >> sh) & kKeep[s])) : ((x & kKeep[s]) | ((y << sh) & ~kKeep[s]));
+    }
+    return x;
+}
+
 // First-pass column of thread t for the paired C2R input below: lanes l < 16
 // of warp w take b = 16 w + l, lanes l >= 16 take 512 - (16 w + l - 16), so
 // lanes l and l ^ 16 hold mirror columns (b + b' = 512); warp 0's lane 16
@@ -596,19 +611,30 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
                                                            (o.pkt0 + c) * o.pkt_stride + o.payload_off);
             const float th = o.thr[pol], off = o.thr[2 + pol];
             float f1 = 0.f, f2 = 0.f;
+            // Word (jj >> 3) + 128 r holds the 4-bit codes of outputs jj + 1024 r
+            // of the 8 lanes jj & 7 = c (lane c at bits 4c).  Each lane builds
+            // its codes of rows r < 8 and 8 <= r < 16 as two words (row r at
+            // bits 4 (r % 8)); an 8 x 8 nibble transpose over the 8 lanes then
+            // leaves lane c with the output words of rows c and 8 + c.
             auto epi = [&](int jj, const float2 *u) {
+                uint32_t wl = 0, wh = 0;
 #pragma unroll
-                for (int r = 0; r < 16; ++r) {
-                    uint32_t q = (code2(u[r].x, th, off) | (code2(u[r].y, th, off) << 2)) << (4 * (jj & 7));
-                    q |= __shfl_xor_sync(0xffffffffu, q, 1);
-                    q |= __shfl_xor_sync(0xffffffffu, q, 2);
-                    q |= __shfl_xor_sync(0xffffffffu, q, 4);
-                    if ((jj & 7) == 0) words[(jj >> 3) + 128 * r] = q;
-                    if constexpr (MODE == 3) {
+                for (int r = 0; r < 8; ++r) {
+                    wl |= (code2(u[r].x, th, off) | (code2(u[r].y, th, off) << 2)) << (4 * r);
+                    wh |= (code2(u[8 + r].x, th, off) | (code2(u[8 + r].y, th, off) << 2)) << (4 * r);
+                }
+                if constexpr (MODE == 3) {
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) {
                         f1 += u[r].x + u[r].y;
                         f2 = fmaf(u[r].x, u[r].x, fmaf(u[r].y, u[r].y, f2));
                     }
                 }
+                const int c = jj & 7;
+                wl = nib_transpose8(wl, c);
+                wh = nib_transpose8(wh, c);
+                words[(jj >> 3) + 128 * c] = wl;
+                words[(jj >> 3) + 128 * (8 + c)] = wh;
             };
             ifft16384(sm, TA, zin, epi);
             if constexpr (MODE == 3) {
