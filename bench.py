@@ -350,13 +350,17 @@ def run_ours(args):
         dominant = "stage_bc" if prof.stage_bc_ms >= prof.stage_a_ms else "stage_a"
         dom_bytes, dom_ms = (bc_bytes, bc_ms) if dominant == "stage_bc" else (a_bytes, a_ms)
         achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+        # DRAM bytes per unit (chunk / snapshot) from an ncu capture of full
+        # wave-64 launches, scaled to this run's average units per launch
         traffic = None
         tpath = os.path.join(ROOT, "profiles", "traffic.txt")
-        if os.path.exists(tpath) and args.wave in (0, 16):  # captured for wave-16 launches
+        if os.path.exists(tpath):
+            units = (prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) if dominant == "stage_bc"
+                     else prof.stage_a_snapshots / max(prof.stage_a_launches, 1))
             for ln in open(tpath):
                 parts = ln.split()
-                if len(parts) == 2 and parts[0] == dominant:
-                    traffic = int(parts[1])
+                if len(parts) == 2 and parts[0] == dominant + "_per_unit":
+                    traffic = int(round(float(parts[1]) * units))
         # FP32 work per launch (nominal 2.5 N log2 N per real transform)
         a_flop = 2.5 * 32768 * 15
         bc_flop = 2.5 * 36608 * np.log2(36608) + 2.5 * 32768 * 15

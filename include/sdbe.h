@@ -100,7 +100,8 @@ typedef struct sdbe_config {
     int32_t pol1_uses_pol0_threshold; /* 1 reproduces .cu:1004-1005 (pol 1 quantized with
                                          pol 0's threshold/offset); 0 = each pol its own    */
     int32_t channel_map;       /* SDBE_MAP_*                                                */
-    int32_t wave_batches;      /* batches per FFT wave (0 = default); bounds scratch        */
+    int32_t wave_batches;      /* batches per FFT wave, 1..64; 0 = 64, or fewer when       */
+                               /* max_frames cannot fill 64; scratch 37.5 MB per batch     */
     int32_t threshold_window;  /* SDBE_THRESH_WINDOW: batches in the window (0 = 64)        */
     int32_t precision;         /* SDBE_PRECISION_*                                          */
     int32_t reserved[7];

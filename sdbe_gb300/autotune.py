@@ -15,7 +15,7 @@ import json
 import os
 from typing import Callable, Iterable
 
-DEFAULT_WAVES = (8, 16, 24, 32)
+DEFAULT_WAVES = (16, 32, 48, 64)
 
 
 def _cache_path() -> str:

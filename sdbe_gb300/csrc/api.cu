@@ -547,7 +547,8 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
         return fail(nullptr, SDBE_ERR_ARG, "threshold_window in [0, 65536]");
     if (cfg->channel_map != SDBE_MAP_APHIDS && cfg->channel_map != SDBE_MAP_MAR2015)
         return fail(nullptr, SDBE_ERR_ARG, "unknown channel_map");
-    if (cfg->wave_batches < 0 || cfg->wave_batches > 64) return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
+    if (cfg->wave_batches < 0 || cfg->wave_batches > kDefaultWave)
+        return fail(nullptr, SDBE_ERR_ARG, "wave_batches in [0, 64]");
     if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16 &&
         cfg->precision != SDBE_PRECISION_TC16_FAST)
         return fail(nullptr, SDBE_ERR_ARG, "unknown precision");
@@ -561,7 +562,14 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     sdbe_resampler *h = new sdbe_resampler();
     h->cfg = *cfg;
     h->skip = skip;
-    h->wave = cfg->wave_batches > 0 ? cfg->wave_batches : 16;
+    // Default wave: 64 batches (fewer launches: each CTA loads its twiddle
+    // tables and waits on its first chunk once per launch; the persistent
+    // grid's last round is a smaller share), but no more than one call can
+    // produce, so that small handles do not hold 37.5 MB of stage-A scratch
+    // per batch they never use.
+    const int call_batches = static_cast<int>((kBatchSnaps - 1 + static_cast<int64_t>(cfg->max_frames) * kSnapsPerFrame) /
+                                              kBatchSnaps);
+    h->wave = cfg->wave_batches > 0 ? cfg->wave_batches : std::max(1, std::min(kDefaultWave, call_batches));
     h->max_snaps = static_cast<int64_t>(cfg->max_frames) * kSnapsPerFrame + kBatchSnaps;
     h->spec_pol_stride = h->max_snaps * kGroups;
     h->ts_pol_stride = static_cast<int64_t>(h->wave) * kBatchSnaps * kNA;

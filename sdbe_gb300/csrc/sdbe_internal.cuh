@@ -29,6 +29,7 @@ constexpr int kOutWords = kNC / 16;              // u32 words per output packet
 constexpr int kOutPktData = 8192;
 constexpr int kOutPkt = 8224;
 constexpr int kMaxSkip = kMB - kChannels;        // 1920
+constexpr int kDefaultWave = 64;                 // batches per FFT wave when wave_batches = 0 (and the maximum)
 
 // Packed spectrum nibble: bits 3..2 = real code, bits 1..0 = imag code, value = code - 2.
 constexpr uint32_t kMissingWord = 0xAAAAAAAAu;   // codes 2/2 = (0, 0) for all 8 channels
