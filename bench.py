@@ -593,7 +593,10 @@ def run_stress(args):
     specs = synth.config5(n_packet_streams=n_streams, n_frames=2048)
     pool = [[synth.generate(sp, frame_offset=g * G, n_frames=G) for g in range(2)] for sp in specs]
     d_pool = [[torch.from_numpy(p).cuda() for p in row] for row in pool]
-    wave = args.wave or 16
+    # 32 batches per wave: the same device time as 16 or 64 (each launch already
+    # spans all 16 handles), fewer per-wave host copies than 16, half the
+    # stage-A scratch of 64 (16 handles x 32 x 37.5 MB)
+    wave = args.wave or 32
     tc = args.precision != "fp32"
     prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
     hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=G, wave_batches=wave,
