@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     auto src_of = [&](int64_t item) {
         const SegA &g = S.s[seg_of(S, item)];
         const int64_t local = item - g.item0;
-        const int64_t pol = local / g.n_snaps, s = local % g.n_snaps;
+        const int64_t pol = local >= g.n_snaps, s = local - pol * g.n_snaps;  // n_pols <= 2: no division
         return reinterpret_cast<const uint4 *>(g.spec + pol * g.spec_pol_stride + (g.snap0 + s) * kGroups);
     };
     int64_t item = blockIdx.x;
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
         const uint32_t *cur = sp + buf * kGroups;
         const SegA &g = S.s[seg_of(S, item)];
         const int64_t local = item - g.item0;
-        const int64_t pol = local / g.n_snaps, s = local % g.n_snaps;
+        const int64_t pol = local >= g.n_snaps, s = local - pol * g.n_snaps;
         float2 *dst = reinterpret_cast<float2 *>(g.out + pol * g.out_pol_stride + s * kNA);
         // The inverse's first pass forms Z[col + 512 r] from the packed bins
         // X[k] (k < 16384; the Nyquist bin X[16384] = 0, Im X[0] dropped), each
@@ -575,8 +575,8 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         const ResampleOut &o = g.o;
         const int n_chunks = g.n_chunks, skip = g.skip;
         const int64_t local = item - g.item0;
-        const int pol = static_cast<int>(local / n_chunks);
-        const int64_t c = local % n_chunks;
+        const int pol = local >= n_chunks;  // n_pols <= 2: no division
+        const int64_t c = local - pol * n_chunks;
         __syncthreads();  // tables loaded / previous item's last smem reads done
         const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
         // forward 18304 with the R2C pairing in its last pass: X[q], q <= 18304
@@ -589,8 +589,8 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
             const int64_t nx = item + gridDim.x;
             const SegB &gn = S.s[seg_of(S, nx)];
             const int64_t ln = nx - gn.item0;
-            const char *zn = reinterpret_cast<const char *>(gn.in + (ln / gn.n_chunks) * gn.in_pol_stride +
-                                                            (ln % gn.n_chunks) * kNB);
+            const int64_t pn = ln >= gn.n_chunks;
+            const char *zn = reinterpret_cast<const char *>(gn.in + pn * gn.in_pol_stride + (ln - pn * gn.n_chunks) * kNB);
             for (int o = tid * 32; o < kNB * 4; o += kNTB * 32) prefetch_l2(zn + o);
         }
         // The inverse's first pass loads Z'[j], j = tid + 512 r, computed on the

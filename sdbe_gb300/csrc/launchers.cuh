@@ -14,7 +14,8 @@ struct ResampleOut {
 };
 
 // Work of one persistent FFT launch as segments: each handle (stream pair)
-// contributes n_pols x n items, pol-major, starting at global item item0.
+// contributes n_pols x n items (n_pols 1 or 2; the kernels find the pol by
+// one comparison), pol-major, starting at global item item0.
 // Passed by value as a __grid_constant__ kernel parameter.
 constexpr int kMaxSegs = 32;
 struct SegA {  // stage A: snapshots snap0 .. snap0+n_snaps of each pol
