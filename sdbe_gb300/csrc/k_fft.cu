@@ -37,25 +37,29 @@ constexpr int kPadB = padb(kMB) + 1;
 constexpr int kT32 = 10 * 32;          // W_1024^{j s}, s = 1..7, then W_1024^{8 j a}, a = 1..3 (16384-point pass 2)
 constexpr int kT128 = tp_len(128);     // two-level halves
 constexpr int kT13 = 12 * 16;          // W_208^{k r}, r = 1..12, k = 0..15   (18304-point radix-13 pass)
-constexpr int kT11 = 10 * 208;         // W_2288^{k r}, r = 1..10, k = 0..207 (18304-point radix-11 pass)
 constexpr int kH18304 = tp_len(143);   // W_18304^{128 a}
-constexpr int kH32768 = tp_len(65);    // W_32768^{128 a}, a <= 64   (C2R pairing, k <= 8192)
-constexpr int kH36608 = tp_len(72);    // W_36608^{128 a}, a <= 71   (R2C pairing, q <= 9152)
-constexpr int kTwA = kT32 + 2 * kT128 + kH32768 + kT128;                       // stage A tables
-constexpr int kTwB = kTwA + kT13 + kT11 + kH18304 + kT128 + kH36608 + kT128;   // stage BC tables
+constexpr int kTwA = kT32 + 2 * kT128;               // stage A tables
+constexpr int kTwB = kTwA + kT13 + kH18304 + kT128;  // stage BC tables
 constexpr size_t kSmemA = 2 * kGroups * sizeof(uint32_t) + (kPadA + kTwA) * sizeof(float2);
 constexpr size_t kSmemB = (kPadB + kTwB) * sizeof(float2);
+// Stage BC fits the 164 KB shared-memory carveout (with its 512-byte static
+// reduction buffer and the 1 KB reserved per block), so the driver can leave
+// 92 KB of the SM's 256 KB to L1 for the first pass's global loads.  Above
+// it (the 196 KB carveout, 60 KB of L1) the kernel measured 1% slower, even
+// with a radix-11 twiddle table that saves work.
+static_assert(kSmemB + 512 + 1024 <= 164 * 1024, "stage BC shared memory above the 164 KB carveout");
 
 // ---- table loading --------------------------------------------------------
-struct TabsA {  // inverse-16384 tables, and the C2R pairing twiddles W_32768^k (two-level)
-    float2 *t32, *h16384, *l16384, *h32768, *l32768;
+struct TabsA {  // inverse-16384 tables
+    float2 *t32, *h16384, *l16384;
 };
-struct TabsB {  // forward-18304 tables, and the R2C pairing twiddles W_36608^q (two-level)
-    float2 *t13, *t11, *h18304, *l18304, *h36608, *l36608;
+struct TabsB {  // forward-18304 tables in shared memory; W_36608^q in global memory
+    float2 *t13, *h18304, *l18304;
+    const float2 *w36608;
 };
 
 __device__ __forceinline__ TabsA tabs_a_at(float2 *p) {
-    return TabsA{p, p + kT32, p + kT32 + kT128, p + kT32 + 2 * kT128, p + kT32 + 2 * kT128 + kH32768};
+    return TabsA{p, p + kT32, p + kT32 + kT128};
 }
 
 __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
@@ -67,32 +71,21 @@ __device__ __forceinline__ void load_tabs_a(TabsA t, const Twiddles &tw) {
     for (int m = threadIdx.x; m < 128; m += blockDim.x) {
         t.h16384[tp(m)] = __ldg(tw.w16384 + 128 * m);
         t.l16384[tp(m)] = __ldg(tw.w16384 + m);
-        t.l32768[tp(m)] = __ldg(tw.w32768 + m);
     }
-    for (int m = threadIdx.x; m < 65; m += blockDim.x) t.h32768[tp(m)] = __ldg(tw.w32768 + 128 * m);
 }
 
 __device__ __forceinline__ void load_tabs_b(TabsB t, const Twiddles &tw) {
-    for (int m = threadIdx.x; m < kT11; m += blockDim.x) {
-        const int r = m / 208 + 1, k = m % 208;
-        t.t11[m] = __ldg(tw.w18304 + 8 * k * r);
-    }
     for (int m = threadIdx.x; m < kT13; m += blockDim.x) {
         const int r = (m >> 4) + 1, k = m & 15;
         t.t13[m] = __ldg(tw.w18304 + 88 * k * r);
     }
     for (int m = threadIdx.x; m < 143; m += blockDim.x) t.h18304[tp(m)] = __ldg(tw.w18304 + 128 * m);
-    for (int m = threadIdx.x; m < 128; m += blockDim.x) {
-        t.l18304[tp(m)] = __ldg(tw.w18304 + m);
-        t.l36608[tp(m)] = __ldg(tw.w36608 + m);
-    }
-    for (int m = threadIdx.x; m < 72; m += blockDim.x) t.h36608[tp(m)] = __ldg(tw.w36608 + 128 * m);
+    for (int m = threadIdx.x; m < 128; m += blockDim.x) t.l18304[tp(m)] = __ldg(tw.w18304 + m);
 }
 
-__device__ __forceinline__ TabsB tabs_b_at(float2 *tb) {
+__device__ __forceinline__ TabsB tabs_b_at(float2 *tb, const Twiddles &tw) {
     float2 *p = tb + kTwA;
-    float2 *q = p + kT13 + kT11 + kH18304 + kT128;
-    return TabsB{p, p + kT13, p + kT13 + kT11, p + kT13 + kT11 + kH18304, q, q + kH36608};
+    return TabsB{p, p + kT13, p + kT13 + kH18304, tw.w36608};
 }
 
 // First-pass lane order of the 18304-point transform: half-warp h takes the
@@ -117,8 +110,24 @@ __constant__ uint8_t kFirstPassGroups[144] = {
 // are distinct mod 16; zin may read `sm`: a barrier separates those reads
 // from the writes); epi(jj, u) receives outputs z[jj + 1024 r], r < 16.
 // blockDim.x is 512.
+// The last pass's per-thread twiddle bases W_16384^(tid s), s = 1..3, and
+// W_16384^(4 tid a), a = 1..3: they depend on the thread only, so a
+// persistent kernel can form them once.
+struct LastTw {
+    float2 S0[4], A0[4];
+};
+__device__ __forceinline__ LastTw last_tw(const TabsA &T) {
+    LastTw t;
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int s = 1; s < 4; ++s) t.S0[s] = tw2(T.h16384, T.l16384, tid * s);
+#pragma unroll
+    for (int a = 1; a < 4; ++a) t.A0[a] = tw2(T.h16384, T.l16384, tid * 4 * a);
+    return t;
+}
+
 template <class In, class Epi>
-__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col = threadIdx.x) {
+__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col, const LastTw &lt) {
     const int tid = threadIdx.x;
     float2 v[32];
     if (tid < 512) {
@@ -162,11 +171,7 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
     __syncthreads();
     // last pass: jj = tid + 512 i, i = 0, 1; W_16384^(jj s) = W^(tid s) W^(512 i s)
-    float2 S0[4], A0[4];
-#pragma unroll
-    for (int s = 1; s < 4; ++s) S0[s] = tw2(T.h16384, T.l16384, tid * s);
-#pragma unroll
-    for (int a = 1; a < 4; ++a) A0[a] = tw2(T.h16384, T.l16384, tid * 4 * a);
+    const float2 *S0 = lt.S0, *A0 = lt.A0;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
         const int jj = tid + 512 * i;
@@ -196,6 +201,11 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
 // Brings the L2 line holding p in from HBM; no register or shared-memory cost.
 __device__ __forceinline__ void prefetch_l2(const void *p) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+template <class In, class Epi>
+__device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col = threadIdx.x) {
+    ifft16384(sm, T, zin, epi, col, last_tw(T));
 }
 
 // f(integral_constant<int, R>) for each R: a loop over compile-time indices.
@@ -263,7 +273,7 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         const int t = threadIdx.x, k = t % 208, nk = k < 512 - 2 * 208 ? 3 : 2;
         float2 w11[11];
 #pragma unroll
-        for (int r = 1; r < 11; ++r) w11[r] = T.t11[208 * (r - 1) + k];
+        for (int r = 1; r < 11; ++r) w11[r] = tw2(T.h18304, T.l18304, 8 * k * r);  // W_2288^(k r), 8 k r < 18304
         for (int m = t / 208; m < 8; m += nk) {
             float2 *p = sm + padb(2288 * m + k);  // padb(base + 208 r) = padb(base) + 221 r
             float2 v[11];
@@ -315,7 +325,7 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         float2 B[5];
 #pragma unroll
         for (int q = 1; q <= 4; ++q) B[q] = tw2(T.h18304, T.l18304, tid * q);
-        const float2 wt = tw2(T.h36608, T.l36608, tid);
+        const float2 wt = __ldg(T.w36608 + tid);  // W_36608^tid
         for_r(std::make_integer_sequence<int, 3>{}, [&](auto ic) {
             constexpr int i = decltype(ic)::value;
             const int u = tid + 512 * i;
@@ -504,6 +514,8 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
     load_tabs_a(T, tw);
     const int col = c2r_col(threadIdx.x);               // the inverse's first-pass column
     const float2 wc = conjf2(__ldg(tw.w32768 + col));  // W_32768^-col
+    __syncthreads();                                    // tables loaded
+    const LastTw lt = last_tw(T);                       // once per CTA
     const int64_t n_items = S.n_items;
     auto src_of = [&](int64_t item) {
         const SegA &g = S.s[seg_of(S, item)];
@@ -542,7 +554,7 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
 #pragma unroll
             for (int r = 0; r < 16; ++r) __stcs(dst + jj + 1024 * r, u[r]);
         };
-        ifft16384(sm, T, zin, epi, col);
+        ifft16384(sm, T, zin, epi, col, lt);
     }
 }
 
@@ -563,7 +575,7 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
     TabsA TA = tabs_a_at(tb);
-    TabsB TB = tabs_b_at(tb);
+    TabsB TB = tabs_b_at(tb, tw);
     __shared__ double red[64];
     load_tabs_a(TA, tw);
     load_tabs_b(TB, tw);
@@ -685,7 +697,7 @@ __global__ void __launch_bounds__(kNTB, 1)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *sm = reinterpret_cast<float2 *>(smem_raw);
     float2 *tb = sm + kPadB;
-    TabsB TB = tabs_b_at(tb);
+    TabsB TB = tabs_b_at(tb, tw);
     load_tabs_b(TB, tw);
     for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
         __syncthreads();
