@@ -235,8 +235,11 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         if (g == 255) continue;
         const int c = threadIdx.x & 7, j = 8 * g + c;
         float2 v[16];
+        // cached read-only loads, not streaming ones: each 128-byte line is read
+        // as two 64-byte halves by different half-warps, often rounds apart,
+        // and the second half should still be in L1 (streaming loads: 2% slower)
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = __ldcs(z + j + NB1 * r);
+        for (int r = 0; r < 16; ++r) v[r] = __ldg(z + j + NB1 * r);
         dft<16, false>(v);
         // rho(8g + c) = g/11 + 13 (g%11) + 143 c; padb(16 rho + r) = 17 rho + r (r < 16)
         float2 *d = sm + 17 * (g / 11 + 13 * (g % 11) + 143 * c);
