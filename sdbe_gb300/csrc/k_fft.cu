@@ -198,11 +198,6 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
 }
 
-// Brings the L2 line holding p in from HBM; no register or shared-memory cost.
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 template <class In, class Epi>
 __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col = threadIdx.x) {
     ifft16384(sm, T, zin, epi, col, last_tw(T));
@@ -596,17 +591,22 @@ __global__ void __launch_bounds__(kNTB, 1) k_resample(const __grid_constant__ Se
         const float2 *z = reinterpret_cast<const float2 *>(g.in + pol * g.in_pol_stride + c * kNB);
         // forward 18304 with the R2C pairing in its last pass: X[q], q <= 18304
         fft18304_from_global<true>(sm, z, TB);
-        // The next item's 146 KB chunk to L2 while this chunk's inverse runs:
-        // pass 1 of the next forward then waits on L2, not HBM (one 32-B
-        // sector per thread and step).  Prefetching the later rounds of the
-        // current pass 1 instead was slower: it delays the first round's loads.
+        // The next item's 146 KB chunk to L2 while this chunk's inverse runs,
+        // as nine bulk prefetches from nine threads: pass 1 of the next
+        // forward then reads from L2, not HBM.  Per-thread prefetch
+        // instructions (9 per thread) cost about 1k cycles of issue per chunk
+        // and gained 0.5%; prefetching at the start of the chunk, or two
+        // chunks ahead, gained less.
         if (item + gridDim.x < n_items) {
             const int64_t nx = item + gridDim.x;
             const SegB &gn = S.s[seg_of(S, nx)];
             const int64_t ln = nx - gn.item0;
             const int64_t pn = ln >= gn.n_chunks;
             const char *zn = reinterpret_cast<const char *>(gn.in + pn * gn.in_pol_stride + (ln - pn * gn.n_chunks) * kNB);
-            for (int o = tid * 32; o < kNB * 4; o += kNTB * 32) prefetch_l2(zn + o);
+            if (tid < 9) {  // 146432 B = 8 x 16384 + 15360, 16-byte aligned pieces
+                const uint32_t bytes = tid < 8 ? 16384u : static_cast<uint32_t>(kNB * 4 - 8 * 16384);
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(zn + 16384 * tid), "r"(bytes) : "memory");
+            }
         }
         // The inverse's first pass loads Z'[j], j = tid + 512 r, computed on the
         // fly by the C2R pairing of the window Y[j] = X[skip + j], j = 0..16384
