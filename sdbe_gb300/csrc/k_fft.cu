@@ -198,6 +198,8 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
     }
 }
 
+// The same, forming the last pass's twiddle bases on each call (for kernels
+// with no registers to keep them across items).
 template <class In, class Epi>
 __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col = threadIdx.x) {
     ifft16384(sm, T, zin, epi, col, last_tw(T));
