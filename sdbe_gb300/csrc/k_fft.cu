@@ -43,10 +43,10 @@ constexpr int kTwB = kTwA + kT13 + kH18304 + kT128;  // stage BC tables
 constexpr size_t kSmemA = 2 * kGroups * sizeof(uint32_t) + (kPadA + kTwA) * sizeof(float2);
 constexpr size_t kSmemB = (kPadB + kTwB) * sizeof(float2);
 // Stage BC fits the 164 KB shared-memory carveout (with its 512-byte static
-// reduction buffer and the 1 KB reserved per block), so the driver can leave
-// 92 KB of the SM's 256 KB to L1 for the first pass's global loads.  Above
-// it (the 196 KB carveout, 60 KB of L1) the kernel measured 1% slower, even
-// with a radix-11 twiddle table that saves work.
+// reduction buffer and the 1 KB reserved per block).  Above it (184 KB: the
+// 196 KB carveout) the kernel measured 1% slower, even with a radix-11
+// twiddle table that saves work, and at 208 KB (the 228 KB carveout) 9.5%
+// slower.
 static_assert(kSmemB + 512 + 1024 <= 164 * 1024, "stage BC shared memory above the 164 KB carveout");
 
 // ---- table loading --------------------------------------------------------
@@ -232,9 +232,10 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
         if (g == 255) continue;
         const int c = threadIdx.x & 7, j = 8 * g + c;
         float2 v[16];
-        // cached read-only loads, not streaming ones: each 128-byte line is read
-        // as two 64-byte halves by different half-warps, often rounds apart,
-        // and the second half should still be in L1 (streaming loads: 2% slower)
+        // read-only loads (ld.global.nc), not streaming ones (ld.global.cs):
+        // measured 2% faster for the kernel, though L1 hits stay rare (7% of
+        // sectors), so the gain is not from reuse of the other half of each
+        // 128-byte line
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = __ldg(z + j + NB1 * r);
         dft<16, false>(v);
