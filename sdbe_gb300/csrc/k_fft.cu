@@ -126,7 +126,10 @@ __device__ __forceinline__ LastTw last_tw(const TabsA &T) {
     return t;
 }
 
-template <class In, class Epi>
+// ZIN_SM: zin reads `sm`, so a barrier must separate those reads from the
+// first pass's stores.  A caller whose zin reads other memory, and whose
+// previous smem reads are behind a barrier already, passes false.
+template <bool ZIN_SM = true, class In, class Epi>
 __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Epi epi, int col, const LastTw &lt) {
     const int tid = threadIdx.x;
     float2 v[32];
@@ -134,7 +137,7 @@ __device__ __forceinline__ void ifft16384(float2 *sm, const TabsA &T, In zin, Ep
         zin(v);
         dft<32, true>(v);
     }
-    __syncthreads();
+    if constexpr (ZIN_SM) __syncthreads();
     // padded addresses as base + compile-time offsets: pad(32 t + r) = 33 t + r,
     // pad(t + 512 r) = pad(t) + 528 r, pad(b + 32 r) = pad(b) + 33 r (b % 32 + r < 32 not
     // needed: b is a multiple of 1024 plus a lane), pad(j + 1024 r) = pad(j) + 1056 r.
@@ -555,7 +558,9 @@ __global__ void __launch_bounds__(kNTA, 1) k_swarm_c2r(const __grid_constant__ S
 #pragma unroll
             for (int r = 0; r < 16; ++r) __stcs(dst + jj + 1024 * r, u[r]);
         };
-        ifft16384(sm, T, zin, epi, col, lt);
+        // zin reads the packed spectrum (`cur`), not `sm`, and the barrier at
+        // the top of this loop follows the previous item's last reads of `sm`
+        ifft16384<false>(sm, T, zin, epi, col, lt);
     }
 }
 
