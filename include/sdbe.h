@@ -322,6 +322,12 @@ int sdbe_host_alloc(void **ptr, size_t bytes);
 int sdbe_host_free(void *ptr);
 
 /* ---- stage entry points (device pointers), one per reference function ---- */
+/* The kernels move data in 8- and 16-byte vectors, so device pointers must
+ * be aligned (cudaMalloc and framework allocations are): 16 bytes for
+ * packets, B-engine buffers, packed spectra, sdbe_swarm_c2r's output,
+ * sdbe_resample_chunks' input and output and sdbe_quantize2bit's input;
+ * 8 bytes for complex (c64) buffers and the float buffers of sdbe_swarm_r2c
+ * and sdbe_r2dbe_c2r.  A misaligned pointer returns SDBE_ERR_ARG. */
 
 /* vdif_to_beng (.cu:404-507) with its pre-zeroing memset (.cu:897-898):
  * int8 [n_frames][128][16384][2] (imag, real) per pol. */

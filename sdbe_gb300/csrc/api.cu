@@ -836,10 +836,18 @@ int sdbe_host_free(void *ptr) {
     return SDBE_OK;
 }
 
+// The stage entry points' device pointers: the kernels move data in 8- and
+// 16-byte vectors (and stage BC bulk-prefetches its input), so a pointer not
+// aligned to its kernel's width is refused with SDBE_ERR_ARG here rather
+// than faulting the device.
+static bool unaligned(const void *p, uintptr_t bytes) { return (reinterpret_cast<uintptr_t>(p) & (bytes - 1)) != 0; }
+
 int sdbe_vdif_to_beng(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t n_frames, int32_t channel_map,
                       int8_t *beng0, int8_t *beng1, void *stream) {
     if (n_frames < 0 || n_packets < 0 || (n_frames > 0 && (!beng0 || !beng1)) || (n_packets > 0 && !packets))
         return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    if ((n_packets > 0 && unaligned(packets, 16)) || unaligned(beng0, 16) || unaligned(beng1, 16))
+        return fail(nullptr, SDBE_ERR_ARG, "packets and B-engine buffers must be 16-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t bytes = static_cast<size_t>(n_frames) * kSnapsPerFrame * kChannels * 2;
     SDBE_CK(nullptr, cudaMemsetAsync(beng0, 0, bytes, st));
@@ -854,6 +862,8 @@ int sdbe_unpack(const void *packets, int64_t n_packets, uint64_t b_zero, int32_t
     if (n_frames < 0 || n_packets < 0 || !spec || !bitmap || !frame_counts || !rejected || snap0 < 0 ||
         (n_packets > 0 && !packets))
         return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    if ((n_packets > 0 && unaligned(packets, 16)) || unaligned(spec, 4))
+        return fail(nullptr, SDBE_ERR_ARG, "packets must be 16-byte aligned, spectra 4-byte aligned");
     SDBE_CK(nullptr, launch_unpack(packets, n_packets, b_zero, n_frames, channel_map, spec, pol_stride_words, snap0,
                                    bitmap, frame_counts, rejected, static_cast<cudaStream_t>(stream)));
     return SDBE_OK;
@@ -869,12 +879,15 @@ int sdbe_fill_missing(const uint32_t *bitmap, int32_t n_frames, int32_t channel_
 
 int sdbe_beng_to_complex(const int8_t *beng, int64_t n_spectra, void *out_c64, void *stream) {
     if (n_spectra < 0 || (n_spectra > 0 && (!beng || !out_c64))) return fail(nullptr, SDBE_ERR_ARG, "bad argument");
+    if (unaligned(beng, 2) || unaligned(out_c64, 8))
+        return fail(nullptr, SDBE_ERR_ARG, "B-engine input must be 2-byte, complex output 8-byte aligned");
     SDBE_CK(nullptr, launch_beng_to_complex(beng, n_spectra, out_c64, static_cast<cudaStream_t>(stream)));
     return SDBE_OK;
 }
 
 int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots, float *out, void *stream) {
     if (!h || n_snapshots < 0 || (n_snapshots > 0 && (!spec || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    if (unaligned(spec, 16) || unaligned(out, 16)) return fail(h, SDBE_ERR_ARG, "spectra and output must be 16-byte aligned");
     DeviceGuard g(h->cfg.device);
     if (h->cfg.precision != SDBE_PRECISION_FP32) return tc_swarm_c2r(h, spec, n_snapshots, out, pick(h, stream));
     SDBE_CK(h, launch_swarm_c2r(spec, 0, 0, n_snapshots, 1, out, 0, h->tw, pick(h, stream)));
@@ -883,6 +896,7 @@ int sdbe_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snapshots,
 
 int sdbe_swarm_r2c(sdbe_resampler *h, const float *in, int64_t n_chunks, void *out_c64, void *stream) {
     if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out_c64))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    if (unaligned(in, 8) || unaligned(out_c64, 8)) return fail(h, SDBE_ERR_ARG, "input and output must be 8-byte aligned");
     DeviceGuard g(h->cfg.device);
     SDBE_CK(h, launch_swarm_r2c(in, n_chunks, out_c64, h->tw, pick(h, stream)));
     return SDBE_OK;
@@ -892,6 +906,7 @@ int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int3
                    void *stream) {
     if (!h || n_chunks < 0 || skip_chan < 0 || skip_chan > kMaxSkip || (n_chunks > 0 && (!in_c64 || !out)))
         return fail(h, SDBE_ERR_ARG, "bad argument");
+    if (unaligned(in_c64, 8) || unaligned(out, 8)) return fail(h, SDBE_ERR_ARG, "input and output must be 8-byte aligned");
     DeviceGuard g(h->cfg.device);
     SDBE_CK(h, launch_r2dbe_c2r(in_c64, kMB + 1, n_chunks, skip_chan, out, h->tw, pick(h, stream)));
     return SDBE_OK;
@@ -899,6 +914,7 @@ int sdbe_r2dbe_c2r(sdbe_resampler *h, const void *in_c64, int64_t n_chunks, int3
 
 int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, float *out, void *stream) {
     if (!h || n_chunks < 0 || (n_chunks > 0 && (!in || !out))) return fail(h, SDBE_ERR_ARG, "bad argument");
+    if (unaligned(in, 16) || unaligned(out, 16)) return fail(h, SDBE_ERR_ARG, "input and output must be 16-byte aligned");
     DeviceGuard g(h->cfg.device);
     if (h->cfg.precision != SDBE_PRECISION_FP32) return tc_resample_chunks(h, in, n_chunks, out, pick(h, stream));
     ResampleOut o{};
@@ -933,6 +949,7 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
 
 int sdbe_quantize2bit(const float *in, uint32_t *out, int64_t n, float thresh, float offset, void *stream) {
     if (n < 0 || (n % 16) != 0 || (n > 0 && (!in || !out))) return fail(nullptr, SDBE_ERR_ARG, "n must be a multiple of 16");
+    if (unaligned(in, 16) || unaligned(out, 4)) return fail(nullptr, SDBE_ERR_ARG, "input must be 16-byte, output 4-byte aligned");
     SDBE_CK(nullptr, launch_quantize_flat(in, out, n, thresh, offset, static_cast<cudaStream_t>(stream)));
     return SDBE_OK;
 }

@@ -220,3 +220,23 @@ def test_reorder_mar2015_exact(N):
     ref = O.reorder_mar2015(chan).reshape(nf - 1, 128, 2048, 8).astype(np.uint32)
     ref_words = np.bitwise_or.reduce(ref << (4 * np.arange(8, dtype=np.uint32)), axis=-1)
     np.testing.assert_array_equal(got, ref_words)
+
+
+def test_misaligned_pointers_refused(N, rs):
+    """The stage entry points refuse device pointers that their kernels'
+    vector accesses cannot take, with SDBE_ERR_ARG and no launch."""
+    lib = N.lib()
+    buf = zeros(4 * 36608 * 4 + 64)
+    out = zeros(4 * 32768 * 4 + 64)
+    base, obase = ptr(buf), ptr(out)
+    assert lib.sdbe_resample_chunks(rs.handle, base + 4, 1, obase, None) == N.ERR_ARG
+    assert lib.sdbe_resample_chunks(rs.handle, base, 1, obase + 8, None) == N.ERR_ARG
+    assert lib.sdbe_swarm_c2r(rs.handle, base + 4, 1, obase, None) == N.ERR_ARG
+    assert lib.sdbe_swarm_r2c(rs.handle, base + 4, 1, obase, None) == N.ERR_ARG
+    assert lib.sdbe_r2dbe_c2r(rs.handle, base + 4, 1, 1200, obase, None) == N.ERR_ARG
+    assert lib.sdbe_quantize2bit(base + 4, obase, 16, 1.0, 0.0, None) == N.ERR_ARG
+    assert lib.sdbe_beng_to_complex(base + 1, 1, obase, None) == N.ERR_ARG
+    assert lib.sdbe_unpack(base + 8, 1, 0, 1, 0, obase, 0, 0, obase, obase, obase, None) == N.ERR_ARG
+    # the aligned call still works afterwards (nothing was launched or left pending)
+    N.check(lib.sdbe_resample_chunks(rs.handle, base, 1, obase, None), rs.handle)
+    N.check(lib.sdbe_sync(rs.handle), rs.handle)
