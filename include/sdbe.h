@@ -203,11 +203,13 @@ int sdbe_align_start(sdbe_resampler *h, const sdbe_time_template *t);
  * or flagged invalid are counted and dropped.  Every shipped group runs the
  * stage and writes one vdif_out_data_group_t ([2][16384][8192]) to out, in
  * ship order, or with SDBE_OUT_FRAMED [2][16384] 8224-B VDIF frames whose
- * headers continue the handle's counters; *n_groups returns how many.  packets must be host memory (the
- * policy reads the headers); out is host (SDBE_OUT_HOST) or device memory
- * with room for out_groups groups (otherwise SDBE_ERR_CAPACITY before any
- * change of state, with *n_groups set to the number the batch ships).  Not
- * available with the Mar-2015 channel map. */
+ * headers continue the handle's counters; *n_groups returns how many.
+ * packets are host (SDBE_IN_HOST) or device memory (16-byte aligned, 8-byte
+ * for SDBE_IN_8PAC; the policy reads headers produced on the device); out is
+ * host (SDBE_OUT_HOST) or 16-byte aligned device memory with room for
+ * out_groups groups (otherwise SDBE_ERR_CAPACITY before any change of state,
+ * with *n_groups set to the number the batch ships).  Not available with the
+ * Mar-2015 channel map. */
 typedef struct sdbe_ingest_stats {
     int64_t packets;           /* received                                      */
     int64_t invalid;           /* invalid flag                                  */

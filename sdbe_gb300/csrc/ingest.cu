@@ -242,6 +242,8 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
         return fail(h, SDBE_ERR_ARG, "8pac input must be 8-byte aligned");
     if (!pac8 && !in_host && (reinterpret_cast<uintptr_t>(packets) & 15u))
         return fail(h, SDBE_ERR_ARG, "device packets must be 16-byte aligned");
+    if (!(flags & SDBE_OUT_HOST) && out_groups > 0 && (reinterpret_cast<uintptr_t>(out) & 15u))
+        return fail(h, SDBE_ERR_ARG, "device output must be 16-byte aligned");
     DeviceGuard g(h->cfg.device);
     if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
     cudaStream_t st = h->stream;
