@@ -408,9 +408,9 @@ int sdbe_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride_bytes, ui
  * forward PFB (pfb_inverse.cu:173-207) gives the spectra, minimum-norm where
  * the spectra leave them free.  Pseudo time stream by FP32 C2R, banded
  * P P^T solve and projection in FP64 (the systems are ill-conditioned).
- * 2 <= ntap <= 8.  The prototype compiles its solve out (#if 0); this
- * restates the method it sets up.  Allocates scratch of nblock*(4 + 8*ntap)*
- * 32768 bytes on the stream. */
+ * 2 <= ntap <= 8; spec_c64 8-byte aligned.  The prototype compiles its
+ * solve out (#if 0); this restates the method it sets up.  Allocates
+ * scratch of nblock*(4 + 8*ntap)*32768 bytes on the stream. */
 int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t nblock, int32_t ntap, float *out,
                      void *stream);
 

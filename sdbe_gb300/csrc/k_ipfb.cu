@@ -159,6 +159,8 @@ using namespace sdbe;
 extern "C" int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t nblock, int32_t ntap, float *out,
                                 void *stream) {
     if (!h || nblock < 1 || ntap < 2 || ntap > 8 || !spec_c64 || !out) return fail(h, SDBE_ERR_ARG, "bad argument");
+    if (reinterpret_cast<uintptr_t>(spec_c64) & 7u)  // read as float2
+        return fail(h, SDBE_ERR_ARG, "complex spectra must be 8-byte aligned");
     if (nblock > (int64_t(1) << 20)) return fail(h, SDBE_ERR_CAPACITY, "at most 2^20 blocks per call");
     DeviceGuard g(h->cfg.device);
     if (!g.ok) return fail(h, SDBE_ERR_CUDA, "cudaSetDevice failed");
