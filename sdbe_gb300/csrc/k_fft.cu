@@ -270,8 +270,9 @@ __device__ __forceinline__ void fft18304_from_global(float2 *sm, const float2 *_
     __syncthreads();
     // radix 11, Ns = 208: twiddles W_2288^{k r}.  Butterfly (m, k) is at base
     // 2288 m + k, m < 8, k < 208; thread t takes k = t % 208 and m = t / 208
-    // + j nk, nk = the threads sharing its k, so its twiddles load once (at
-    // most 4 butterflies a thread, as with b = t + 512 j).
+    // + j nk, nk = the threads sharing its k, so its ten twiddles are formed
+    // once per transform, from the two-level W_18304 tables (at most 4
+    // butterflies a thread, as with b = t + 512 j).
     {
         static_assert(kNTB == 512, "512 threads share 208 x 8 butterflies");
         const int t = threadIdx.x, k = t % 208, nk = k < 512 - 2 * 208 ? 3 : 2;
