@@ -379,6 +379,9 @@ def run_ours(args):
         if tc:
             roofline = _tc_roofline(prof, args.steps, 3 if args.precision == "tc16" else 2)
         cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
+        if cpu is not None:  # the same path on one thread (pocketfft in scipy.fft, workers=1)
+            one = cpu_baseline(sample_frames=8, workers=1)
+            cpu["single_thread"] = {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"]}
         lib = cufft_library_baseline(int(n_batches), samples_per_step, rs.skip_chan) if world == 1 else None
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
