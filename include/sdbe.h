@@ -371,7 +371,10 @@ int sdbe_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, f
                          void *stream);
 
 /* summary_stats + transform_reduce (.cu:66-137,953-977) in FP64:
- * out[0] = mean (quantizeOffset), out[1] = sqrt(M2/(n-1)) (quantizeThreshold). */
+ * out[0] = mean (quantizeOffset), out[1] = sqrt(M2/(n-1)) (quantizeThreshold).
+ * The sums are of the samples minus the first one, so a large common offset
+ * does not cancel digits of the variance.  Allocates n/256 (at most 1216)
+ * pairs of FP64 partial sums on the stream and waits for it. */
 int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *stream);
 
 /* Allocation-free variant of sdbe_summary_stats.  No counterpart in the
@@ -384,9 +387,13 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
  * SDBE_NOALLOC_MAX_SAMPLES (8192 partials x 16384 samples), larger n returns
  * SDBE_ERR_CAPACITY.  The first call on a device looks up the array's device
  * address with that device current; make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other host threads) race.  Nothing accumulates in it across calls,
- * so it needs no clearing.  Allocates nothing, device or host. */
+ * capture.  The address stays valid for the life of the device's context (a
+ * cudaDeviceReset ends it: make no call on that device after a reset).  Each
+ * call waits for its stream before returning, since the result goes to host
+ * memory.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race, so callers serialize them.  Nothing
+ * accumulates in it across calls, so it needs no clearing.  Allocates
+ * nothing, device or host. */
 #define SDBE_NOALLOC_MAX_SAMPLES 134217728LL
 int sdbe_summary_stats_noalloc(const float *in, int64_t n, double *out_host, void *stream);
 
@@ -409,8 +416,9 @@ int sdbe_vdif_headers(void *frames, int64_t n_pkts, int64_t pol_stride_bytes, ui
  * the spectra leave them free.  Pseudo time stream by FP32 C2R, banded
  * P P^T solve and projection in FP64 (the systems are ill-conditioned).
  * 2 <= ntap <= 8; spec_c64 8-byte aligned.  The prototype compiles its
- * solve out (#if 0); this restates the method it sets up.  Allocates
- * scratch of nblock*(4 + 8*ntap)*32768 bytes on the stream. */
+ * solve out (#if 0); this restates the method it sets up.  Uses handle
+ * scratch of nblock*(4 + 8*ntap)*32768 bytes, allocated when a call needs
+ * more than any earlier one (that growth synchronizes the device). */
 int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t nblock, int32_t ntap, float *out,
                      void *stream);
 

@@ -73,6 +73,8 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->ing_hdr);
     cudaFree(h->reform_dev);
     cudaFree(h->ipfb_tab);
+    cudaFree(h->ipfb_y);
+    cudaFree(h->ipfb_scr);
     cudaFree(h->wring);
     cudaFree(h->wpart);
     cudaFree(h->tc_f128);
@@ -109,6 +111,32 @@ int64_t frames_out(const sdbe_resampler *h, int32_t n_frames) {
 
 int64_t batches_for(const sdbe_resampler *h, int32_t n_frames) {
     return (h->carry + frames_out(h, n_frames) * kSnapsPerFrame) / kBatchSnaps;
+}
+
+cudaError_t thread_scratch(size_t bytes, void **out) {
+    struct Slot {
+        void *p = nullptr;
+        size_t bytes = 0;
+    };
+    thread_local std::vector<Slot> slots;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (static_cast<size_t>(dev) >= slots.size()) slots.resize(static_cast<size_t>(dev) + 1);
+    Slot &sl = slots[static_cast<size_t>(dev)];
+    if (sl.bytes < bytes) {
+        if (sl.p) {
+            e = cudaFree(sl.p);
+            if (e != cudaSuccess) return e;
+        }
+        sl.p = nullptr;
+        sl.bytes = 0;
+        e = cudaMalloc(&sl.p, bytes);
+        if (e != cudaSuccess) return e;
+        sl.bytes = bytes;
+    }
+    *out = sl.p;
+    return cudaSuccess;
 }
 
 int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what) {
@@ -927,12 +955,14 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
     if (!in || !out_host || n < 2) return fail(nullptr, SDBE_ERR_ARG, "need n >= 2 and non-null pointers");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int blocks = stats_partial_blocks(n);
-    double *part = nullptr;
-    SDBE_CK(nullptr, cudaMallocAsync(&part, static_cast<size_t>(blocks) * 2 * sizeof(double), st));
+    void *scr = nullptr;  // this thread's reusable scratch: the call waits for its stream below
+    SDBE_CK(nullptr, thread_scratch(static_cast<size_t>(blocks) * 2 * sizeof(double), &scr));
+    double *part = static_cast<double *>(scr);
     std::vector<double> hp(static_cast<size_t>(blocks) * 2);
+    float shift = 0.f;  // the partial sums are of x - in[0]
     cudaError_t e = launch_stats_partial(in, n, part, blocks, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
-    cudaFreeAsync(part, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&shift, in, sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(nullptr, SDBE_ERR_CUDA, std::string("summary_stats: ") + cudaGetErrorString(e));
     double s1 = 0.0, s2 = 0.0;
@@ -941,9 +971,9 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
         s2 += hp[2 * b + 1];
     }
     const double nn = static_cast<double>(n);
-    const double mean = s1 / nn;
-    out_host[0] = mean;
-    out_host[1] = std::sqrt((s2 - s1 * mean) / (nn - 1.0));
+    const double dmean = s1 / nn;
+    out_host[0] = static_cast<double>(shift) + dmean;
+    out_host[1] = std::sqrt((s2 - s1 * dmean) / (nn - 1.0));
     return SDBE_OK;
 }
 

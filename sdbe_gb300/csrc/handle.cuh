@@ -64,6 +64,10 @@ struct sdbe_resampler {
     sdbe_reform_state *reform_dev = nullptr;                // kernel's output state
     double *ipfb_tab = nullptr;   // inverse PFB: [2][ntap][32768] band of P P^T and P taps (FP64)
     int ipfb_ntap = 0;
+    uint8_t *ipfb_y = nullptr;    // inverse PFB scratch, grown to the largest call: y [nblock][32768] f32
+    int64_t ipfb_y_bytes = 0;
+    uint8_t *ipfb_scr = nullptr;  // factors [nblock][ntap][32768] f64
+    int64_t ipfb_scr_bytes = 0;
     int64_t b_first = -1;
     int64_t ing_ref = 0;
     int64_t g_count[4] = {0, 0, 0, 0};
@@ -127,6 +131,11 @@ struct DeviceGuard {
 cudaError_t timed_begin(sdbe_resampler *h, int kind, int64_t units, cudaStream_t st, size_t *slot);
 cudaError_t timed_end(sdbe_resampler *h, size_t slot, cudaStream_t st);
 int grow(sdbe_resampler *h, uint8_t **buf, int64_t *cap, int64_t need, const char *what);
+// A device buffer of at least `bytes` owned by the calling host thread on the
+// current device, kept and reused by later calls of that thread (grown when
+// too small).  For handle-less entry points that wait for their stream before
+// returning, so that one thread's calls never overlap on it.
+cudaError_t thread_scratch(size_t bytes, void **out);
 
 // Where the FFT waves write their payload packets.
 struct PayloadTarget {

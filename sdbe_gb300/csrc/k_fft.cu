@@ -923,14 +923,18 @@ __global__ void k_quantize_flat(const float *__restrict__ in, uint32_t *__restri
     out[w] = word;
 }
 
-// Per-block FP64 sums for summary statistics over n floats.
+// Per-block FP64 sums for summary statistics over n floats, of the samples
+// shifted by the first one (x - in[0]): a large common offset then cancels
+// before the sums, not in the variance (the shifted-data algorithm; the
+// finalizers add in[0] back to the mean).
 __global__ void __launch_bounds__(256) k_stats_partial(const float *__restrict__ in, int64_t n,
                                                        double *__restrict__ partials) {
     __shared__ double red[64];
+    const double c = __ldg(in);
     double s1 = 0.0, s2 = 0.0;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const double v = __ldg(in + i);
+        const double v = static_cast<double>(__ldg(in + i)) - c;
         s1 += v;
         s2 += v * v;
     }

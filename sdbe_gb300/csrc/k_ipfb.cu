@@ -178,20 +178,23 @@ extern "C" int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t
         SDBE_CK(h, cudaStreamSynchronize(st));  // tab is freed on return
         h->ipfb_ntap = ntap;
     }
-    float *y = nullptr;
-    double *scr = nullptr;
-    SDBE_CK(h, cudaMallocAsync(reinterpret_cast<void **>(&y), static_cast<size_t>(nblock) * kNA * sizeof(float), st));
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&scr), static_cast<size_t>(nblock) * ntap * kNA * sizeof(double), st);
-    if (e == cudaSuccess && h->cfg.precision != SDBE_PRECISION_FP32) {
+    // scratch owned by the handle, grown to the largest call so far
+    if (int rc = grow(h, &h->ipfb_y, &h->ipfb_y_bytes, nblock * kNA * static_cast<int64_t>(sizeof(float)),
+                      "the inverse PFB scratch"))
+        return rc;
+    if (int rc = grow(h, &h->ipfb_scr, &h->ipfb_scr_bytes,
+                      nblock * ntap * kNA * static_cast<int64_t>(sizeof(double)), "the inverse PFB scratch"))
+        return rc;
+    float *y = reinterpret_cast<float *>(h->ipfb_y);
+    double *scr = reinterpret_cast<double *>(h->ipfb_scr);
+    cudaError_t e = cudaSuccess;
+    if (h->cfg.precision != SDBE_PRECISION_FP32) {
         // the pseudo time stream on the tensor cores; scr holds the paired spectra
         // first (n x 16384 complex fits its n x ntap x 32768 doubles)
         if (int rc = tc_c2r_spectra(h, static_cast<const float2 *>(spec_c64), kMA + 1, nblock,
-                                    reinterpret_cast<float2 *>(scr), y, st)) {
-            cudaFreeAsync(scr, st);
-            cudaFreeAsync(y, st);
+                                    reinterpret_cast<float2 *>(scr), y, st))
             return rc;
-        }
-    } else if (e == cudaSuccess) {
+    } else {
         e = launch_r2dbe_c2r(spec_c64, kMA + 1, nblock, 0, y, h->tw, st);
     }
     if (e == cudaSuccess) {
@@ -205,8 +208,6 @@ extern "C" int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t
             default: e = launch_solve<8>(y, nblock, h->ipfb_tab, scr, out, st); break;
         }
     }
-    if (scr) cudaFreeAsync(scr, st);
-    cudaFreeAsync(y, st);
     if (e != cudaSuccess) return fail(h, SDBE_ERR_CUDA, std::string("inverse_pfb: ") + cudaGetErrorString(e));
     h->launches += 2;
     return SDBE_OK;

@@ -304,12 +304,12 @@ int sdbe_beng_reform(sdbe_reform_state *st, void *pkts, int64_t n_pkts, void *st
     if (reinterpret_cast<uintptr_t>(pkts) & 3u) return fail(nullptr, SDBE_ERR_ARG, "packets must be 4-byte aligned");
     if (n_pkts == 0) return SDBE_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    sdbe_reform_state *dev = nullptr;
-    SDBE_CK(nullptr, cudaMallocAsync(reinterpret_cast<void **>(&dev), sizeof(sdbe_reform_state), s));
+    void *scr = nullptr;  // this thread's reusable scratch: the call waits for its stream below
+    SDBE_CK(nullptr, thread_scratch(sizeof(sdbe_reform_state), &scr));
+    sdbe_reform_state *dev = static_cast<sdbe_reform_state *>(scr);
     cudaError_t e = launch_beng_reform(pkts, n_pkts, *st, dev, nullptr, s);
     sdbe_reform_state out{};
     if (e == cudaSuccess) e = cudaMemcpyAsync(&out, dev, sizeof(out), cudaMemcpyDeviceToHost, s);
-    cudaFreeAsync(dev, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(nullptr, SDBE_ERR_CUDA, std::string("beng_reform: ") + cudaGetErrorString(e));
     *st = out;

@@ -10,7 +10,7 @@
 // pair of FP64 sums per block, 256 threads x 64 samples per block) land in
 // g_noalloc_scratch; a one-thread kernel in this file merges them in block
 // order and leaves (mean, std) in the last two slots, which are copied to the
-// caller's host memory.
+// caller's host memory.  The call waits for its stream before it returns.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -29,7 +29,9 @@ constexpr int kNoallocMaxDevices = 64;
 // the library, held until the process exits.
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNoallocBlocks + 2];
 
-__global__ void k_noalloc_finalize(int blocks, int64_t n) {
+// The partial sums are of x - in[0] (k_stats_partial), so the mean is in[0]
+// plus their mean and no large offset cancels in the variance.
+__global__ void k_noalloc_finalize(const float *in, int blocks, int64_t n) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double s1 = 0.0, s2 = 0.0;
     for (int b = 0; b < blocks; ++b) {
@@ -37,9 +39,9 @@ __global__ void k_noalloc_finalize(int blocks, int64_t n) {
         s2 += g_noalloc_scratch[2 * b + 1];
     }
     const double nn = static_cast<double>(n);
-    const double mean = s1 / nn;
-    g_noalloc_scratch[2 * kNoallocBlocks] = mean;
-    g_noalloc_scratch[2 * kNoallocBlocks + 1] = sqrt((s2 - s1 * mean) / (nn - 1.0));
+    const double dmean = s1 / nn;
+    g_noalloc_scratch[2 * kNoallocBlocks] = static_cast<double>(in[0]) + dmean;
+    g_noalloc_scratch[2 * kNoallocBlocks + 1] = sqrt((s2 - s1 * dmean) / (nn - 1.0));
 }
 
 namespace {
@@ -85,7 +87,7 @@ extern "C" int sdbe_summary_stats_noalloc(const float *in, int64_t n, double *ou
     const int blocks = static_cast<int>((n + kNoallocSamplesPerBlock - 1) / kNoallocSamplesPerBlock);
     if (e == cudaSuccess) e = launch_stats_partial(in, n, scratch, blocks, st);
     if (e == cudaSuccess) {
-        k_noalloc_finalize<<<1, 32, 0, st>>>(blocks, n);
+        k_noalloc_finalize<<<1, 32, 0, st>>>(in, blocks, n);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)

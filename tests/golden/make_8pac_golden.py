@@ -5,7 +5,7 @@ Builds ``oracle/_ref/ref_8pac`` from ``software/aphids/vdif_8pac.c`` and
 streams cut into receive batches, and stores inputs, batch cuts, the unpacked
 and reformed packets and the final reform state (T0 as ``get_beng_t0``
 returns it, TPREV, BPREV) in ``pac8_reform.npz``.  Run where the reference
-checkout exists (``SDBE_REFERENCE``, default below); the fixture is committed.
+checkout exists, with ``SDBE_REFERENCE`` set to it; the fixture is committed.
 
 Cases: ``regular`` (on-grid timestamps across a second boundary, random
 payloads in the first units), ``jitter`` (off-grid by up to 1500 clocks),
@@ -24,7 +24,7 @@ import tempfile
 
 import numpy as np
 
-REF = os.environ.get("SDBE_REFERENCE", "/root/reference")
+REF = os.environ.get("SDBE_REFERENCE", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 BIN = os.path.join(ROOT, "oracle", "_ref", "ref_8pac")
@@ -132,6 +132,8 @@ def run_reference(src: np.ndarray, batches):
 
 
 def main():
+    if not REF:
+        sys.exit("set SDBE_REFERENCE to the Smithsonian/sdbe checkout")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), f"REF={os.path.join(REF, 'software', 'aphids')}"],
                    check=True)
     arrays = {}

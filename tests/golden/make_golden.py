@@ -1,8 +1,9 @@
 """Generate golden fixtures by running the reference's own Python code.
 
-Run in a container that has the Smithsonian/sdbe checkout (default path
-below, or ``SDBE_REFERENCE``); the fixtures it writes are committed so tests
-never need the reference at run time.
+Run where a Smithsonian/sdbe checkout exists, with ``SDBE_REFERENCE`` set to
+it (``SDBE_REFERENCE=<checkout> python tests/golden/make_golden.py``); the
+fixtures it writes are committed so tests never need the reference at run
+time.
 
 The reference prototypes are Python 2.  They are loaded here unchanged except
 for one exact semantic shim: every ``/`` becomes ``_py2div(a, b)``, which is
@@ -33,7 +34,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("SDBE_REFERENCE", "/root/reference")
+REF = os.environ.get("SDBE_REFERENCE", "")
 PROTO = os.path.join(REF, "software", "prototyping")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -197,6 +198,8 @@ def golden_fft_resample(seed=20150401):
 
 
 def main():
+    if not REF:
+        sys.exit("set SDBE_REFERENCE to the Smithsonian/sdbe checkout")
     rng = np.random.default_rng(1056)
     golden_dbe_frame(rng)
     golden_quantize_pack(rng)

@@ -60,3 +60,20 @@ def test_noalloc_largest_size_and_rejects_larger(N):
     rc = N.lib().sdbe_summary_stats_noalloc(C.c_void_p(t.data_ptr()), n + 1, out, None)
     assert rc == N.ERR_CAPACITY
     assert "exceeds the maximum" in N.last_error()
+
+
+def test_large_offset_against_oracle(N):
+    """A common offset 1e4 times the spread: both entry points sum the samples
+    minus the first one, so the variance keeps its digits (FP64 oracle)."""
+    import torch
+
+    from oracle import sdbe_oracle as O
+
+    g = torch.Generator(device="cuda").manual_seed(99)
+    t = torch.randn(2_000_000, device="cuda", generator=g) * 0.5 + 5.0e3
+    x = t.cpu().numpy()
+    mean_o, std_o = O.summary_stats(x)
+    for fn in ("sdbe_summary_stats", "sdbe_summary_stats_noalloc"):
+        mean, std = _stats(N, fn, t)
+        assert abs(mean - mean_o) <= REL_TOL * std_o * 1e3, fn
+        assert abs(std - std_o) <= 1e-9 * std_o, fn
