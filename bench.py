@@ -211,6 +211,75 @@ def cpu_baseline(sample_frames=96, workers=None):
                       f"{dt:.1f} s"}
 
 
+PRECISION_BATCHES = (0, 229)
+
+
+def oracle_fp64_series(pkts, b_start, batches=PRECISION_BATCHES):
+    """The CPU leg's FP64 reference for the precision figures: the oracle's
+    series of pol 0 for each sampled batch of the bench stream (before
+    requantization), with its FP64 offset and threshold."""
+    from oracle import sdbe_oracle as O
+
+    skip = O.skip_chan_from_mhz(TRIM_MHZ)
+    w = os.cpu_count() or 1
+    refs = {}
+    for b in batches:
+        s0, s1 = b * 143, (b + 1) * 143
+        f0, f1 = s0 // 128, (s1 - 1) // 128 + 1
+        beng = O.vdif_to_beng(pkts[f0 * 2048:f1 * 2048], b_start + f0, f1 - f0)
+        spec = O.beng_to_complex(beng[0].reshape(-1, 16384, 2))[s0 - f0 * 128:s1 - f0 * 128]
+        y = O.r2dbe_c2r(O.swarm_r2c(O.swarm_c2r(spec, workers=w).reshape(-1), workers=w), skip, workers=w)
+        off, th = O.summary_stats(y)
+        refs[b] = (y, off, th, O.quantize2bit_codes(y, th, off))
+    return refs
+
+
+def _codes(y, th, off):
+    v = np.asarray(y, np.float32) - np.float32(off)
+    th = np.float32(th)
+    # code2 of quantize2bit (.cu:565-583): |v| >= th is outer, v < 0 negative
+    return np.where(v >= 0, np.where(v >= th, 3, 2), np.where(v <= -th, 0, 1)).astype(np.uint8)
+
+
+def gpu_precision(rs, d_pkts, b_start, refs):
+    """Relative RMS of the resampled series before requantization and 2-bit
+    code agreement against the FP64 series, for the handle's precision: the
+    sampled batches of pol 0 through the stage entry points (sdbe_unpack,
+    sdbe_swarm_c2r, sdbe_resample_chunks); the GPU codes use FP64 statistics
+    of the GPU's own series, as the stage does."""
+    import torch
+
+    from sdbe_gb300 import _native as N
+
+    lib = N.lib()
+    out = {}
+    for b, (ref, _, _, ref_codes) in refs.items():
+        s0 = b * 143
+        f0, f1 = s0 // 128, (s0 + 142) // 128 + 1
+        nf = f1 - f0
+        words = torch.empty(2 * nf * 128 * 2048, dtype=torch.int32, device="cuda")
+        bitmap = torch.zeros(nf * 256, dtype=torch.uint8, device="cuda")
+        counts = torch.zeros(nf, dtype=torch.int32, device="cuda")
+        rej = torch.zeros(1, dtype=torch.int32, device="cuda")
+        sel = d_pkts[f0 * 2048:f1 * 2048]
+        N.check(lib.sdbe_unpack(sel.data_ptr(), sel.shape[0], b_start + f0, nf, 0, words.data_ptr(),
+                                nf * 128 * 2048, 0, bitmap.data_ptr(), counts.data_ptr(), rej.data_ptr(), None))
+        ts = torch.empty(143 * 32768, dtype=torch.float32, device="cuda")
+        y = torch.empty(128 * 32768, dtype=torch.float32, device="cuda")
+        src = words.data_ptr() + (s0 - f0 * 128) * 2048 * 4
+        N.check(lib.sdbe_swarm_c2r(rs.handle, src, 143, ts.data_ptr(), None), rs.handle)
+        N.check(lib.sdbe_resample_chunks(rs.handle, ts.data_ptr(), 128, y.data_ptr(), None), rs.handle)
+        torch.cuda.synchronize()
+        got = y.cpu().numpy().astype(np.float64)
+        rms = float(np.sqrt(np.mean((got - ref.ravel()) ** 2) / np.mean(ref ** 2)))
+        g_off, g_th = float(got.mean()), float(got.std(ddof=1))
+        agree = float(np.mean(_codes(got, g_th, g_off) == ref_codes.ravel()))
+        out[b] = {"rel_rms": rms, "code_agreement": agree}
+    return {"batches": list(refs.keys()), "rel_rms": max(v["rel_rms"] for v in out.values()),
+            "code_agreement": min(v["code_agreement"] for v in out.values()), "per_batch": out,
+            "against": "FP64 oracle series of pol 0 (numpy), its own FP64 mean/std thresholds"}
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm on the host cores (CPU oracle port)."""
     rank, _, world = _env_rank()
@@ -247,30 +316,58 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
+PRECS = ("fp32", "tc16", "tc16fast")
+
+
+def _prec_code(name):
+    from sdbe_gb300 import _native as N
+
+    return {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[name]
+
+
+def _traffic_per_unit():
+    """DRAM bytes per unit of work of the FP32 kernels from profiles/traffic.txt."""
+    d = {}
+    tpath = os.path.join(ROOT, "profiles", "traffic.txt")
+    if os.path.exists(tpath):
+        for ln in open(tpath):
+            parts = ln.split()
+            if len(parts) == 2 and parts[0].endswith("_per_unit"):
+                d[parts[0][:-len("_per_unit")]] = float(parts[1])
+    return d
+
+
+def fp32_fma_peak(device):
+    """Measured FP32 FMA rate (sdbe_fp32_fma_rate) in TFLOP/s."""
+    import ctypes as C
+
+    from sdbe_gb300 import _native as N
+
+    tf, ms = C.c_double(), C.c_double()
+    N.check(N.lib().sdbe_fp32_fma_rate(device, C.byref(tf), C.byref(ms)))
+    return tf.value, ms.value
+
+
+# Nominal FFT work per unit (2.5 N log2 N per real transform): stage A one
+# C2R 32768 per snapshot; stage BC one R2C 36608 + one C2R 32768 per chunk.
+FLOP_A = 2.5 * 32768 * 15
+FLOP_BC = 2.5 * 36608 * float(np.log2(36608)) + 2.5 * 32768 * 15
+
+
+def _group_arm(prec, frames, spec, pkts, d_pkts, steps, warmup, local_rank, world, e2e_steps, clocks=None, wave=0):
+    """One precision on the group512 workload: device-resident timing (value,
+    per-stage CUDA events), then end to end through the C ABI with pinned
+    host buffers (e2e).  Returns the figures and the open handle."""
     import torch
     import torch.distributed as dist
 
-    rank, local_rank, world = _env_rank()
-    torch.cuda.set_device(local_rank)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    from sdbe_gb300 import Resampler, host_buffer, synth
+    from sdbe_gb300 import Resampler, host_buffer
 
-    frames = args.frames
-    spec = synth.config2(stream=rank, n_frames=frames)
-    pkts = synth.generate(spec)
-    n_pkts = pkts.shape[0]
-    from sdbe_gb300 import _native as N
-
-    tc = args.precision != "fp32"
-    prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
-    rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=args.wave,
-                   precision=prec)
+    rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=wave,
+                   precision=_prec_code(prec))
     out_bytes = rs.output_bytes(frames)
     n_batches = out_bytes // (2 * 128 * 8192)
-    samples_per_step = n_batches * OUT_SAMPLES_PER_BATCH * 2
-    d_pkts = torch.from_numpy(pkts).cuda()
+    samples = n_batches * OUT_SAMPLES_PER_BATCH * 2
     d_out = torch.empty(out_bytes, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
 
@@ -284,38 +381,35 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident timing (value) + live per-kernel roofline ----
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         step_dev()
     barrier()
     rs.read_profile()
     rs.profile(True)
-    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
-                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
-    clocks.start()
+    if clocks:
+        clocks.start()
     barrier()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         step_dev()
     ev1.record(stream)
     barrier()
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop() if clocks else None
+    ms = ev0.elapsed_time(ev1) / steps
     prof = rs.read_profile()
     rs.profile(False)
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_max = float(t.item())
-    value = world * samples_per_step / (ms_max * 1e-3) / 1e9
+    value = world * samples / (ms_max * 1e-3) / 1e9
 
-    # ---- end to end through the C ABI with pinned host buffers (e2e) ----
-    # Every step uploads its packets from pinned host memory and downloads its
-    # payloads; calls are issued asynchronously so one step's upload overlaps
-    # the previous step's compute, as consecutive groups do in the pipeline.
-    h_pkts = host_buffer(pkts.nbytes).reshape(pkts.shape)
+    # end to end: every step uploads its packets from pinned host memory and
+    # downloads its payloads; calls are queued asynchronously so one step's
+    # upload overlaps the previous step's compute, as consecutive groups do
+    h_base = host_buffer(pkts.nbytes)
+    h_pkts = h_base.reshape(pkts.shape)
     h_pkts[...] = pkts
     h_out = host_buffer(out_bytes)
 
@@ -327,7 +421,6 @@ def run_ours(args):
         step_e2e()
     rs.sync()
     barrier()
-    e2e_steps = max(3, min(args.steps, 10))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         step_e2e()
@@ -336,53 +429,133 @@ def run_ours(args):
     t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * samples_per_step / (float(t.item()) * 1e-3) / 1e9
+    e2e_ms = float(t.item())
     e2e_ok = bool(np.array_equal(np.asarray(h_out[:1 << 20]), d_out[:1 << 20].cpu().numpy()))
+    h_base.free()
+    h_out.free()
+    return rs, {
+        "value": value, "ms_per_step": ms_max, "steps": steps, "samples_per_step": samples,
+        "n_batches": int(n_batches), "out_bytes": int(out_bytes), "prof": prof, "clocks": clk,
+        "x_realtime": value / (REALTIME_GSPS * 2 * world),
+        "e2e": {"value": world * samples / (e2e_ms * 1e-3) / 1e9, "unit": "GS/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(pkts.shape[0] * 1056), "d2h_bytes_per_step": int(out_bytes),
+                "api": "Resampler.process(host pinned buffers) -> sdbe_process(SDBE_IN_HOST|SDBE_OUT_HOST|"
+                       "SDBE_ASYNC), sdbe_sync after the timed steps",
+                "matches_device_path": e2e_ok},
+    }
 
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, local_rank, world = _env_rank()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    from sdbe_gb300 import synth
+
+    frames = args.frames
+    spec = synth.config2(stream=rank, n_frames=frames)
+    pkts = synth.generate(spec)
+    n_pkts = pkts.shape[0]
+    d_pkts = torch.from_numpy(pkts).cuda()
+    gpu = (int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
+           if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
+
+    # ---- headline arm: the precision asked for (FP32 by default) -----------
+    rs, main = _group_arm(args.precision, frames, spec, pkts, d_pkts, args.steps, args.warmup, local_rank, world,
+                          max(3, min(args.steps, 10)), clocks=ClockSampler(gpu), wave=args.wave)
+    prof = main["prof"]
+    samples_per_step = main["samples_per_step"]
+    n_batches = main["n_batches"]
+    out_bytes = main["out_bytes"]
+    value, ms_max = main["value"], main["ms_per_step"]
+    skip_chan = rs.skip_chan
+    line = None
     if rank == 0:
-        peak, peak_kind = _load_peaks()
+        hbm, hbm_kind = _load_peaks()
+        fma_tf, fma_ms = fp32_fma_peak(local_rank)
         a_ms = prof.stage_a_ms / max(prof.stage_a_launches, 1)
         bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
-        # algorithmic bytes: stage A reads 8 KB packed + writes 128 KB per snapshot;
-        # stage BC reads 36608 floats + writes 8 KB per chunk
-        a_bytes = prof.stage_a_snapshots / max(prof.stage_a_launches, 1) * (8192 + 131072)
-        bc_bytes = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) * (36608 * 4 + 8192)
+        a_units = prof.stage_a_snapshots / max(prof.stage_a_launches, 1)
+        bc_units = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1)
         dominant = "stage_bc" if prof.stage_bc_ms >= prof.stage_a_ms else "stage_a"
-        dom_bytes, dom_ms = (bc_bytes, bc_ms) if dominant == "stage_bc" else (a_bytes, a_ms)
-        achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-        # DRAM bytes per unit (chunk / snapshot) from an ncu capture of full
-        # wave-64 launches, scaled to this run's average units per launch
-        traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.txt")
-        if os.path.exists(tpath):
-            units = (prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) if dominant == "stage_bc"
-                     else prof.stage_a_snapshots / max(prof.stage_a_launches, 1))
-            for ln in open(tpath):
-                parts = ln.split()
-                if len(parts) == 2 and parts[0] == dominant + "_per_unit":
-                    traffic = int(round(float(parts[1]) * units))
-        # FP32 work per launch (nominal 2.5 N log2 N per real transform)
-        a_flop = 2.5 * 32768 * 15
-        bc_flop = 2.5 * 36608 * np.log2(36608) + 2.5 * 32768 * 15
-        nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
-        fp32 = {"stage_a_tflops": prof.stage_a_snapshots * a_flop / (prof.stage_a_ms * 1e-3) / 1e12
-                if prof.stage_a_ms else None,
-                "stage_bc_tflops": prof.stage_bc_chunks * bc_flop / (prof.stage_bc_ms * 1e-3) / 1e12
-                if prof.stage_bc_ms else None,
-                "peak_tflops": nominal_fp32, "peak_kind": "nominal (152 SM x 128 FP32 lanes x 2 x 2.07 GHz)"}
-        roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                    "ms_per_launch": dom_ms, "algorithmic_bytes_per_launch": dom_bytes,
-                    "stage_ms_per_step": {"stage_a": prof.stage_a_ms / args.steps,
-                                          "stage_bc": prof.stage_bc_ms / args.steps},
-                    "fp32": fp32}
-        if tc:
-            roofline = _tc_roofline(prof, args.steps, 3 if args.precision == "tc16" else 2)
-        cpu = cpu_baseline() if (world == 1 and not args.no_cpu) else None
-        if cpu is not None:  # the same path on one thread (pocketfft in scipy.fft, workers=1)
-            one = cpu_baseline(sample_frames=8, workers=1)
+        # algorithmic bytes of the whole step (packets in once, 2-bit payloads out once)
+        alg_bytes = n_pkts * 1056 + out_bytes
+        tpu = _traffic_per_unit()
+        measured = None
+        if {"stage_a", "stage_bc", "unpack"} <= set(tpu):
+            measured = (tpu["stage_a"] * prof.stage_a_snapshots + tpu["stage_bc"] * prof.stage_bc_chunks) / \
+                args.steps + tpu["unpack"] * n_pkts
+        hbm_view = {
+            "algorithmic_bytes_per_step": int(alg_bytes),
+            "hbm_frac_algorithmic": alg_bytes / (ms_max * 1e-3) / 1e9 / hbm, "hbm_peak_gbs": hbm,
+            "hbm_peak_kind": hbm_kind,
+            "measured_dram_bytes_per_step": int(measured) if measured else None,
+            "traffic_ratio": measured / alg_bytes if measured else None,
+            "traffic_source": "per-unit DRAM bytes of the FP32 kernels' ncu capture (profiles/traffic.txt)"}
+        if args.precision == "fp32":
+            dom_flop = FLOP_BC * bc_units if dominant == "stage_bc" else FLOP_A * a_units
+            dom_ms = bc_ms if dominant == "stage_bc" else a_ms
+            ach = dom_flop / (dom_ms * 1e-3) / 1e12
+            traffic = None
+            if dominant in tpu:
+                traffic = int(round(tpu[dominant] * (bc_units if dominant == "stage_bc" else a_units)))
+            roofline = {
+                "bound": "fp32_issue", "kernel": "k_resample<0> (stage BC)" if dominant == "stage_bc"
+                else "k_swarm_c2r (stage A)", "achieved": ach, "peak": fma_tf, "unit": "TFLOP/s",
+                "frac": ach / fma_tf, "traffic": traffic,
+                "peak_kind": f"measured FP32 FMA rate (sdbe_fp32_fma_rate, {fma_ms:.1f} ms launch, clocks of the "
+                             f"timed region: {main['clocks'].get('sm_mhz') if main['clocks'] else None} MHz)",
+                "flop_per_unit": FLOP_BC if dominant == "stage_bc" else FLOP_A,
+                "flop_per_launch": dom_flop, "ms_per_launch": dom_ms,
+                "units_per_launch": bc_units if dominant == "stage_bc" else a_units,
+                "stage_ms_per_step": {"stage_a": prof.stage_a_ms / args.steps,
+                                      "stage_bc": prof.stage_bc_ms / args.steps},
+                "stage_tflops": {"stage_a": FLOP_A * a_units / (a_ms * 1e-3) / 1e12 if a_ms else None,
+                                 "stage_bc": FLOP_BC * bc_units / (bc_ms * 1e-3) / 1e12 if bc_ms else None},
+                **hbm_view}
+        else:
+            roofline = {**_tc_roofline(prof, args.steps, 3 if args.precision == "tc16" else 2), **hbm_view}
+
+        # ---- the other precisions on the same stream (tensor-core arms) -------
+        others = {}
+        if world == 1 and not args.no_arms:
+            for prec in PRECS:
+                if prec == args.precision:
+                    continue
+                ors, o = _group_arm(prec, frames, spec, pkts, d_pkts, min(args.steps, 10), 3, local_rank, 1, 3)
+                others[prec] = (ors, o)
+        cpu = refs = None
+        if world == 1 and not args.no_cpu:
+            cpu = cpu_baseline()
+            one = cpu_baseline(sample_frames=8, workers=1)   # the same path on one thread
             cpu["single_thread"] = {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"]}
-        lib = cufft_library_baseline(int(n_batches), samples_per_step, rs.skip_chan) if world == 1 else None
+            refs = oracle_fp64_series(pkts, spec.b_start)
+        precision = {}
+        if refs is not None:
+            precision[args.precision] = gpu_precision(rs, d_pkts, spec.b_start, refs)
+            for prec, (ors, _) in others.items():
+                precision[prec] = gpu_precision(ors, d_pkts, spec.b_start, refs)
+        arms = {}
+        for prec, (ors, o) in others.items():
+            ors.close()
+            op = o["prof"]
+            arms[prec] = {"value": o["value"], "unit": "GS/s", "x_realtime": o["x_realtime"],
+                          "ms_per_step": o["ms_per_step"], "steps": o["steps"], "e2e": o["e2e"],
+                          "stage_ms_per_step": {"stage_a": op.stage_a_ms / o["steps"],
+                                                "stage_bc": op.stage_bc_ms / o["steps"]},
+                          "vs_headline": o["value"] / value, "precision": precision.get(prec),
+                          "roofline": _tc_roofline(op, o["steps"], 3 if prec == "tc16" else 2)
+                          if prec != "fp32" else None}
+        streams8 = {}
+        if world == 1 and not args.no_arms:
+            s8 = _streams8_setup(local_rank)
+            for prec in PRECS:
+                r = _streams8_measure(prec, s8, min(args.steps, 10), 3, local_rank, None)
+                streams8[prec] = {k: r[k] for k in ("value", "x_realtime", "ms_per_step", "wave_batches", "e2e")}
+        lib = cufft_library_baseline(int(n_batches), samples_per_step, skip_chan) if world == 1 else None
         line = {
             "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -393,51 +566,52 @@ def run_ours(args):
                        "frames": frames, "batches": int(n_batches), "streams_per_gpu": 2,
                        "packets_per_step": int(n_pkts), "wave_batches": args.wave,
                        "l2": "inputs larger than L2 (packets 1.08 GB/step, payload 0.96 GB/step)"},
-            "x_realtime": value / (REALTIME_GSPS * 2 * world),
+            "x_realtime": main["x_realtime"],
             "roofline": roofline,
+            "precision": precision.get(args.precision),
+            "tc" if args.precision == "fp32" else "other_precisions": arms,
+            "streams8": streams8,
             "cpu_baseline": cpu,
             "gpu_library_baseline": lib,
-            "e2e": {"value": e2e_value, "unit": "GS/s", "ms_per_step": float(t.item()),
-                    "h2d_bytes_per_step": int(n_pkts * 1056), "d2h_bytes_per_step": int(out_bytes),
-                    "api": "Resampler.process(host pinned buffers) -> sdbe_process(SDBE_IN_HOST|SDBE_OUT_HOST|"
-                           "SDBE_ASYNC), sdbe_sync after the timed steps",
-                    "matches_device_path": e2e_ok},
+            "e2e": main["e2e"],
             "gpu_launches": int(prof.launches),
-            "clocks": clk,
+            "clocks": main["clocks"],
         }
-        print(json.dumps(line), flush=True)
     rs.close()
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
 
 
-def run_streams(args):
-    """--workload streams8: 8 streams (4 packet streams x 2 phased sums) of
-    uneven seeded lengths (64-512 B-frames) and per-stream noise sigma in one
-    sdbe_process_multi pass per step, captured once into a CUDA graph and
-    replayed; wave size from the autotuner (timed in the untimed warm-up)."""
+def _streams8_setup(local_rank):
+    """The uneven-streams workload: 4 packet streams (8 phased sums), seeded
+    lengths 64-512 B-frames and per-stream sigma, resident on the device."""
     import torch
 
-    rank, local_rank, world = _env_rank()
-    torch.cuda.set_device(local_rank)
-    if rank != 0 and world > 1:
-        return 0
-    from sdbe_gb300 import Resampler, autotune, host_buffer, process_multi, synth
+    from sdbe_gb300 import synth
 
-    from sdbe_gb300 import _native as N
-
-    tc = args.precision != "fp32"
-    prec = {"fp32": N.PRECISION_FP32, "tc16": N.PRECISION_TC16, "tc16fast": N.PRECISION_TC16_FAST}[args.precision]
     specs = synth.config4(n_packet_streams=4)
     pk = [synth.generate(sp) for sp in specs]
-    frames = [sp.n_frames for sp in specs]
-    d_pk = [torch.from_numpy(p).cuda() for p in pk]
+    return {"specs": specs, "pk": pk, "frames": [sp.n_frames for sp in specs],
+            "d_pk": [torch.from_numpy(p).cuda() for p in pk]}
+
+
+def _streams8_measure(prec, s8, steps, warmup, local_rank, clocks, wave_arg=0):
+    """One sdbe_process_multi pass over the 8 streams per step, captured once
+    into a CUDA graph and replayed; wave size from the autotuner (timed in the
+    untimed warm-up); then end to end with pinned host buffers."""
+    import torch
+
+    from sdbe_gb300 import Resampler, autotune, host_buffer, process_multi
+
+    specs, pk, frames, d_pk = s8["specs"], s8["pk"], s8["frames"], s8["d_pk"]
     stream = torch.cuda.Stream()
 
     def make(wave):
-        hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=f, wave_batches=wave, precision=prec)
-              for f in frames]
+        hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=f, wave_batches=wave,
+                        precision=_prec_code(prec)) for f in frames]
         outs = [torch.empty(h.output_bytes(f), dtype=torch.uint8, device="cuda") for h, f in zip(hs, frames)]
         return hs, outs
 
@@ -461,12 +635,12 @@ def run_streams(args):
             h.close()
         return e0.elapsed_time(e1) / 2
 
-    key = "streams8|" + ("" if not tc else args.precision + "|") + ",".join(map(str, frames))
-    wave, table = (args.wave, {}) if args.wave else autotune.tune(key, measure)
+    key = "streams8|" + ("" if prec == "fp32" else prec + "|") + ",".join(map(str, frames))
+    wave, table = (wave_arg, {}) if wave_arg else autotune.tune(key, measure)
     hs, outs = make(wave)
     n_batches = [h.output_bytes(f) // (2 * 128 * 8192) for h, f in zip(hs, frames)]
     samples = sum(n_batches) * OUT_SAMPLES_PER_BATCH * 2
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         one_pass(hs, outs)
     torch.cuda.synchronize()
     # stage split and launch count of one pass (not graph-captured); reading
@@ -480,15 +654,13 @@ def run_streams(args):
     hs[0].profile(False)
     prof = profs[0]  # the shared FFT launches are timed on the first handle
     launches = sum(int(q.launches) for q in profs)
-    # direct passes (no graph)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         one_pass(hs, outs)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms_direct = e0.elapsed_time(e1) / args.steps
-    # one pass captured into a graph, replayed per step
+    ms_direct = e0.elapsed_time(e1) / steps
     for h in hs:
         h.reset()
     g = torch.cuda.CUDAGraph()
@@ -498,22 +670,22 @@ def run_streams(args):
     for _ in range(3):
         g.replay()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local_rank)
-    clocks.start()
+    if clocks:
+        clocks.start()
     e0.record(stream)
     with torch.cuda.stream(stream):
-        for _ in range(args.steps):
+        for _ in range(steps):
             g.replay()
     e1.record(stream)
     torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop() if clocks else None
+    ms = e0.elapsed_time(e1) / steps
     value = samples / (ms * 1e-3) / 1e9
     graph_out = [o[:1 << 20].cpu() for o in outs]
-    # end to end: pinned host buffers through the same call
-    h_pk = []
+    h_pk, h_bases = [], []
     for p in pk:
-        hb = host_buffer(p.nbytes).reshape(p.shape)
+        h_bases.append(host_buffer(p.nbytes))
+        hb = h_bases[-1].reshape(p.shape)
         hb[...] = p
         h_pk.append(hb)
     h_out = [host_buffer(int(o.numel())) for o in outs]
@@ -524,53 +696,77 @@ def run_streams(args):
         process_multi(hs, [(hp, f, sp.b_start, ho) for hp, f, sp, ho in zip(h_pk, frames, specs, h_out)],
                       asynchronous=True)
 
-    def sync_all():
-        for h in hs:
-            h.sync()
-
     pass_e2e()
-    sync_all()
+    for h in hs:
+        h.sync()
     t0 = time.perf_counter()
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(steps, 10))
     for _ in range(e2e_steps):
         pass_e2e()
-    sync_all()
+    for h in hs:
+        h.sync()
     e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
     e2e_ok = all(np.array_equal(np.asarray(ho[:1 << 20]), go.numpy()) for ho, go in zip(h_out, graph_out))
-    peak, peak_kind = _load_peaks()
-    bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
-    bc_bytes = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1) * (36608 * 4 + 8192)
-    achieved = bc_bytes / (bc_ms * 1e-3) / 1e9 if bc_ms else None
-    roofline = {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes}
-    if tc:
+    for b in h_bases + h_out:
+        b.free()
+    for h in hs:
+        h.close()
+    return {"value": value, "x_realtime": value / (REALTIME_GSPS * 8), "ms_per_step": ms,
+            "direct_ms_per_step": ms_direct, "wave_batches": wave, "autotune_ms_per_pass": table,
+            "n_batches": n_batches, "prof": prof, "launches": launches, "clocks": clk,
+            "e2e": {"value": samples / (e2e_ms * 1e-3) / 1e9, "unit": "GS/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(sum(p.nbytes for p in pk)),
+                    "d2h_bytes_per_step": int(sum(o.numel() for o in outs)),
+                    "api": "process_multi(host pinned buffers) -> sdbe_process_multi(SDBE_IN_HOST|SDBE_OUT_HOST|"
+                           "SDBE_ASYNC), sdbe_sync of every handle after the timed passes",
+                    "matches_device_path": e2e_ok}}
+
+
+def run_streams(args):
+    """--workload streams8: 8 streams (4 packet streams x 2 phased sums) of
+    uneven seeded lengths (64-512 B-frames) and per-stream noise sigma in one
+    sdbe_process_multi pass per step, captured once into a CUDA graph and
+    replayed; wave size from the autotuner (timed in the untimed warm-up)."""
+    import torch
+
+    rank, local_rank, world = _env_rank()
+    torch.cuda.set_device(local_rank)
+    if rank != 0 and world > 1:
+        return 0
+    s8 = _streams8_setup(local_rank)
+    r = _streams8_measure(args.precision, s8, args.steps, args.warmup, local_rank, ClockSampler(local_rank),
+                          args.wave)
+    prof = r["prof"]
+    if args.precision == "fp32":
+        fma_tf, fma_ms = fp32_fma_peak(local_rank)
+        bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
+        bc_units = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1)
+        ach = FLOP_BC * bc_units / (bc_ms * 1e-3) / 1e12 if bc_ms else None
+        roofline = {"bound": "fp32_issue", "kernel": "k_resample<0> (stage BC)", "achieved": ach, "peak": fma_tf,
+                    "unit": "TFLOP/s", "frac": ach / fma_tf if ach else None, "traffic": None,
+                    "peak_kind": f"measured FP32 FMA rate (sdbe_fp32_fma_rate, {fma_ms:.1f} ms launch)",
+                    "ms_per_launch": bc_ms, "flop_per_launch": FLOP_BC * bc_units}
+    else:
         roofline = _tc_roofline(prof, 1, 3 if args.precision == "tc16" else 2)
+    frames = s8["frames"]
     line = {
-        "metric": "output GS/s", "value": value, "unit": "GS/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": _DTYPE[args.precision], "data": "synthetic",
+        "metric": "output GS/s", "value": r["value"], "unit": "GS/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": _DTYPE[args.precision], "data": "synthetic",
         "config": {"workload": "8 streams (4 packet streams x 2 phased sums), uneven seeded lengths, per-stream "
                                "sigma; one sdbe_process_multi pass per step, CUDA-graph replay; "
                                + _PATH[args.precision] + "-FFT path",
-                   "frames_per_packet_stream": frames, "batches_per_packet_stream": n_batches,
-                   "wave_batches": wave, "autotune_ms_per_pass": table,
+                   "frames_per_packet_stream": frames, "batches_per_packet_stream": r["n_batches"],
+                   "wave_batches": r["wave_batches"], "autotune_ms_per_pass": r["autotune_ms_per_pass"],
                    "l2": "inputs larger than L2"},
-        "x_realtime": value / (REALTIME_GSPS * 8),
-        "direct_ms_per_step": ms_direct,
+        "x_realtime": r["x_realtime"],
+        "direct_ms_per_step": r["direct_ms_per_step"],
         "roofline": roofline,
-        "e2e": {"value": samples / (e2e_ms * 1e-3) / 1e9, "unit": "GS/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": int(sum(p.nbytes for p in pk)),
-                "d2h_bytes_per_step": int(sum(o.numel() for o in outs)),
-                "api": "process_multi(host pinned buffers) -> sdbe_process_multi(SDBE_IN_HOST|SDBE_OUT_HOST|"
-                       "SDBE_ASYNC), sdbe_sync of every handle after the timed passes",
-                "matches_device_path": e2e_ok},
-        "gpu_launches": int(launches) * args.steps,
-        "clocks": clk,
+        "e2e": r["e2e"],
+        "gpu_launches": int(r["launches"]) * args.steps,
+        "clocks": r["clocks"],
     }
     print(json.dumps(line), flush=True)
-    for h in hs:
-        h.close()
     return 0
 
 
@@ -710,7 +906,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=FRAMES)
     ap.add_argument("--wave", type=int, default=0, help="batches per FFT wave (0 = library default)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample and the precision figures")
+    ap.add_argument("--no-arms", action="store_true",
+                    help="skip the other precisions and the 8-stream figures of the default workload")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16", "tc16fast"],
                     help="fp32 radix kernels (default) or an FP16 tensor-core form "
                          "(tc16: data and DFT matrix split hi+lo; tc16fast: DFT matrix split, data FP16)")

@@ -426,6 +426,13 @@ int sdbe_inverse_pfb(sdbe_resampler *h, const void *spec_c64, int64_t nblock, in
  * [n_frames][128][2048 u32] -> [n_frames-1][128][2048 u32]. */
 int sdbe_reorder_mar2015(const uint32_t *spec_in, int32_t n_frames, uint32_t *spec_out, void *stream);
 
+/* ---- measurement helper (no counterpart in the reference) --------------- */
+/* FP32 FMA rate of a device, TFLOP/s (2 flops per FMA), from one timed
+ * launch of 16 independent FMA chains per thread, two 512-thread CTAs per
+ * SM; *ms = the launch's CUDA-event time.  The roofline denominator of the
+ * FP32 radix kernels, which are bound by FP32 issue. */
+int sdbe_fp32_fma_rate(int32_t device, double *tflops, double *ms);
+
 #ifdef __cplusplus
 }
 #endif

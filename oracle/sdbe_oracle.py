@@ -143,20 +143,18 @@ def vdif_to_beng(packets, b_zero: int, n_frames: int = BENG_FRAMES_PER_GROUP,
     sel = np.nonzero(ok)[0]
     if sel.size == 0:
         return beng[0], beng[1]
-    payload = pk[sel, IN_HDR_BYTES:].view("<u4").reshape(sel.size, BENG_SNAPSHOTS, 2)
+    # per packet and snapshot the two little-endian words as 8 bytes; byte j of
+    # word h carries channel 4h + 3 - j, so reversing each word's bytes puts
+    # channel k of the packet at position k
+    raw = pk[sel, IN_HDR_BYTES:].reshape(sel.size, BENG_SNAPSHOTS, 2, 4)
+    b8 = raw[..., ::-1].reshape(sel.size, BENG_SNAPSHOTS, 8).astype(np.int16)
+    # bit pairs of a byte, LSB first: pol1 im, pol1 re, pol0 im, pol0 re
+    vals = [((b8 >> (2 * q)) & 3) - 2 for q in range(4)]
     fr = frame[sel]
-    bs = base[sel]
-    for half in range(2):              # word 0 -> channels 3..0, word 1 -> 7..4
-        w = payload[:, :, half].astype(np.uint32)
-        for isample in range(4):
-            byte = (w >> np.uint32(8 * isample)) & np.uint32(0xFF)
-            ch = bs + (4 * half + 3 - isample)
-            vals = [((byte >> np.uint32(2 * q)) & np.uint32(3)).astype(np.int16) - 2 for q in range(4)]
-            # order of extraction: pol1 im, pol1 re, pol0 im, pol0 re
-            beng[1, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 0] = vals[0]
-            beng[1, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 1] = vals[1]
-            beng[0, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 0] = vals[2]
-            beng[0, fr[:, None], np.arange(BENG_SNAPSHOTS)[None, :], ch[:, None], 1] = vals[3]
+    grp = base[sel] // 8                       # packets carry 8 consecutive channels
+    view = beng.reshape(2, n_frames, BENG_SNAPSHOTS, BENG_CHANNELS_ // 8, 8, 2)
+    view[1][fr, :, grp] = np.stack([vals[0], vals[1]], axis=-1).astype(np.int8)   # (imag, real)
+    view[0][fr, :, grp] = np.stack([vals[2], vals[3]], axis=-1).astype(np.int8)
     return beng[0], beng[1]
 
 
@@ -169,10 +167,8 @@ def completion_bitmap(packets, b_zero: int, n_frames: int):
     """
     frame, c, f, ok = packet_frame_index(packets, b_zero, n_frames)
     cc = np.zeros((n_frames, 256), dtype=np.uint8)
-    counts = np.zeros(n_frames, dtype=np.int64)
-    for fr, cc_i, ff in zip(frame[ok], c[ok], f[ok]):
-        cc[fr, cc_i] |= np.uint8(1 << ff)
-        counts[fr] += 1
+    np.bitwise_or.at(cc, (frame[ok], c[ok]), (1 << f[ok]).astype(np.uint8))
+    counts = np.bincount(frame[ok], minlength=n_frames).astype(np.int64)
     return cc, counts
 
 

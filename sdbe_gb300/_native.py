@@ -128,6 +128,7 @@ SIGNATURES = {
     "sdbe_quantize2bit": (C.c_int, [vp, vp, i64, f32, f32, vp]),
     "sdbe_vdif_headers": (C.c_int, [vp, i64, i64, u32, u32, u64, u32, u32, u32, u32, vp]),
     "sdbe_reorder_mar2015": (C.c_int, [vp, i32, vp, vp]),
+    "sdbe_fp32_fma_rate": (C.c_int, [i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 SYNTH_SIGNATURES = {

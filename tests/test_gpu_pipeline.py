@@ -196,7 +196,7 @@ def test_bad_calls_raise(S, cfg1):
 
 
 def test_full_size_512_frames_properties(S):
-    """512-frame stream (the bench workload): sampled batches match the oracle,
+    """512-frame stream (the bench workload): every 16th batch matches the oracle,
     the run is deterministic, and the code histogram is the 2-bit Gaussian one."""
     from sdbe_gb300 import Resampler
 
@@ -219,7 +219,7 @@ def test_full_size_512_frames_properties(S):
     # inflate the std, leaving fewer than the Gaussian 15.87% beyond +-1 sigma.
     hist = np.bincount(codes_of(out[0, :128 * 8]), minlength=4) / (128 * 8 * 32768)
     assert 0.08 < hist[0] < 0.1587 and 0.08 < hist[3] < 0.1587 and abs(hist[0] - hist[3]) < 0.02
-    for b in (0, 229, 457):
+    for b in sorted(set(range(0, 458, 16)) | {457}):   # every 16th batch and the last
         s0, s1 = b * 143, (b + 1) * 143
         f0, f1 = s0 // 128, (s1 - 1) // 128 + 1
         sel = p[f0 * 2048:f1 * 2048]
