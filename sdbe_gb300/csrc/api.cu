@@ -81,6 +81,7 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->tc_f143);
     cudaFree(h->tc_bufx);
     cudaFree(h->tc_bufy);
+    cudaFree(h->tcf_tabs);
     if (h->tc_status_host) cudaFreeHost(h->tc_status_host);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);

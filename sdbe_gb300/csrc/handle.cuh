@@ -83,6 +83,7 @@ struct sdbe_resampler {
     void *tc_f128 = nullptr, *tc_f143 = nullptr;
     float2 *tc_bufx = nullptr;    // [2][wave*143][16384]
     float2 *tc_bufy = nullptr;    // [2][wave*128][18304]
+    void *tcf_tabs = nullptr;     // SDBE_PRECISION_TC16_FAST: DFT matrices and twiddle tables (on first use)
     int *tc_status_host = nullptr;  // 1 after a tensor-core barrier time-out (pinned, mapped)
     int *tc_status = nullptr;       // its device address
     // Mar-2015 format: unpacked frames land here first; the last one is held
@@ -190,6 +191,18 @@ struct TcWaveItem {
 // One wave over several tensor-core handles of the same precision, the three
 // transforms in shared launches; `first`: each item is its handle's first batch.
 int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st);
+
+// Stage A of the fast tensor-core form (k_tcf.cu): per segment, snapshots
+// [snap0, snap0 + n_snaps) of n_pols pols -> float time series [n_snaps][32768]
+// at out + pol * out_pol_stride; all segments in one launch.
+struct TcfASeg {
+    const uint32_t *spec;
+    int64_t spec_pol_stride, snap0, n_snaps;
+    float *out;
+    int64_t out_pol_stride;
+};
+int tcf_prepare(sdbe_resampler *h, cudaStream_t st);
+int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, cudaStream_t st);
 
 // sdbe_swarm_c2r / sdbe_resample_chunks of a SDBE_PRECISION_TC16 handle (one pol).
 int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st);

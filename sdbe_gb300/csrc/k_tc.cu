@@ -785,14 +785,22 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
     const int ns = tc_splits(h0);
     size_t slot = 0;
     if (!first) SDBE_CK(h0, timed_begin(h0, 0, units_a, st, &slot));
-    for (const auto &it : w) {  // stage A pairing: packed spectra -> Z (bufx)
-        const int64_t snaps = it.nb * kBatchSnaps;
-        k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(it.spec, it.spec_pol_stride,
-                                                                      it.b0 * kBatchSnaps, snaps, it.h->tc_bufx,
-                                                                      tw.w32768);
-        SDBE_CK(it.h, cudaGetLastError());
+    if (ns == 2) {  // SDBE_PRECISION_TC16_FAST: packed spectra -> time series in one launch (k_tcf.cu)
+        std::vector<TcfASeg> segs;
+        for (const auto &it : w)
+            segs.push_back(TcfASeg{it.spec, it.spec_pol_stride, it.b0 * kBatchSnaps, it.nb * kBatchSnaps,
+                                   it.h->ts, it.h->ts_pol_stride});
+        if (int rc = tcf_stage_a(h0, segs.data(), static_cast<int>(segs.size()), 2, st)) return rc;
+    } else {
+        for (const auto &it : w) {  // stage A pairing: packed spectra -> Z (bufx)
+            const int64_t snaps = it.nb * kBatchSnaps;
+            k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(it.spec, it.spec_pol_stride,
+                                                                          it.b0 * kBatchSnaps, snaps, it.h->tc_bufx,
+                                                                          tw.w32768);
+            SDBE_CK(it.h, cudaGetLastError());
+        }
+        SDBE_CK(h0, (launch_tc_fft<128, true>(A, ns, st)));  // -> time series (ts)
     }
-    SDBE_CK(h0, (launch_tc_fft<128, true>(A, ns, st)));  // -> time series (ts)
     if (!first) {
         SDBE_CK(h0, timed_end(h0, slot, st));
         SDBE_CK(h0, timed_begin(h0, 1, units_bc, st, &slot));
@@ -862,6 +870,10 @@ int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float
         return fail(h, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 needs a 16-byte aligned output buffer");
     if (int rc = tc_prepare(h, st)) return rc;
     const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
+    if (tc_splits(h) == 2) {  // SDBE_PRECISION_TC16_FAST: straight from the packed spectra (k_tcf.cu)
+        const TcfASeg seg{spec, 0, 0, n_snaps, out, 0};
+        return tcf_stage_a(h, &seg, 1, 1, st);
+    }
     const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kBatchSnaps;
     for (int64_t s0 = 0; s0 < n_snaps; s0 += cap) {
         const int64_t n = n_snaps - s0 < cap ? n_snaps - s0 : cap;

@@ -149,7 +149,10 @@ def test_impaired_windowed_streams_vs_oracle(impaired, path):
         assert res[i].frames_incomplete > 0
         (th0, th1), _, _ = thr[i]
         for pol, th in enumerate((th0, th1)):
-            assert abs(th - st.threshold[pol]) <= THR_TOL[path] * st.threshold[pol], (i, pol, th)
+            # 256 batches end on a block boundary: the handle already holds the
+            # thresholds of the next block, from batches [192, 256)
+            _, th_next = O.window_thresholds(st, pol, 256, 64)
+            assert abs(th - th_next) <= THR_TOL[path] * th_next, (i, pol, th, th_next)
             agree = float(np.mean(codes_of(outs[i][pol]) == codes_of(ref[pol])))
             print(f"{path} impaired stream {i} pol {pol}: agreement {agree:.6f} over 256 batches")
             assert agree >= AGREE_MIN, (path, i, pol, agree)
