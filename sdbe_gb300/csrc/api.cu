@@ -82,6 +82,8 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->tc_bufx);
     cudaFree(h->tc_bufy);
     cudaFree(h->tcf_tabs);
+    cudaFree(h->tcf_bins);
+    cudaFree(h->tcf_half);
     if (h->tc_status_host) cudaFreeHost(h->tc_status_host);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);

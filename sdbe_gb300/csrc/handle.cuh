@@ -84,6 +84,10 @@ struct sdbe_resampler {
     float2 *tc_bufx = nullptr;    // [2][wave*143][16384]
     float2 *tc_bufy = nullptr;    // [2][wave*128][18304]
     void *tcf_tabs = nullptr;     // SDBE_PRECISION_TC16_FAST: DFT matrices and twiddle tables (on first use)
+    uint32_t *tcf_bins = nullptr; // its R2C bins [2][wave*128][kTcfBinsLen] half2 (on first use)
+    int64_t tcf_bins_bytes = 0;
+    void *tcf_half = nullptr;     // FP16 time series of sdbe_resample_chunks inputs (on first use)
+    int64_t tcf_half_bytes = 0;
     int *tc_status_host = nullptr;  // 1 after a tensor-core barrier time-out (pinned, mapped)
     int *tc_status = nullptr;       // its device address
     // Mar-2015 format: unpacked frames land here first; the last one is held
@@ -198,11 +202,29 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
 struct TcfASeg {
     const uint32_t *spec;
     int64_t spec_pol_stride, snap0, n_snaps;
-    float *out;
-    int64_t out_pol_stride;
+    void *out;               // float, or FP16 x 2^-2
+    int64_t out_pol_stride;  // elements
 };
 int tcf_prepare(sdbe_resampler *h, cudaStream_t st);
-int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, cudaStream_t st);
+int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, bool half_out, cudaStream_t st);
+// Stages B and C of the fast tensor-core form: per segment n_chunks chunks of
+// n_pols pols of FP16 time series (x 2^-2) -> R2C bins [skip, skip + 16384]
+// (scratch, kTcfBinsLen half2 per chunk) -> mode 0: 2-bit payload (o.out ...),
+// 1: floats (o.fout) + per-chunk (n, mean, M2) in o.partials, 3: 2-bit payload
+// + per-chunk (n, sum, sum of squares) in o.partials (if not null), 5: floats.
+struct TcfBCSeg {
+    const void *ts;
+    int64_t ts_pol_stride;   // halves
+    uint32_t *bins;
+    int64_t bins_pol_stride; // bins
+    int64_t n_chunks;
+    int skip;
+    ResampleOut o;
+};
+int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols, int mode, cudaStream_t st);
+cudaError_t tcf_to_half(const float *in, void *out, int64_t n_floats, cudaStream_t st);
+// One wave of the fast tensor-core chain over several handles (as tc_wave_multi).
+int tcf_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st);
 
 // sdbe_swarm_c2r / sdbe_resample_chunks of a SDBE_PRECISION_TC16 handle (one pol).
 int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float *out, cudaStream_t st);

@@ -753,6 +753,7 @@ int tc_prepare(sdbe_resampler *h, cudaStream_t st) {
 int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st) {
     if (w.empty()) return SDBE_OK;
     sdbe_resampler *h0 = w[0].h;
+    if (tc_splits(h0) == 2) return tcf_wave_multi(w, first, st);  // SDBE_PRECISION_TC16_FAST (k_tcf.cu)
     for (const auto &it : w) {
         if (int rc = tc_prepare(it.h, st)) return rc;
         if (*reinterpret_cast<volatile int *>(it.h->tc_status_host))  // written by an earlier call's kernels
@@ -785,22 +786,14 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
     const int ns = tc_splits(h0);
     size_t slot = 0;
     if (!first) SDBE_CK(h0, timed_begin(h0, 0, units_a, st, &slot));
-    if (ns == 2) {  // SDBE_PRECISION_TC16_FAST: packed spectra -> time series in one launch (k_tcf.cu)
-        std::vector<TcfASeg> segs;
-        for (const auto &it : w)
-            segs.push_back(TcfASeg{it.spec, it.spec_pol_stride, it.b0 * kBatchSnaps, it.nb * kBatchSnaps,
-                                   it.h->ts, it.h->ts_pol_stride});
-        if (int rc = tcf_stage_a(h0, segs.data(), static_cast<int>(segs.size()), 2, st)) return rc;
-    } else {
-        for (const auto &it : w) {  // stage A pairing: packed spectra -> Z (bufx)
-            const int64_t snaps = it.nb * kBatchSnaps;
-            k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(it.spec, it.spec_pol_stride,
-                                                                          it.b0 * kBatchSnaps, snaps, it.h->tc_bufx,
-                                                                          tw.w32768);
-            SDBE_CK(it.h, cudaGetLastError());
-        }
-        SDBE_CK(h0, (launch_tc_fft<128, true>(A, ns, st)));  // -> time series (ts)
+    for (const auto &it : w) {  // stage A pairing: packed spectra -> Z (bufx)
+        const int64_t snaps = it.nb * kBatchSnaps;
+        k_tc_prep_a<<<static_cast<unsigned>(2 * snaps), 256, 0, st>>>(it.spec, it.spec_pol_stride,
+                                                                      it.b0 * kBatchSnaps, snaps, it.h->tc_bufx,
+                                                                      tw.w32768);
+        SDBE_CK(it.h, cudaGetLastError());
     }
+    SDBE_CK(h0, (launch_tc_fft<128, true>(A, ns, st)));  // -> time series (ts)
     if (!first) {
         SDBE_CK(h0, timed_end(h0, slot, st));
         SDBE_CK(h0, timed_begin(h0, 1, units_bc, st, &slot));
@@ -872,7 +865,7 @@ int tc_swarm_c2r(sdbe_resampler *h, const uint32_t *spec, int64_t n_snaps, float
     const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
     if (tc_splits(h) == 2) {  // SDBE_PRECISION_TC16_FAST: straight from the packed spectra (k_tcf.cu)
         const TcfASeg seg{spec, 0, 0, n_snaps, out, 0};
-        return tcf_stage_a(h, &seg, 1, 1, st);
+        return tcf_stage_a(h, &seg, 1, 1, false, st);
     }
     const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kBatchSnaps;
     for (int64_t s0 = 0; s0 < n_snaps; s0 += cap) {
@@ -890,6 +883,28 @@ int tc_resample_chunks(sdbe_resampler *h, const float *in, int64_t n_chunks, flo
     if (n_chunks <= 0) return SDBE_OK;
     if ((reinterpret_cast<uintptr_t>(in) & 7u) || (reinterpret_cast<uintptr_t>(out) & 15u))
         return fail(h, SDBE_ERR_ARG, "SDBE_PRECISION_TC16 needs 8-byte aligned input and 16-byte aligned output");
+    if (tc_splits(h) == 2) {  // SDBE_PRECISION_TC16_FAST (k_tcf.cu): FP16 copy of the input, stages B and C
+        if (int rc = tcf_prepare(h, st)) return rc;
+        const int64_t cap = 2 * static_cast<int64_t>(h->wave) * kChunks;
+        if (int rc = grow(h, reinterpret_cast<uint8_t **>(&h->tcf_half), &h->tcf_half_bytes, cap * kNB * 2,
+                          "the tensor-core FP16 input"))
+            return rc;
+        if (int rc = grow(h, reinterpret_cast<uint8_t **>(&h->tcf_bins), &h->tcf_bins_bytes, cap * kTcfBinsLen * 4,
+                          "the tensor-core bins"))
+            return rc;
+        for (int64_t c0 = 0; c0 < n_chunks; c0 += cap) {
+            const int64_t n = n_chunks - c0 < cap ? n_chunks - c0 : cap;
+            SDBE_CK(h, tcf_to_half(in + c0 * kNB, h->tcf_half, n * kNB, st));
+            TcfBCSeg b{};
+            b.ts = h->tcf_half;
+            b.bins = h->tcf_bins;
+            b.n_chunks = n;
+            b.skip = h->skip;
+            b.o.fout = out + c0 * kNC;
+            if (int rc = tcf_stage_bc(h, &b, 1, 1, 5, st)) return rc;
+        }
+        return SDBE_OK;
+    }
     if (int rc = tc_prepare(h, st)) return rc;
     const uint8_t *f128 = static_cast<const uint8_t *>(h->tc_f128);
     const uint8_t *f143 = static_cast<const uint8_t *>(h->tc_f143);

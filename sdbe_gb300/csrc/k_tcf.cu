@@ -1,32 +1,44 @@
-// The fast tensor-core form (SDBE_PRECISION_TC16_FAST): each transform runs
+// The fast tensor-core form (SDBE_PRECISION_TC16_FAST): every transform runs
 // as a chain of small DFT GEMMs on the 5th-generation tensor cores, with the
-// twiddle multiplications between them on the CUDA cores.
+// twiddles and index permutations between them on the CUDA cores.
 //
-// A 16384-point transform (stage A's C2R 32768; stage C) is radices 32 x 32 x
-// 16 in decimation in time: with k = 512 n1 + 16 n2 + n3 and
-// m = k1 + 32 k2 + 1024 k3,
-//   stage 1  rows n' = 16 n2 + n3 (512), DFT-32 over n1, twiddle W_16384^(n' k1)
-//   stage 2  rows (k1, n3)       (512), DFT-32 over n2, twiddle W_512^(n3 k2)
-//   stage 3  rows (k1, k2)      (1024), DFT-16 over n3, output z[m].
-// Every stage is D[row][col] = sum_k X[row][k] G[col][k]: X holds the data as
-// FP16 (re, im) pairs along K (the A operand, 128 rows per MMA), G the real
-// form of the complex DFT matrix split into FP16 hi and lo halves stacked along
-// N ([hi | lo], so the data is read from shared memory once per K-step), and
-// D accumulates in FP32 in tensor memory.  The epilogue adds the hi and lo
-// halves, applies the twiddles in FP32 and rounds the result to FP16 into the
-// next stage's operand (a transposition: each thread's row scatters into the
-// next stage's rows).  Operands use the 128-byte (K = 64) and 64-byte (K = 32)
-// swizzles, and the row orders of the three stages are chosen so that every
-// scatter is one shared-memory wavefront per warp.
+// Every GEMM stage is D[row][col] = sum_k X[row][k] G[col][k]: X holds the
+// data as FP16 (re, im) pairs along K (the A operand, 128 rows per MMA), G
+// the real form of the complex DFT matrix split into FP16 hi and lo halves
+// stacked along N ([hi | lo], so the data is read from shared memory once per
+// K-step), and D accumulates in FP32 in tensor memory.  The epilogue adds the
+// hi and lo halves, applies the twiddles in FP32 and rounds to FP16 into the
+// next stage's operand: a transposition in which each thread's row scatters
+// into the next stage's rows.  Row orders are chosen so that most scatters
+// take one shared-memory wavefront per warp.
 //
-// One CTA per SM: warp 0 issues the MMAs (one thread), warps 1-16 are four
-// epilogue groups of four warps (one per tensor-memory lane quarter); group g
-// drains accumulator slot g (128 columns), tiles taking the slots in turn.
-// Two operand buffers alternate, so a transform's next stage is written while
-// the tensor cores still run the current one, and the next transform's input
-// is written while the last stage of the current one runs.  Every mbarrier
-// wait is bounded: on time-out the kernel records the failure in `status`,
-// stops waiting and completes.
+// Kernels (one CTA per SM, persistent over items):
+//  * k_tcf_inv: a 16384-point inverse transform, radices 32 x 32 x 16 in
+//    decimation in time (k = 512 n1 + 16 n2 + n3, m = k1 + 32 k2 + 1024 k3):
+//      stage 1  rows n' = 16 n2 + n3 (512), DFT-32 over n1, twiddle W^(n' k1)
+//      stage 2  rows (k1, n3)       (512), DFT-32 over n2, twiddle W_512^(n3 k2)
+//      stage 3  rows (k1, k2)      (1024), DFT-16 over n3, output z[m].
+//    Stage A's C2R 32768 per snapshot (input: the packed 2-bit spectrum) and
+//    stage C's C2R 32768 per chunk (input: the R2C bins [skip, skip + 16384]
+//    of stage B); the C2R pairing of the 16385 bins into 16384 complex values
+//    is folded into the input step.
+//  * k_tcf_fwd: stage B's R2C 36608 per chunk, an 18304-point forward
+//    transform of z[p] = x[2p] + i x[2p + 1] in the prime-factor map
+//    18304 = 143 x 128 (143 = 11 x 13, 128 = 16 x 8): four stages DFT-16,
+//    DFT-8, DFT-11, DFT-13 with one twiddle, W_128^(n8 k16), after the first;
+//    then the R2C pairing and the trim to bins [skip, skip + 16384].
+//
+// Warp 0 issues the MMAs (one thread); warps 1-16 are four epilogue groups of
+// four warps, one per tensor-memory lane quarter; group g drains accumulator
+// slot g (128 columns), tiles taking the slots in turn.  Two operand buffers
+// alternate so that the tensor cores run one stage while the CUDA cores write
+// the next.  Every mbarrier wait is bounded: on time-out the kernel records
+// the failure in `status`, stops waiting and completes.
+//
+// Fixed power-of-two scales keep every FP16 operand below 2^16 in magnitude
+// for any 2-bit input (per-stage bounds from the input energy: Parseval and
+// Cauchy-Schwarz), and the outputs are scaled back exactly to cuFFT's
+// unnormalised convention.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -45,50 +57,225 @@ using namespace tc5;
 
 constexpr int kEpiWarps = 16;
 constexpr int kEpiThreads = 32 * kEpiWarps;
-constexpr int kThreadsA = 32 + kEpiThreads;
+constexpr int kThreads = 32 + kEpiThreads;
 constexpr uint32_t kTmemCols = 512;
 
-// ---- stage A: shared-memory map (bytes from a 1024-byte aligned base) ------
-constexpr uint32_t kOpBytes = 65536;                     // one operand buffer (16384 complex FP16)
-constexpr uint32_t kG32Bytes = 128 * 64 * 2;             // DFT-32, [hi | lo] x K 64
-constexpr uint32_t kG16Bytes = 64 * 32 * 2;              // DFT-16, [hi | lo] x K 32
-constexpr uint32_t kOffX0 = 0, kOffX1 = kOpBytes;
-constexpr uint32_t kOffG32 = 2 * kOpBytes;
-constexpr uint32_t kOffG16 = kOffG32 + kG32Bytes;
-constexpr uint32_t kOffStg = kOffG16 + kG16Bytes;        // packed spectrum of one snapshot (8 KB)
-constexpr uint32_t kOffTab = kOffStg + 8192;
+// Scales (powers of two, exact).  Stage A stores its time series x 2^-2
+// (|x| <= 32768 * 2 sqrt 2 < 2^17); stage B's four stages scale by 2^-2,
+// 2^-1, 2^-2, 2^-3 (a stage of radix r multiplies the energy by r, and a
+// chunk's energy is at most 2 * 32768^2 * 8 before stage A's scale); stage C
+// halves its C2R pairing and scales its stages 1 and 2 by 2^-5.
+constexpr float kScaleA = 0.25f;
+constexpr float kScaleB1 = 0.25f, kScaleB2 = 0.5f, kScaleB3 = 0.25f, kScaleB4 = 0.125f;
+constexpr float kScaleC1 = 1.f / 32.f, kScaleC2 = 1.f / 32.f;
+// stage C output x 2^21 = back to the unnormalised value (2^-2 * 2^-8 * 2^-1 * 2^-10)
+constexpr float kUnscaleC = 2097152.f;
+
+// ---- shared memory of k_tcf_inv (bytes from a 1024-byte aligned base) -----
+constexpr uint32_t kOpBytes = 65536;                // one operand buffer (16384 complex FP16)
+constexpr uint32_t kG32Bytes = 128 * 64 * 2;        // DFT-32, [hi | lo] x K 64
+constexpr uint32_t kG16Bytes = 64 * 32 * 2;         // DFT-16, [hi | lo] x K 32
+constexpr uint32_t kInvOffG = 2 * kOpBytes;
+constexpr uint32_t kInvOffStg = kInvOffG + kG32Bytes + kG16Bytes;
 // float2 tables: e^{2 pi i n1/64} (n1 <= 16, 32 slots), e^{2 pi i n'/32768} (512),
 // e^{2 pi i n'/16384} (512), e^{2 pi i n3/512} (16)
-constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 512, kTabLen = kTabC + 16;
-constexpr uint32_t kSmemA = kOffTab + kTabLen * 8 + 1024;  // + alignment slack
+constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 512, kInvTabLen = kTabC + 16;
+constexpr uint32_t kStgPacked = 8192, kStgBins = kTcfBinsLen * 4;
+constexpr uint32_t inv_smem(bool bins) { return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + 1024; }
 
-struct SegTA {
-    const uint32_t *spec;     // packed spectra of the stream pair
-    void *out;                // time series [pol][snapshot][32768], float or half
-    int64_t spec_pol_stride;  // words
-    int64_t snap0, n_snaps;   // first snapshot, snapshots per pol
-    int64_t out_pol_stride;   // elements
-    int64_t item0;
-};
-struct ArgsTA {
-    int64_t n_items;
-    int n;
-    SegTA s[kMaxSegs];
-    const uint8_t *g;         // DFT-32 then DFT-16 matrices (inverse), pre-tiled
-    const float2 *tab;        // the kTabLen twiddle values
-    int *status;              // set to 1 on a barrier time-out (host-mapped)
-};
+// ---- shared memory of k_tcf_fwd --------------------------------------------
+constexpr uint32_t kFwdX0 = 90112;                  // raw chunk, DFT-8 operand, DFT-13 operand
+constexpr uint32_t kFwdX1 = 80896;                  // DFT-16 operand, DFT-11 operand (+128-byte tail), Z
+constexpr uint32_t kG16f = 64 * 32 * 2, kG8f = 32 * 16 * 2, kG11f = 64 * 32 * 2, kG13f = 64 * 32 * 2;
+constexpr uint32_t kFwdOffG = kFwdX0 + kFwdX1;
+constexpr uint32_t kFwdOffTab = kFwdOffG + kG16f + kG8f + kG11f + kG13f;
+// float2 tables: W_128^n8 (8), W_36608^(128 a) (a <= 143, 144 slots), W_36608^b (b < 128)
+constexpr int kTabW128 = 0, kTabQHi = 8, kTabQLo = kTabQHi + 144, kFwdTabLen = kTabQLo + 128;
+constexpr uint32_t kFwdSmem = kFwdOffTab + kFwdTabLen * 8 + 1024;
+static_assert(kFwdSmem <= 232448 && inv_smem(true) <= 232448, "shared memory above 227 KB");
 
-__device__ __forceinline__ const SegTA &seg_of(const ArgsTA &a, int64_t item) {
-    int j = 0;
-    while (j + 1 < a.n && item >= a.s[j + 1].item0) ++j;
-    return a.s[j];
-}
-
+// ---- device helpers --------------------------------------------------------
 __device__ __forceinline__ void named_sync_epi() { asm volatile("bar.sync 1, %0;" ::"r"(kEpiThreads) : "memory"); }
 
+__device__ __forceinline__ uint32_t sw32_off(int row, int kc) {
+    return static_cast<uint32_t>((row >> 3) * 256 + (row & 7) * 32 + ((((kc >> 2) ^ ((row & 7) >> 2)) & 1) << 4) +
+                                 (kc & 3) * 4);
+}
+// K-major, no swizzle, 3 core matrices (12 complex) per row group: the
+// DFT-11 operand.  Its second K-step also reads a 4th core matrix, which is
+// the next row group's first (finite data that meets zero columns of G).
+__device__ __forceinline__ uint32_t k24_off(int row, int kc) {
+    return static_cast<uint32_t>((row >> 3) * 384 + (kc >> 2) * 128 + (row & 7) * 16 + (kc & 3) * 4);
+}
+
+__device__ __forceinline__ float2 h2f(uint32_t w) {
+    const __half2 h = *reinterpret_cast<const __half2 *>(&w);
+    return __half22float2(h);
+}
+
+__device__ __forceinline__ float2 hilo(const uint32_t *hi, const uint32_t *lo, int i) {
+    return make_float2(__uint_as_float(hi[2 * i]) + __uint_as_float(lo[2 * i]),
+                       __uint_as_float(hi[2 * i + 1]) + __uint_as_float(lo[2 * i + 1]));
+}
+
+// Bulk copy global -> shared of `bytes` (multiple of 16), completing on mbar.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+// Common kernel state: barriers, tensor memory, error flag.
+struct Ctl {
+    uint64_t full[4], empty[4], ready[2], done, stg;
+    uint32_t tmem_base;
+    int err;
+};
+
+__device__ __forceinline__ void ctl_init(Ctl &c) {
+    for (int i = 0; i < 4; ++i) {
+        mbar_init(&c.full[i], 1);
+        mbar_init(&c.empty[i], 4);
+    }
+    mbar_init(&c.ready[0], kEpiWarps);
+    mbar_init(&c.ready[1], kEpiWarps);
+    mbar_init(&c.done, 1);
+    mbar_init(&c.stg, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    c.err = 0;
+}
+
+__device__ __forceinline__ bool err_set(const Ctl &c) { return *reinterpret_cast<const volatile int *>(&c.err) != 0; }
+__device__ __forceinline__ void raise_err(Ctl &c) { *reinterpret_cast<volatile int *>(&c.err) = 1; }
+
+// MMA issuer state (one thread).
+struct Issuer {
+    Ctl *c;
+    uint32_t tb, T = 0, uses[2] = {0, 0};
+    // One GEMM stage over `tiles` 128-row tiles of the operand in buffer buf
+    // (published on ready[buf]): per K-step one MMA of N columns into the
+    // tile's slot.
+    __device__ void stage(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, int ksteps, uint32_t kstep_bytes,
+                          uint32_t lbo, uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, int n) {
+        if (!err_set(*c) && !mbar_wait(&c->ready[buf], uses[buf] & 1u)) raise_err(*c);
+        ++uses[buf];
+        fence_after();
+        const uint32_t id = idesc_f16(128, n);
+        for (int j = 0; j < tiles; ++j, ++T) {
+            const uint32_t slot = T & 3u;
+            if (T >= 4 && !err_set(*c) && !mbar_wait(&c->empty[slot], ((T >> 2) - 1) & 1u)) raise_err(*c);
+            fence_after();
+            if (!err_set(*c)) {
+                const uint32_t d = tb + slot * 128;
+                for (int ks = 0; ks < ksteps; ++ks)
+                    mma_f16(d, desc(xa + j * tile_bytes + ks * kstep_bytes, lbo, sbo, layout),
+                            desc(g + ks * 256, 128, g_sbo, kNoSwizzle), id, ks > 0);
+            }
+            commit(&c->full[slot]);
+        }
+    }
+    __device__ void finish() {  // every MMA retired before tensor memory is freed
+        commit(&c->done);
+        if (!mbar_wait(&c->done, 0)) raise_err(*c);
+    }
+};
+
+// Epilogue warp state.
+struct Epi {
+    Ctl *c;
+    int lane, grp, q, et;
+    uint32_t tl;  // tensor-memory address of this warp's lane quarter in its group's slot
+    uint32_t T = 0, stg_uses = 0;
+    __device__ bool mine() const { return static_cast<int>(T & 3u) == grp; }
+    __device__ void wait_tile() {
+        if (!err_set(*c) && !mbar_wait(&c->full[T & 3u], (T >> 2) & 1u)) raise_err(*c);
+        fence_after();
+    }
+    __device__ void release_tile() {
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&c->empty[T & 3u]);
+    }
+    __device__ void publish(int buf) {  // this warp's part of an operand is written
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&c->ready[buf]);
+    }
+    __device__ void wait_staging() {
+        if (!err_set(*c) && !mbar_wait(&c->stg, stg_uses & 1u)) raise_err(*c);
+        ++stg_uses;
+    }
+    // Runs f(j) on this group's tiles of a stage of n tiles.
+    template <class F>
+    __device__ void tiles(int n, F f) {
+        for (int j = 0; j < n; ++j, ++T)
+            if (mine()) {
+                wait_tile();
+                f(j);
+                release_tile();
+            }
+    }
+};
+
+__device__ __forceinline__ void tmem_alloc_all(Ctl &c, int warp) {
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&c.tmem_base)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+}
+
+__device__ __forceinline__ void teardown(Ctl &c, int *status, int warp) {
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && err_set(c)) *reinterpret_cast<volatile int *>(status) = 1;
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem_base), "r"(kTmemCols));
+}
+
+template <class A>
+__device__ __forceinline__ int seg_index(const A &a, int64_t item) {
+    int j = 0;
+    while (j + 1 < a.n && item >= a.s[j + 1].item0) ++j;
+    return j;
+}
+
+// 8 TMEM columns of this thread's lane, no wait.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
+// ============================================================================
+// k_tcf_inv: 16384-point inverse transforms (stages A and C)
+// ============================================================================
+enum : int { IN_PACKED = 0, IN_BINS = 1 };
+enum : int { OUT_TS_HALF = 0, OUT_TS_FLOAT = 1, OUT_QUANT = 2, OUT_FLOAT_MOMENTS = 3, OUT_QUANT_SUMS = 4, OUT_FLOAT = 5 };
+
+struct SegInv {
+    const void *in;          // packed spectra (u32 words) or R2C bins (half2, kTcfBinsLen per chunk)
+    void *out;               // stage A: time series [pol][n][32768], half or float
+    int64_t in_pol_stride;   // words (packed) or bins
+    int64_t first, n;        // first snapshot (packed input), items per pol
+    int64_t out_pol_stride;  // elements
+    int64_t item0;
+    ResampleOut o;           // stage C: payload target, thresholds, floats, partials
+};
+struct ArgsInv {
+    int64_t n_items;
+    int n;
+    SegInv s[kMaxSegs];
+    const uint8_t *g;        // inverse DFT-32 then DFT-16 matrices, pre-tiled
+    const float2 *tab;       // the kInvTabLen twiddle values
+    int *status;             // set to 1 on a barrier time-out (host-mapped)
+};
+
 // Staged packed spectrum: word w at w ^ ((w >> 6) & 1) ^ (((w >> 7) & 1) << 4),
-// so that the input stage's 32 lanes (8 values of n2 % 8 x 4 of n1 % 4) read
+// so that the input step's 32 lanes (8 values of n2 % 8 x 4 of n1 % 4) read
 // 32 distinct banks.
 __device__ __forceinline__ uint32_t stg_pos(uint32_t w) { return w ^ ((w >> 6) & 1u) ^ (((w >> 7) & 1u) << 4); }
 
@@ -99,161 +286,175 @@ __device__ __forceinline__ float2 stg_value(const uint32_t *stg, int k) {
     return make_float2(re, im);
 }
 
-// Packed spectrum of an item (segment, pol, snapshot; items are pol-major
-// within a segment and a segment holds at most two pols).
-__device__ __forceinline__ const uint32_t *item_spec(const ArgsTA &a, int64_t item) {
-    const SegTA &s = seg_of(a, item);
-    const int64_t local = item - s.item0;
-    const int64_t pol = local >= s.n_snaps ? 1 : 0, loc = local - pol * s.n_snaps;
-    return s.spec + pol * s.spec_pol_stride + (s.snap0 + loc) * kGroups;
-}
-
-template <bool OUT_HALF>
-__global__ void __launch_bounds__(kThreadsA, 1) k_tcf_a(const __grid_constant__ ArgsTA a) {
+template <int IN, int OUT>
+__global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
+    constexpr bool kBins = IN == IN_BINS;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    auto X = [sm](int buf) { return sm + (buf ? kOffX1 : kOffX0); };  // operand buffers
-    uint32_t *stg = reinterpret_cast<uint32_t *>(sm + kOffStg);
-    float2 *tab = reinterpret_cast<float2 *>(sm + kOffTab);
-    __shared__ __align__(8) uint64_t full[4], empty[4], ready[2], done;
-    __shared__ uint32_t tmem_base;
-    __shared__ volatile int s_err;
+    auto X = [sm](int buf) { return sm + (buf ? kOpBytes : 0u); };
+    uint32_t *stg = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
+    float2 *tab = reinterpret_cast<float2 *>(sm + kInvOffStg + (kBins ? kStgBins : kStgPacked));
+    __shared__ __align__(8) Ctl ctl;
+    __shared__ double red[2 * kEpiWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    if (tid == 0) {
-        for (int i = 0; i < 4; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], 4);
-        }
-        mbar_init(&ready[0], kEpiWarps);
-        mbar_init(&ready[1], kEpiWarps);
-        mbar_init(&done, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_err = 0;
-    }
-    // DFT matrices and twiddle tables into shared memory
+    if (tid == 0) ctl_init(ctl);
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.g);
-        uint4 *dst = reinterpret_cast<uint4 *>(sm + kOffG32);
-        for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kThreadsA) dst[i] = __ldg(src + i);
-        for (int i = tid; i < kTabLen; i += kThreadsA) tab[i] = __ldg(a.tab + i);
+        uint4 *dst = reinterpret_cast<uint4 *>(sm + kInvOffG);
+        for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kThreads) dst[i] = __ldg(src + i);
+        for (int i = tid; i < kInvTabLen; i += kThreads) tab[i] = __ldg(a.tab + i);
     }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(kTmemCols));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
+    tmem_alloc_all(ctl, warp);
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tb = tmem_base;
+    const uint32_t tb = ctl.tmem_base;
 
     if (warp == 0) {
-        // ---- MMA issuer ------------------------------------------------------
         if (lane == 0) {
-            uint32_t T = 0, uses[2] = {0, 0};
-            const uint32_t g32 = smem_u32(sm + kOffG32), g16 = smem_u32(sm + kOffG16);
-            auto stage = [&](int buf, int tiles, uint32_t tile_bytes, int ksteps, uint32_t sbo, uint32_t layout,
-                             uint32_t g, uint32_t g_sbo, int n) {
-                if (!s_err && !mbar_wait(&ready[buf], uses[buf] & 1u)) s_err = 1;
-                ++uses[buf];
-                fence_after();
-                const uint32_t xa = smem_u32(X(buf));
-                const uint32_t id = idesc_f16(128, n);
-                for (int j = 0; j < tiles; ++j, ++T) {
-                    const uint32_t slot = T & 3u;
-                    if (T >= 4 && !s_err && !mbar_wait(&empty[slot], ((T >> 2) - 1) & 1u)) s_err = 1;
-                    fence_after();
-                    if (!s_err) {
-                        const uint32_t d = tb + slot * 128;
-                        for (int ks = 0; ks < ksteps; ++ks)
-                            mma_f16(d, desc(xa + j * tile_bytes + ks * 32, 16, sbo, layout),
-                                    desc(g + ks * 256, 128, g_sbo, kNoSwizzle), id, ks > 0);
-                    }
-                    commit(&full[slot]);
-                }
-            };
+            Issuer is{&ctl, tb};
+            const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
             int p = 0;
             for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-                stage(p, 4, 16384, 4, 1024, kSwizzle128, g32, 1024, 128);      // DFT-32 over n1
-                stage(p ^ 1, 4, 16384, 4, 1024, kSwizzle128, g32, 1024, 128);  // DFT-32 over n2
-                stage(p, 8, 8192, 2, 512, kSwizzle64, g16, 512, 64);           // DFT-16 over n3
+                is.stage(p, smem_u32(X(p)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 128);
+                is.stage(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 128);
+                is.stage(p, smem_u32(X(p)), 8, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 64);
             }
-            commit(&done);  // every MMA retired before tensor memory is freed
-            if (!mbar_wait(&done, 0)) s_err = 1;
+            is.finish();
         }
         __syncwarp();
     } else {
-        // ---- epilogue warps -------------------------------------------------------
-        const int e = warp - 1, grp = e >> 2, q = warp & 3;
-        const int et = e * 32 + lane;  // 0 .. 511
-        const uint32_t tl = tb + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(grp) * 128;
-        uint32_t T = 0;
-        auto wait_tile = [&](uint32_t t) {
-            if (!s_err && !mbar_wait(&full[t & 3u], (t >> 2) & 1u)) s_err = 1;
-            fence_after();
+        Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
+               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>((warp - 1) >> 2) * 128};
+        const int e = warp - 1, q = ep.q, et = ep.et;
+        const uint32_t tl = ep.tl;
+
+        // ---- input staging ---------------------------------------------------
+        uint4 pre = make_uint4(0, 0, 0, 0);  // packed input: next snapshot, 16 bytes per thread
+        auto item_in = [&](int64_t item) -> const void * {
+            const SegInv &s = a.s[seg_index(a, item)];
+            const int64_t local = item - s.item0;
+            const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
+            if constexpr (kBins)
+                return static_cast<const uint32_t *>(s.in) + (pol * s.in_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen));
+            else
+                return static_cast<const uint32_t *>(s.in) + pol * s.in_pol_stride + (s.first + loc) * kGroups;
         };
-        auto release_tile = [&](uint32_t t) {
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[t & 3u]);
+        auto fetch = [&](int64_t item) {  // start bringing the item's input in
+            if (item >= a.n_items) return;
+            if constexpr (kBins) {
+                if (et == 0) {
+                    fence_async_smem();
+                    bulk_g2s(stg, item_in(item), kStgBins, &ctl.stg);
+                }
+            } else {
+                pre = __ldg(reinterpret_cast<const uint4 *>(item_in(item)) + et);
+            }
         };
-        auto publish = [&](int buf) {  // this warp's part of an operand is written
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&ready[buf]);
+        auto land = [&]() {  // the fetched input is in shared memory (all epilogue threads)
+            if constexpr (kBins) {
+                ep.wait_staging();
+            } else {
+                const uint32_t w = 4u * static_cast<uint32_t>(et);
+                const uint32_t u0 = (w >> 6) & 1u, u1 = (w >> 7) & 1u;
+                uint4 v = pre;
+                if (u0) v = make_uint4(pre.y, pre.x, pre.w, pre.z);
+                *reinterpret_cast<uint4 *>(stg + (w ^ (u1 << 4))) = v;
+                named_sync_epi();
+            }
         };
-        // next snapshot's packed spectrum, 16 bytes per thread, held in registers
-        uint4 pre = make_uint4(0, 0, 0, 0);
-        auto prefetch = [&](int64_t item) {
-            if (item < a.n_items) pre = __ldg(reinterpret_cast<const uint4 *>(item_spec(a, item)) + et);
-        };
-        auto stage_spectrum = [&]() {  // registers -> swizzled staging buffer
-            const uint32_t w = 4u * static_cast<uint32_t>(et);
-            const uint32_t u0 = (w >> 6) & 1u, u1 = (w >> 7) & 1u;
-            uint4 v = pre;
-            if (u0) v = make_uint4(pre.y, pre.x, pre.w, pre.z);
-            *reinterpret_cast<uint4 *>(stg + (w ^ (u1 << 4))) = v;
-        };
-        // C2R pairing into the stage-1 operand: Z[k] and Z[16384 - k] for
-        // k = 512 n1 + 16 n2 + n3, n3 = this warp, (n2 % 8, n1 % 4) = this lane
+
+        // ---- input step: C2R pairing into the stage-1 operand -------------------
+        // Packed input (stage A): row n' = 16 n2 + n3 at 32 n3 + n2; thread:
+        // n3 = its warp, (n2 % 8, n1 % 4) = its lane.  Bins input (stage C): rows
+        // in natural order n'; thread: n' = et, four consecutive n1 per store.
         auto input = [&](int buf) {
             uint8_t *op = X(buf);
-            const int n3 = e;
+            if constexpr (!kBins) {
+                const int n3 = e;
 #pragma unroll 1
-            for (int it = 0; it < 16; ++it) {
-                const int n1 = 4 * (it >> 2) + (lane >> 3), n2 = 8 * (it & 3) + (lane & 7);
-                const int np = 16 * n2 + n3, k = 512 * n1 + np;
-                float2 y = stg_value(stg, k);
-                float2 ym = make_float2(0.f, 0.f);
-                const int km = kMA - k;
-                if (k == 0)
-                    y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
-                else
-                    ym = stg_value(stg, km);
-                float2 zk, zm;
-                c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
-                *reinterpret_cast<uint32_t *>(op + sw128_off(32 * n3 + n2, n1)) = pack_half2(zk.x, zk.y);
-                if (k != 0) {
-                    const int n1m = km >> 9, npm = km & 511;
-                    *reinterpret_cast<uint32_t *>(op + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
-                        pack_half2(zm.x, zm.y);
+                for (int it = 0; it < 16; ++it) {
+                    const int n1 = 4 * (it >> 2) + (lane >> 3), n2 = 8 * (it & 3) + (lane & 7);
+                    const int np = 16 * n2 + n3, k = 512 * n1 + np;
+                    float2 y = stg_value(stg, k);
+                    float2 ym = make_float2(0.f, 0.f);
+                    const int km = kMA - k;
+                    if (k == 0)
+                        y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
+                    else
+                        ym = stg_value(stg, km);
+                    float2 zk, zm;
+                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(op + sw128_off(32 * n3 + n2, n1)) = pack_half2(zk.x, zk.y);
+                    if (k != 0) {
+                        const int n1m = km >> 9, npm = km & 511;
+                        *reinterpret_cast<uint32_t *>(op + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
+                            pack_half2(zm.x, zm.y);
+                    }
+                }
+                if (et == 0) {  // k = 8192, its own mirror
+                    const float2 y = stg_value(stg, kMA / 2);
+                    float2 zk, zm;
+                    c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
+                }
+            } else {
+                const int np = et;
+                const float2 wb = tab[kTabA2 + np];
+#pragma unroll 1
+                for (int c = 0; c < 4; ++c) {
+                    uint32_t zk[4], zm[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int n1 = 4 * c + i, k = 512 * n1 + np;
+                        float2 y = h2f(stg[k]), ym = h2f(stg[kMA - k]);
+                        if (k == 0) {  // Im of bins 0 and 16384 are ignored (C2R)
+                            y.y = 0.f;
+                            ym.y = 0.f;
+                        }
+                        y = make_float2(0.5f * y.x, 0.5f * y.y);
+                        ym = make_float2(0.5f * ym.x, 0.5f * ym.y);
+                        float2 a0, a1;
+                        c2r_pair(y, ym, cmul(tab[kTabA1 + n1], wb), a0, a1);
+                        zk[i] = pack_half2(a0.x, a0.y);
+                        zm[i] = pack_half2(a1.x, a1.y);
+                    }
+                    *reinterpret_cast<uint4 *>(op + sw128_off(np, 4 * c)) = make_uint4(zk[0], zk[1], zk[2], zk[3]);
+                    if (np != 0) {  // mirrors 16384 - k: row 512 - n', K 31 - n1 (a 4-aligned group, reversed)
+                        *reinterpret_cast<uint4 *>(op + sw128_off(512 - np, 28 - 4 * c)) =
+                            make_uint4(zm[3], zm[2], zm[1], zm[0]);
+                    } else {  // row 0: 16384 - 512 n1 lies at K 32 - n1; n1 = 0 mirrors the Nyquist bin
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            if (4 * c + i > 0)
+                                *reinterpret_cast<uint32_t *>(op + sw128_off(0, 32 - 4 * c - i)) = zm[i];
+                    }
+                }
+                if (et == 0) {  // k = 8192, its own mirror
+                    float2 y = h2f(stg[kMA / 2]);
+                    y = make_float2(0.5f * y.x, 0.5f * y.y);
+                    float2 zk, zm;
+                    c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
                 }
             }
-            if (et == 0) {  // k = 8192, its own mirror
-                const float2 y = stg_value(stg, kMA / 2);
-                float2 zk, zm;
-                c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
-                *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
-            }
         };
-        // Stage 1 -> stage-2 operand.  Row n' = 16 lane + n3 (n3 = 4 j + q),
-        // column k1; stage-2 row 16 k1 + n3, K index n2 = lane.
+
+        // ---- stage 1 -> stage-2 operand (row 16 k1 + n3, K n2) --------------------
         auto epi1 = [&](int j, uint8_t *dst) {
-            const int n3 = 4 * j + q, np = 16 * lane + n3;
-            const float2 b = tab[kTabB + np];
-            float2 w = make_float2(1.f, 0.f);
+            int n2, n3;
+            if constexpr (!kBins) {  // row n' = 16 lane + n3, n3 = 4 j + q
+                n3 = 4 * j + q;
+                n2 = lane;
+            } else {                 // natural rows: n' = 128 j + 32 q + lane
+                const int np = 128 * j + 32 * q + lane;
+                n3 = np & 15;
+                n2 = np >> 4;
+            }
+            const float2 b = tab[kTabB + 16 * n2 + n3];
+            float2 w = make_float2(kBins ? kScaleC1 : 1.f, 0.f);
 #pragma unroll
             for (int h = 0; h < 4; ++h) {  // k1 in [8h, 8h + 8)
                 uint32_t hi[16], lo[16];
@@ -263,20 +464,17 @@ __global__ void __launch_bounds__(kThreadsA, 1) k_tcf_a(const __grid_constant__ 
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int k1 = 8 * h + i;
-                    const float2 v = make_float2(__uint_as_float(hi[2 * i]) + __uint_as_float(lo[2 * i]),
-                                                 __uint_as_float(hi[2 * i + 1]) + __uint_as_float(lo[2 * i + 1]));
-                    const float2 y = cmul(v, w);
+                    const float2 y = cmul(hilo(hi, lo, i), w);
                     w = cmul(w, b);
-                    *reinterpret_cast<uint32_t *>(dst + sw128_off(16 * k1 + n3, lane)) = pack_half2(y.x, y.y);
+                    *reinterpret_cast<uint32_t *>(dst + sw128_off(16 * k1 + n3, n2)) = pack_half2(y.x, y.y);
                 }
             }
         };
-        // Stage 2 -> stage-3 operand.  Row 16 k1 + n3 = 128 j + 32 q + lane,
-        // column k2; stage-3 row 32 k2 + k1, K index n3.
+        // ---- stage 2 -> stage-3 operand (row 32 k2 + k1, K n3) --------------------
         auto epi2 = [&](int j, uint8_t *dst) {
             const int r = 128 * j + 32 * q + lane, k1 = r >> 4, n3 = r & 15;
             const float2 b = tab[kTabC + n3];
-            float2 w = make_float2(1.f, 0.f);
+            float2 w = make_float2(kBins ? kScaleC2 : 1.f, 0.f);
 #pragma unroll
             for (int h = 0; h < 4; ++h) {
                 uint32_t hi[16], lo[16];
@@ -286,19 +484,268 @@ __global__ void __launch_bounds__(kThreadsA, 1) k_tcf_a(const __grid_constant__ 
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int k2 = 8 * h + i;
-                    const float2 v = make_float2(__uint_as_float(hi[2 * i]) + __uint_as_float(lo[2 * i]),
-                                                 __uint_as_float(hi[2 * i + 1]) + __uint_as_float(lo[2 * i + 1]));
-                    const float2 y = cmul(v, w);
+                    const float2 y = cmul(hilo(hi, lo, i), w);
                     w = cmul(w, b);
                     *reinterpret_cast<uint32_t *>(dst + sw64_off(32 * k2 + k1, n3)) = pack_half2(y.x, y.y);
                 }
             }
         };
-        // Stage 3 -> output.  Row 32 k2 + k1 = 128 j + 32 q + lane, column k3:
-        // z[k1 + 32 k2 + 1024 k3] = (x[2m], x[2m+1]); a warp stores 32
+        // ---- stage 3 -> output.  Row 32 k2 + k1 = 128 j + 32 q + lane, column k3:
+        // z[m], m = k1 + 32 k2 + 1024 k3, = samples (2m, 2m + 1); a warp covers 32
         // consecutive m.
-        auto epi3 = [&](int j, void *out) {
+        float f1 = 0.f, f2 = 0.f;  // OUT_QUANT_SUMS: this thread's sums over the chunk
+        double d1 = 0.0, d2 = 0.0; // OUT_FLOAT_MOMENTS
+        auto epi3 = [&](int j, const SegInv &s, int64_t pol, int64_t loc) {
             const int r = 128 * j + 32 * q + lane;
+            float2 v[16];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                uint32_t hi[16], lo[16];
+                tmem_ld16(tl + 16 * h, hi);
+                tmem_ld16(tl + 32 + 16 * h, lo);
+                tmem_wait<16>(hi, lo);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[8 * h + i] = hilo(hi, lo, i);
+            }
+            if constexpr (OUT == OUT_TS_HALF || OUT == OUT_TS_FLOAT) {
+                const int64_t off = pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int m = r + 1024 * i;
+                    if constexpr (OUT == OUT_TS_HALF)
+                        __stcs(reinterpret_cast<unsigned int *>(static_cast<__half *>(s.out) + off) + m,
+                               pack_half2(kScaleA * v[i].x, kScaleA * v[i].y));
+                    else
+                        __stcs(reinterpret_cast<float2 *>(static_cast<float *>(s.out) + off) + m, v[i]);
+                }
+            } else if constexpr (OUT == OUT_FLOAT || OUT == OUT_FLOAT_MOMENTS) {
+                float2 *fo = reinterpret_cast<float2 *>(s.o.fout + pol * s.o.fout_pol_stride + loc * kNC);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const float2 x = make_float2(kUnscaleC * v[i].x, kUnscaleC * v[i].y);
+                    __stcs(fo + r + 1024 * i, x);
+                    if constexpr (OUT == OUT_FLOAT_MOMENTS) {
+                        d1 += static_cast<double>(x.x) + static_cast<double>(x.y);
+                        d2 += static_cast<double>(x.x) * x.x + static_cast<double>(x.y) * x.y;
+                    }
+                }
+            } else {  // 2-bit codes: sample 2m at bits 4 (m % 8) of word m / 8 (m % 8 = lane % 8)
+                uint32_t *words = reinterpret_cast<uint32_t *>(s.o.out + pol * s.o.out_pol_stride +
+                                                               (s.o.pkt0 + loc) * s.o.pkt_stride + s.o.payload_off);
+                const float th = s.o.thr[pol], off = s.o.thr[2 + pol];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const float2 x = make_float2(kUnscaleC * v[i].x, kUnscaleC * v[i].y);
+                    if constexpr (OUT == OUT_QUANT_SUMS) {
+                        f1 += x.x + x.y;
+                        f2 = fmaf(x.x, x.x, fmaf(x.y, x.y, f2));
+                    }
+                    uint32_t nib = (code2(x.x, th, off) | (code2(x.y, th, off) << 2)) << (4 * (lane & 7));
+                    nib |= __shfl_xor_sync(0xffffffffu, nib, 1);
+                    nib |= __shfl_xor_sync(0xffffffffu, nib, 2);
+                    nib |= __shfl_xor_sync(0xffffffffu, nib, 4);
+                    if ((lane & 7) == 0) words[(r + 1024 * i) >> 3] = nib;
+                }
+            }
+        };
+        // Per-chunk statistics of stage C (all epilogue warps, after stage 3).
+        auto chunk_stats = [&](const SegInv &s, int64_t pol, int64_t loc) {
+            if constexpr (OUT == OUT_FLOAT_MOMENTS || OUT == OUT_QUANT_SUMS) {
+                if (s.o.partials == nullptr) return;
+                double s1, s2;
+                if constexpr (OUT == OUT_FLOAT_MOMENTS) {
+                    s1 = warp_sum(d1);
+                    s2 = warp_sum(d2);
+                } else {
+                    s1 = static_cast<double>(warp_sum_f(f1));
+                    s2 = static_cast<double>(warp_sum_f(f2));
+                }
+                if (lane == 0) {
+                    red[e] = s1;
+                    red[kEpiWarps + e] = s2;
+                }
+                named_sync_epi();
+                if (et == 0) {
+                    double t1 = 0.0, t2 = 0.0;
+                    for (int w = 0; w < kEpiWarps; ++w) {
+                        t1 += red[w];
+                        t2 += red[kEpiWarps + w];
+                    }
+                    double *pp = s.o.partials + (pol * s.n + loc) * 3;
+                    const double nn = static_cast<double>(kNC);
+                    pp[0] = nn;
+                    if constexpr (OUT == OUT_FLOAT_MOMENTS) {
+                        pp[1] = t1 / nn;
+                        pp[2] = t2 - t1 * (t1 / nn);
+                    } else {
+                        pp[1] = t1;
+                        pp[2] = t2;
+                    }
+                }
+                named_sync_epi();  // red reusable
+                d1 = d2 = 0.0;
+                f1 = f2 = 0.f;
+            }
+        };
+
+        int p = 0;
+        if (blockIdx.x < a.n_items) {
+            fetch(blockIdx.x);
+            land();
+            input(0);
+            ep.publish(0);
+            named_sync_epi();  // the staging buffer is free again
+            fetch(blockIdx.x + gridDim.x);
+        }
+        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
+            ep.tiles(4, [&](int j) { epi1(j, X(p ^ 1)); });
+            ep.publish(p ^ 1);
+            ep.tiles(4, [&](int j) { epi2(j, X(p)); });
+            ep.publish(p);
+            // every stage-2 MMA has retired (each group saw its tiles' commits),
+            // so operand p ^ 1 takes the next item's input
+            named_sync_epi();
+            const int64_t next = item + gridDim.x;
+            if (next < a.n_items) {
+                land();
+                input(p ^ 1);
+                ep.publish(p ^ 1);
+                named_sync_epi();
+                fetch(next + gridDim.x);
+            }
+            const SegInv &s = a.s[seg_index(a, item)];
+            const int64_t local = item - s.item0;
+            const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
+            ep.tiles(8, [&](int j) { epi3(j, s, pol, loc); });
+            chunk_stats(s, pol, loc);
+        }
+    }
+    teardown(ctl, a.status, warp);
+}
+
+// ============================================================================
+// k_tcf_fwd: stage B, R2C 36608 per chunk -> bins [skip, skip + 16384]
+// ============================================================================
+// Index maps (N = 18304 = 143 x 128): n = (128 nA + 143 nB) mod N with
+// nA = (13 n11 + 11 n13) mod 143 and nB = 8 n16 + n8; the output bin k has
+// k mod 143 = kA with kA mod 11 = k11, kA mod 13 = k13, and k mod 128 =
+// k16 + 16 k8, i.e. k = (2432 kA + 15873 kB) mod N.  Rows are labelled by
+// nA' = 13 n11 + n13 (a relabelling of nA).
+//   B1  DFT-16 over n16: rows 8 nA' + n8        (1144 in 9 tiles), K n16 (64-byte swizzle)
+//       twiddle W_128^(n8 k16)
+//   B2  DFT-8 over n8:   rows nA' + 143 k16     (2288 in 18 tiles), K n8 (32-byte swizzle)
+//   B3  DFT-11 over n11: rows n13 + 13 kB       (1664 in 13 tiles), K n11 (3 core matrices)
+//   B4  DFT-13 over n13: rows 128 k11 + kB      (1408 in 11 tiles), K n13 (64-byte swizzle)
+//   Z[k] in natural order -> R2C pairing -> bins [skip, skip + 16384] (FP16) to global.
+struct SegFwd {
+    const __half *in;        // time series x 2^-2, [pol][chunks][36608]
+    uint32_t *out;           // bins (half2) [pol][chunks][kTcfBinsLen]
+    int64_t in_pol_stride;   // halves
+    int64_t out_pol_stride;  // bins
+    int64_t n, item0;        // chunks per pol
+    int skip;
+};
+struct ArgsFwd {
+    int64_t n_items;
+    int n;
+    SegFwd s[kMaxSegs];
+    const uint8_t *g;        // forward DFT-16, DFT-8, DFT-11, DFT-13 matrices, pre-tiled
+    const float2 *tab;       // the kFwdTabLen twiddle values
+    int *status;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__ ArgsFwd a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    uint8_t *X0 = sm, *X1 = sm + kFwdX0;
+    float2 *tab = reinterpret_cast<float2 *>(sm + kFwdOffTab);
+    __shared__ __align__(8) Ctl ctl;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) ctl_init(ctl);
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.g);
+        uint4 *dst = reinterpret_cast<uint4 *>(sm + kFwdOffG);
+        for (int i = tid; i < static_cast<int>((kG16f + kG8f + kG11f + kG13f) / 16); i += kThreads)
+            dst[i] = __ldg(src + i);
+        for (int i = tid; i < kFwdTabLen; i += kThreads) tab[i] = __ldg(a.tab + i);
+        // operands start finite (padding rows and K columns are read, against zero G entries)
+        uint4 *z = reinterpret_cast<uint4 *>(sm);
+        for (int i = tid; i < static_cast<int>((kFwdX0 + kFwdX1) / 16); i += kThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    tmem_alloc_all(ctl, warp);
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tb = ctl.tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            Issuer is{&ctl, tb};
+            const uint32_t g16 = smem_u32(sm + kFwdOffG), g8 = g16 + kG16f, g11 = g8 + kG8f, g13 = g11 + kG11f;
+            const uint32_t x0 = smem_u32(X0), x1 = smem_u32(X1);
+            for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+                is.stage(1, x1, 9, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 64);     // DFT-16
+                is.stage(0, x0, 18, 4096, 1, 32, 16, 256, kSwizzle32, g8, 256, 32);     // DFT-8
+                is.stage(1, x1, 13, 6144, 2, 256, 128, 384, kNoSwizzle, g11, 512, 64);  // DFT-11
+                is.stage(0, x0, 11, 8192, 2, 32, 16, 512, kSwizzle64, g13, 512, 64);    // DFT-13
+            }
+            is.finish();
+        }
+        __syncwarp();
+    } else {
+        Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
+               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>((warp - 1) >> 2) * 128};
+        const int e = warp - 1, q = ep.q, et = ep.et;
+        const uint32_t tl = ep.tl;
+        const uint32_t *raw = reinterpret_cast<const uint32_t *>(X0);
+        uint32_t *Z = reinterpret_cast<uint32_t *>(X1);
+
+        auto item_pos = [&](int64_t item, int64_t &pol, int64_t &loc) -> int {
+            const int si = seg_index(a, item);
+            const int64_t local = item - a.s[si].item0;
+            pol = local >= a.s[si].n ? 1 : 0;
+            loc = local - pol * a.s[si].n;
+            return si;
+        };
+        auto fetch = [&](int64_t item) {  // the item's 36608 FP16 samples -> X0 (73,216 bytes)
+            if (item >= a.n_items || et != 0) return;
+            int64_t pol, loc;
+            const SegFwd &s = a.s[item_pos(item, pol, loc)];
+            fence_async_smem();
+            bulk_g2s(X0, s.in + pol * s.in_pol_stride + loc * static_cast<int64_t>(kNB), kNB * 2, &ctl.stg);
+        };
+        // input step: raw (natural order) -> DFT-16 operand.  Thread: row
+        // (nA' = 4 w + lane / 8, n8 = lane % 8); its 16 gathers start at
+        // n16 = lane / 8 so that a warp's loads and stores hit 32 banks.
+        auto input = [&]() {
+#pragma unroll 1
+            for (int w = e; w < 36; w += kEpiWarps) {
+                const int nAp = 4 * w + (lane >> 3), n8 = lane & 7;
+                if (nAp >= 143) continue;
+                const int n11 = nAp / 13, n13 = nAp - 13 * n11;
+                int nA = 13 * n11 + 11 * n13;
+                nA -= nA >= 143 ? 143 : 0;
+                nA -= nA >= 143 ? 143 : 0;
+                int base = 128 * nA + 143 * n8;
+                base -= base >= kMB ? kMB : 0;
+                const int row = 8 * nAp + n8;
+#pragma unroll 4
+                for (int i = 0; i < 16; ++i) {
+                    const int n16 = (i + (lane >> 3)) & 15;
+                    int n = base + 1144 * n16;
+                    n -= n >= kMB ? kMB : 0;
+                    *reinterpret_cast<uint32_t *>(X1 + sw64_off(row, n16)) = raw[n];
+                }
+            }
+        };
+        // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row nA' + 143 k16, K n8
+        auto epi1 = [&](int j) {
+            const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
+            const bool ok = nAp < 143;
+            const float2 b = tab[kTabW128 + n8];
+            float2 w = make_float2(kScaleB1, 0.f);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 uint32_t hi[16], lo[16];
@@ -307,91 +754,146 @@ __global__ void __launch_bounds__(kThreadsA, 1) k_tcf_a(const __grid_constant__ 
                 tmem_wait<16>(hi, lo);
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const int m = r + 1024 * (8 * h + i);
-                    const float re = __uint_as_float(hi[2 * i]) + __uint_as_float(lo[2 * i]);
-                    const float im = __uint_as_float(hi[2 * i + 1]) + __uint_as_float(lo[2 * i + 1]);
-                    if constexpr (OUT_HALF) {
-                        // a quarter of the unnormalised value: |x| < 32768 * 2 * sqrt(2) / 4 fits FP16
-                        __stcs(reinterpret_cast<unsigned int *>(out) + m, pack_half2(0.25f * re, 0.25f * im));
-                    } else {
-                        __stcs(reinterpret_cast<float2 *>(out) + m, make_float2(re, im));
-                    }
+                    const int k16 = 8 * h + i;
+                    const float2 y = cmul(hilo(hi, lo, i), w);
+                    w = cmul(w, b);
+                    if (ok) *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y.x, y.y);
                 }
             }
         };
-        auto out_ptr = [&](int64_t item) -> void * {
-            const SegTA &s = seg_of(a, item);
-            const int64_t local = item - s.item0;
-            const int64_t pol = local >= s.n_snaps ? 1 : 0, loc = local - pol * s.n_snaps;
-            const int64_t off = pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA);
-            return OUT_HALF ? static_cast<void *>(static_cast<__half *>(s.out) + off)
-                            : static_cast<void *>(static_cast<float *>(s.out) + off);
+        // B2: DFT-8 out (k8), rows nA' + 143 k16 -> B3 operand row n13 + 13 (k16 + 16 k8), K n11
+        auto epi2 = [&](int j) {
+            const int r = 128 * j + 32 * q + lane;
+            const bool ok = r < 2288;
+            const int k16 = r / 143, nAp = r - 143 * k16, n11 = nAp / 13, n13 = nAp - 13 * n11;
+            uint32_t hi[16], lo[16];
+            tmem_ld16(tl, hi);
+            tmem_ld16(tl + 16, lo);
+            tmem_wait<16>(hi, lo);
+#pragma unroll
+            for (int k8 = 0; k8 < 8; ++k8) {
+                const float2 v = hilo(hi, lo, k8);
+                if (ok)
+                    *reinterpret_cast<uint32_t *>(X1 + k24_off(n13 + 13 * (k16 + 16 * k8), n11)) =
+                        pack_half2(kScaleB2 * v.x, kScaleB2 * v.y);
+            }
+        };
+        // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13
+        auto epi3 = [&](int j) {
+            const int r = 128 * j + 32 * q + lane, kB = r / 13, n13 = r - 13 * kB;
+            uint32_t hi[16], lo[16];
+            tmem_ld16(tl, hi);        // hi: columns 0..21 (k11 < 8 here)
+            tmem_ld16(tl + 32, lo);   // lo: columns 32..53
+            tmem_wait<16>(hi, lo);
+#pragma unroll
+            for (int k11 = 0; k11 < 8; ++k11) {
+                const float2 v = hilo(hi, lo, k11);
+                *reinterpret_cast<uint32_t *>(X0 + sw64_off(128 * k11 + kB, n13)) =
+                    pack_half2(kScaleB3 * v.x, kScaleB3 * v.y);
+            }
+            uint32_t hi2[8], lo2[8];
+            tmem_ld8(tl + 16, hi2);   // k11 = 8..11 (11 unused)
+            tmem_ld8(tl + 48, lo2);
+            tmem_wait<8>(hi2, lo2);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float2 v = hilo(hi2, lo2, i);
+                *reinterpret_cast<uint32_t *>(X0 + sw64_off(128 * (8 + i) + kB, n13)) =
+                    pack_half2(kScaleB3 * v.x, kScaleB3 * v.y);
+            }
+        };
+        // B4: DFT-13 out (k13), rows 128 k11 + kB -> Z[k], k = (2432 kA + 15873 kB) mod N,
+        // kA = (78 k11 + 66 k13) mod 143: k advances by 14080 per k13.
+        auto epi4 = [&](int j) {
+            const int kB = 32 * q + lane;
+            const int kA0 = (78 * j) % 143;
+            int k = (2432 * kA0 + 15873 * kB) % kMB;
+            uint32_t hi[16], lo[16];
+            tmem_ld16(tl, hi);        // hi: columns 0..25
+            tmem_ld16(tl + 32, lo);   // lo: columns 32..57
+            tmem_wait<16>(hi, lo);
+#pragma unroll
+            for (int k13 = 0; k13 < 8; ++k13) {
+                const float2 v = hilo(hi, lo, k13);
+                Z[k] = pack_half2(kScaleB4 * v.x, kScaleB4 * v.y);
+                k += 14080;
+                k -= k >= kMB ? kMB : 0;
+            }
+            uint32_t hi2[16], lo2[16];
+            tmem_ld16(tl + 16, hi2);
+            tmem_ld16(tl + 48, lo2);
+            tmem_wait<16>(hi2, lo2);
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {  // k13 = 8..12
+                const float2 v = hilo(hi2, lo2, i);
+                Z[k] = pack_half2(kScaleB4 * v.x, kScaleB4 * v.y);
+                k += 14080;
+                k -= k >= kMB ? kMB : 0;
+            }
+        };
+        // R2C pairing: bins q = skip + jj, jj = 0..16384, from Z[q], Z[N - q]
+        auto pairing = [&](const SegFwd &s, int64_t pol, int64_t loc) {
+            uint32_t *yo = s.out + pol * s.out_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen);
+#pragma unroll 1
+            for (int jj = et; jj <= kMA; jj += kEpiThreads) {
+                const int qq = s.skip + jj;
+                float2 y;
+                if (qq == 0 || qq == kMB) {
+                    const float2 z0 = h2f(Z[0]);
+                    y = make_float2(qq == 0 ? z0.x + z0.y : z0.x - z0.y, 0.f);
+                } else {
+                    const float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
+                    float2 xq, xm;
+                    r2c_pair(h2f(Z[qq]), h2f(Z[kMB - qq]), w, xq, xm);
+                    y = xq;
+                }
+                __stcs(yo + jj, pack_half2(y.x, y.y));
+            }
         };
 
-        int p = 0;
-        if (blockIdx.x < a.n_items) {
-            prefetch(blockIdx.x);
-            stage_spectrum();
-            named_sync_epi();
-            input(0);
-            publish(0);
-            prefetch(blockIdx.x + gridDim.x);
-        }
-        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-            // stage 1 -> operand p ^ 1
-            for (int j = 0; j < 4; ++j, ++T)
-                if (static_cast<int>(T & 3u) == grp) {
-                    wait_tile(T);
-                    epi1(j, X(p ^ 1));
-                    release_tile(T);
-                }
-            publish(p ^ 1);
-            // stage 2 -> operand p
-            for (int j = 0; j < 4; ++j, ++T)
-                if (static_cast<int>(T & 3u) == grp) {
-                    wait_tile(T);
-                    epi2(j, X(p));
-                    release_tile(T);
-                }
-            publish(p);
-            // every stage-2 MMA has retired (each group saw its tiles' commits),
-            // so operand p ^ 1 takes the next item's input
-            named_sync_epi();
-            const int64_t next = item + gridDim.x;
-            if (next < a.n_items) {
-                stage_spectrum();
-                named_sync_epi();
-                input(p ^ 1);
-                publish(p ^ 1);
-                prefetch(next + gridDim.x);
-            }
-            // stage 3 -> output
-            void *out = out_ptr(item);
-            for (int j = 0; j < 8; ++j, ++T)
-                if (static_cast<int>(T & 3u) == grp) {
-                    wait_tile(T);
-                    epi3(j, out);
-                    release_tile(T);
-                }
+        if (blockIdx.x < a.n_items) fetch(blockIdx.x);
+        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+            ep.wait_staging();
+            input();
+            ep.publish(1);
+            ep.tiles(9, [&](int j) { epi1(j); });
+            ep.publish(0);
+            ep.tiles(18, [&](int j) { epi2(j); });
+            ep.publish(1);
+            ep.tiles(13, [&](int j) { epi3(j); });
+            ep.publish(0);
+            ep.tiles(11, [&](int j) { epi4(j); });
+            named_sync_epi();  // Z complete; every DFT-13 MMA retired: X0 takes the next chunk
+            fetch(item + gridDim.x);
+            int64_t pol, loc;
+            const SegFwd &s = a.s[item_pos(item, pol, loc)];
+            pairing(s, pol, loc);
+            named_sync_epi();  // Z read: X1 takes the next input step
         }
     }
-    fence_before();
-    __syncthreads();
-    if (tid == 0 && s_err) *reinterpret_cast<volatile int *>(a.status) = 1;
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tb), "r"(kTmemCols));
+    teardown(ctl, a.status, warp);
+}
+
+// Float time series -> FP16 x 2^-2 (sdbe_resample_chunks in this form).
+__global__ void k_tcf_to_half(const float *__restrict__ in, uint32_t *__restrict__ out, int64_t n_pairs) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n_pairs;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2 *>(in)[i];
+        out[i] = pack_half2(kScaleA * v.x, kScaleA * v.y);
+    }
 }
 
 // ---- host side ------------------------------------------------------------
 
-// Real form of the complex DFT matrix of size r (sign +1: inverse), split
-// into FP16 hi and lo halves stacked along N ([hi | lo]: 4r rows of K = 2r),
-// K-major in core-matrix order (8 rows x 16 bytes; 128 bytes between core
-// matrices along K, (K / 8) * 128 between row groups).  Row 2 kk + t of a
-// half is output component t (re, im) of bin kk; column 2 nn + u is input
-// component u of element nn.
-std::vector<__half> dft_matrix_hilo(int r, int sign) {
-    const int K = 2 * r, N = 4 * r;
-    std::vector<__half> out(static_cast<size_t>(N) * K);
+// Real form of the complex DFT matrix of size r (sign -1 forward, +1 inverse),
+// split into FP16 hi and lo halves: N = np rows (hi at rows [0, 2r), lo at
+// [lo_row, lo_row + 2r), zero elsewhere), K = kp columns (2r used), K-major in
+// core-matrix order (8 rows x 16 bytes; 128 bytes between core matrices along
+// K, (K / 8) * 128 between row groups).  Row 2 kk + t of a half is output
+// component t (re, im) of bin kk; column 2 nn + u is input component u of
+// element nn.
+std::vector<__half> dft_matrix_hilo(int r, int sign, int kp, int lo_row, int np) {
+    std::vector<__half> out(static_cast<size_t>(np) * kp, __float2half_rn(0.f));
     for (int kk = 0; kk < r; ++kk)
         for (int nn = 0; nn < r; ++nn) {
             const long long e = static_cast<long long>(kk) * nn % r;
@@ -404,8 +906,9 @@ std::vector<__half> dft_matrix_hilo(int r, int sign) {
                     const __half hv = __float2half_rn(static_cast<float>(v));
                     const __half lv = __float2half_rn(static_cast<float>(v - static_cast<double>(__half2float(hv))));
                     for (int part = 0; part < 2; ++part) {
-                        const int n = part * 2 * r + 2 * kk + t, k = 2 * nn + u;
-                        const size_t off = static_cast<size_t>((n >> 3) * (K / 8) * 64 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7));
+                        const int n = (part ? lo_row : 0) + 2 * kk + t, k = 2 * nn + u;
+                        const size_t off =
+                            static_cast<size_t>((n >> 3) * (kp / 8) * 64 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7));
                         out[off] = part ? lv : hv;
                     }
                 }
@@ -413,32 +916,79 @@ std::vector<__half> dft_matrix_hilo(int r, int sign) {
     return out;
 }
 
-std::vector<float2> tables_a() {
-    std::vector<float2> t(kTabLen, make_float2(0.f, 0.f));
-    auto cis = [](double num, double den) {
-        const double ang = 2.0 * 3.14159265358979323846 * num / den;
-        return make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
-    };
-    for (int i = 0; i <= 16; ++i) t[kTabA1 + i] = cis(i, 64);
-    for (int i = 0; i < 512; ++i) t[kTabA2 + i] = cis(i, 32768);
-    for (int i = 0; i < 512; ++i) t[kTabB + i] = cis(i, 16384);
-    for (int i = 0; i < 16; ++i) t[kTabC + i] = cis(i, 512);
-    return t;
+float2 cis(double num, double den, int sign = +1) {
+    const double ang = sign * 2.0 * 3.14159265358979323846 * num / den;
+    return make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
 }
 
-template <bool OUT_HALF>
-cudaError_t launch_tcf_a(const ArgsTA &args, cudaStream_t st) {
-    if (args.n_items <= 0) return cudaSuccess;
+template <class T>
+void append(std::vector<uint8_t> &blob, const std::vector<T> &v) {
+    const size_t o = blob.size();
+    blob.resize(o + v.size() * sizeof(T));
+    std::memcpy(blob.data() + o, v.data(), v.size() * sizeof(T));
+}
+
+constexpr size_t kInvGBytes = kG32Bytes + kG16Bytes, kFwdGBytes = kG16f + kG8f + kG11f + kG13f;
+// blob: inverse matrices, inverse tables, forward matrices, forward tables
+constexpr size_t kBlobInvTab = kInvGBytes, kBlobFwdG = kBlobInvTab + kInvTabLen * 8,
+                 kBlobFwdTab = kBlobFwdG + kFwdGBytes, kBlobBytes = kBlobFwdTab + kFwdTabLen * 8;
+static_assert(kBlobFwdG % 16 == 0 && kBlobFwdTab % 16 == 0, "16-byte aligned blob parts");
+
+std::vector<uint8_t> build_blob() {
+    std::vector<uint8_t> blob;
+    append(blob, dft_matrix_hilo(32, +1, 64, 64, 128));
+    append(blob, dft_matrix_hilo(16, +1, 32, 32, 64));
+    std::vector<float2> ti(kInvTabLen, make_float2(0.f, 0.f));
+    for (int i = 0; i <= 16; ++i) ti[kTabA1 + i] = cis(i, 64);
+    for (int i = 0; i < 512; ++i) ti[kTabA2 + i] = cis(i, 32768);
+    for (int i = 0; i < 512; ++i) ti[kTabB + i] = cis(i, 16384);
+    for (int i = 0; i < 16; ++i) ti[kTabC + i] = cis(i, 512);
+    append(blob, ti);
+    append(blob, dft_matrix_hilo(16, -1, 32, 32, 64));
+    append(blob, dft_matrix_hilo(8, -1, 16, 16, 32));
+    append(blob, dft_matrix_hilo(11, -1, 32, 32, 64));
+    append(blob, dft_matrix_hilo(13, -1, 32, 32, 64));
+    std::vector<float2> tf(kFwdTabLen, make_float2(0.f, 0.f));
+    for (int i = 0; i < 8; ++i) tf[kTabW128 + i] = cis(i, 128, -1);
+    for (int i = 0; i < 144; ++i) tf[kTabQHi + i] = cis(128.0 * i, 36608, -1);
+    for (int i = 0; i < 128; ++i) tf[kTabQLo + i] = cis(i, 36608, -1);
+    append(blob, tf);
+    return blob;
+}
+
+cudaError_t grid_for(int64_t n_items, unsigned *grid) {
     int dev = 0, sms = 1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    *grid = static_cast<unsigned>(n_items < sms ? n_items : sms);
+    return e;
+}
+
+template <int IN, int OUT>
+cudaError_t launch_inv(const ArgsInv &args, cudaStream_t st) {
+    if (args.n_items <= 0) return cudaSuccess;
+    unsigned grid = 0;
+    cudaError_t e = grid_for(args.n_items, &grid);
+    constexpr uint32_t smem = inv_smem(IN == IN_BINS);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tcf_a<OUT_HALF>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kSmemA));
+        e = cudaFuncSetAttribute(k_tcf_inv<IN, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    const unsigned grid = static_cast<unsigned>(args.n_items < sms ? args.n_items : sms);
-    k_tcf_a<OUT_HALF><<<grid, kThreadsA, kSmemA, st>>>(args);
+    k_tcf_inv<IN, OUT><<<grid, kThreads, smem, st>>>(args);
     return cudaGetLastError();
 }
+
+cudaError_t launch_fwd(const ArgsFwd &args, cudaStream_t st) {
+    if (args.n_items <= 0) return cudaSuccess;
+    unsigned grid = 0;
+    cudaError_t e = grid_for(args.n_items, &grid);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tcf_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kFwdSmem));
+    if (e != cudaSuccess) return e;
+    k_tcf_fwd<<<grid, kThreads, kFwdSmem, st>>>(args);
+    return cudaGetLastError();
+}
+
+const uint8_t *blob_of(const sdbe_resampler *h) { return static_cast<const uint8_t *>(h->tcf_tabs); }
 
 }  // namespace
 
@@ -453,12 +1003,8 @@ int tcf_prepare(sdbe_resampler *h, cudaStream_t st) {
         *h->tc_status_host = 0;
         SDBE_CK(h, cudaHostGetDevicePointer(reinterpret_cast<void **>(&h->tc_status), h->tc_status_host, 0));
     }
-    const std::vector<__half> g32 = dft_matrix_hilo(32, +1), g16 = dft_matrix_hilo(16, +1);
-    const std::vector<float2> ta = tables_a();
-    std::vector<uint8_t> blob(kG32Bytes + kG16Bytes + ta.size() * sizeof(float2));
-    std::memcpy(blob.data(), g32.data(), kG32Bytes);
-    std::memcpy(blob.data() + kG32Bytes, g16.data(), kG16Bytes);
-    std::memcpy(blob.data() + kG32Bytes + kG16Bytes, ta.data(), ta.size() * sizeof(float2));
+    const std::vector<uint8_t> blob = build_blob();
+    if (blob.size() != kBlobBytes) return fail(h, SDBE_ERR_STATE, "tensor-core table layout mismatch");
     if (cudaMalloc(&h->tcf_tabs, blob.size()) != cudaSuccess) {
         cudaGetLastError();
         return fail(h, SDBE_ERR_NOMEM, "cannot allocate the tensor-core tables");
@@ -470,22 +1016,160 @@ int tcf_prepare(sdbe_resampler *h, cudaStream_t st) {
 
 // Stage A in the fast tensor-core form over several stream pairs in one
 // launch: per segment, snapshots [snap0, snap0 + n_snaps) of n_pols pols of
-// the packed spectra -> float time series out + pol * out_pol_stride,
-// [n_snaps][32768] per pol.
-int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, cudaStream_t st) {
+// the packed spectra -> time series out + pol * out_pol_stride (elements),
+// [n_snaps][32768] per pol, FP16 x 2^-2 (half_out) or FP32.
+int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, bool half_out, cudaStream_t st) {
     if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
     if (int rc = tcf_prepare(h, st)) return rc;
-    ArgsTA A{};
+    ArgsInv A{};
     for (int i = 0; i < n_segs; ++i) {
         const TcfASeg &g = segs[i];
-        A.s[A.n++] = SegTA{g.spec, g.out, g.spec_pol_stride, g.snap0, g.n_snaps, g.out_pol_stride, A.n_items};
+        SegInv s{};
+        s.in = g.spec;
+        s.out = g.out;
+        s.in_pol_stride = g.spec_pol_stride;
+        s.first = g.snap0;
+        s.n = g.n_snaps;
+        s.out_pol_stride = g.out_pol_stride;
+        s.item0 = A.n_items;
+        A.s[A.n++] = s;
         A.n_items += n_pols * g.n_snaps;
     }
-    A.g = static_cast<const uint8_t *>(h->tcf_tabs);
-    A.tab = reinterpret_cast<const float2 *>(static_cast<const uint8_t *>(h->tcf_tabs) + kG32Bytes + kG16Bytes);
+    A.g = blob_of(h);
+    A.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
     A.status = h->tc_status;
-    SDBE_CK(h, launch_tcf_a<false>(A, st));
+    SDBE_CK(h, (half_out ? launch_inv<IN_PACKED, OUT_TS_HALF>(A, st) : launch_inv<IN_PACKED, OUT_TS_FLOAT>(A, st)));
     return SDBE_OK;
+}
+
+// Stages B and C in the fast tensor-core form over several stream pairs: per
+// segment n_chunks chunks of n_pols pols of FP16 time series (x 2^-2) -> R2C
+// bins (scratch) -> the output `mode` asks for: 0 2-bit payload, 1 floats +
+// per-chunk (n, mean, M2), 3 2-bit payload + per-chunk (n, sum, sum of
+// squares), 5 floats.
+int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols, int mode, cudaStream_t st) {
+    if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
+    if (int rc = tcf_prepare(h, st)) return rc;
+    ArgsFwd B{};
+    ArgsInv C{};
+    for (int i = 0; i < n_segs; ++i) {
+        const TcfBCSeg &g = segs[i];
+        B.s[B.n++] = SegFwd{static_cast<const __half *>(g.ts), g.bins, g.ts_pol_stride, g.bins_pol_stride, g.n_chunks,
+                            B.n_items, g.skip};
+        B.n_items += n_pols * g.n_chunks;
+        SegInv s{};
+        s.in = g.bins;
+        s.in_pol_stride = g.bins_pol_stride;
+        s.n = g.n_chunks;
+        s.item0 = C.n_items;
+        s.o = g.o;
+        C.s[C.n++] = s;
+        C.n_items += n_pols * g.n_chunks;
+    }
+    B.g = blob_of(h) + kBlobFwdG;
+    B.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobFwdTab);
+    B.status = h->tc_status;
+    C.g = blob_of(h);
+    C.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
+    C.status = h->tc_status;
+    SDBE_CK(h, launch_fwd(B, st));
+    switch (mode) {
+        case 0: SDBE_CK(h, (launch_inv<IN_BINS, OUT_QUANT>(C, st))); break;
+        case 1: SDBE_CK(h, (launch_inv<IN_BINS, OUT_FLOAT_MOMENTS>(C, st))); break;
+        case 3: SDBE_CK(h, (launch_inv<IN_BINS, OUT_QUANT_SUMS>(C, st))); break;
+        default: SDBE_CK(h, (launch_inv<IN_BINS, OUT_FLOAT>(C, st))); break;
+    }
+    return SDBE_OK;
+}
+
+// One wave of the fast tensor-core chain over several handles (one stream
+// pair each): stage A of every handle's batches in one launch (FP16 time
+// series into the handle's stage-A scratch), then stages B and C in one launch
+// each, writing the payloads.  With `first` each item is its handle's first
+// batch: stage C writes floats and FP64 moments, the thresholds are set from
+// them, then the floats are packed, as the FP32 path does.
+int tcf_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st) {
+    if (w.empty()) return SDBE_OK;
+    if (w.size() > static_cast<size_t>(kMaxSegs)) return fail(w[0].h, SDBE_ERR_ARG, "too many handles");
+    sdbe_resampler *h0 = w[0].h;
+    std::vector<TcfASeg> sa;
+    std::vector<TcfBCSeg> sb;
+    int64_t units_a = 0, units_bc = 0;
+    bool any_win = false;
+    for (const auto &it : w) {
+        sdbe_resampler *h = it.h;
+        if (int rc = tcf_prepare(h, st)) return rc;
+        if (*reinterpret_cast<volatile int *>(h->tc_status_host))  // written by an earlier call's kernels
+            return fail(h, SDBE_ERR_CUDA, "a tensor-core transform timed out on its mbarrier wait");
+        const int64_t per_pol = static_cast<int64_t>(h->wave) * kChunks;
+        if (int rc = grow(h, reinterpret_cast<uint8_t **>(&h->tcf_bins), &h->tcf_bins_bytes,
+                          2 * per_pol * kTcfBinsLen * 4, "the tensor-core bins"))
+            return rc;
+        const int64_t snaps = it.nb * kBatchSnaps, chunks = it.nb * kChunks;
+        sa.push_back(TcfASeg{it.spec, it.spec_pol_stride, it.b0 * kBatchSnaps, snaps, h->ts, h->ts_pol_stride});
+        TcfBCSeg b{};
+        b.ts = h->ts;  // FP16 in the float scratch: same element stride, half the bytes
+        b.ts_pol_stride = h->ts_pol_stride;
+        b.bins = h->tcf_bins;
+        b.bins_pol_stride = per_pol * kTcfBinsLen;
+        b.n_chunks = chunks;
+        b.skip = h->skip;
+        const bool win = h->cfg.threshold_mode == SDBE_THRESH_WINDOW;
+        if (first) {
+            b.o.fout = h->fout;
+            b.o.fout_pol_stride = static_cast<int64_t>(kChunks) * kNC;
+            b.o.partials = h->partials;
+        } else {
+            const PayloadTarget &t = it.tgt;
+            b.o.out = t.base;
+            b.o.out_pol_stride = t.pol_stride;
+            b.o.pkt_stride = t.pkt_stride;
+            b.o.payload_off = t.payload_off;
+            b.o.pkt0 = it.b0 * kChunks;
+            b.o.thr = h->thr;
+            b.o.partials = win ? h->wpart : nullptr;
+            any_win = any_win || win;
+        }
+        sb.push_back(b);
+        units_a += 2 * snaps;
+        units_bc += 2 * chunks;
+    }
+    const int n = static_cast<int>(w.size());
+    size_t slot = 0;
+    if (!first) SDBE_CK(h0, timed_begin(h0, 0, units_a, st, &slot));
+    if (int rc = tcf_stage_a(h0, sa.data(), n, 2, true, st)) return rc;
+    if (!first) {
+        SDBE_CK(h0, timed_end(h0, slot, st));
+        SDBE_CK(h0, timed_begin(h0, 1, units_bc, st, &slot));
+    }
+    if (int rc = tcf_stage_bc(h0, sb.data(), n, 2, first ? 1 : (any_win ? 3 : 0), st)) return rc;
+    WinUpds U{};
+    for (const auto &it : w) {
+        sdbe_resampler *h = it.h;
+        if (first) {
+            SDBE_CK(h, launch_finalize_thresholds(h->partials, kChunks, h->cfg.pol1_uses_pol0_threshold, h->thr, st));
+            const PayloadTarget &t = it.tgt;
+            SDBE_CK(h, launch_quantize_chunks(h->fout, static_cast<int64_t>(kChunks) * kNC, kChunks, h->thr, t.base,
+                                              t.pol_stride, t.pkt_stride, t.payload_off, it.b0 * kChunks, st));
+            h->thresholds_set = true;
+            h->stream_batch = 0;
+            h->launches += 2;
+        }
+        // the window ring takes the wave's statistics after it was packed with the old thresholds
+        window_step(h, first ? h->partials : h->wpart, it.nb, first, U);
+    }
+    if (U.n) {
+        SDBE_CK(h0, launch_window_update(U, st));
+        h0->launches += 1;
+    }
+    if (!first) SDBE_CK(h0, timed_end(h0, slot, st));
+    h0->launches += 3;  // stage A, stage B, stage C
+    return SDBE_OK;
+}
+
+cudaError_t tcf_to_half(const float *in, void *out, int64_t n_floats, cudaStream_t st) {
+    k_tcf_to_half<<<1216, 256, 0, st>>>(in, static_cast<uint32_t *>(out), n_floats / 2);
+    return cudaGetLastError();
 }
 
 }  // namespace sdbe

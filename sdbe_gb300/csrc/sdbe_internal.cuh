@@ -30,6 +30,8 @@ constexpr int kOutPktData = 8192;
 constexpr int kOutPkt = 8224;
 constexpr int kMaxSkip = kMB - kChannels;        // 1920
 constexpr int kDefaultWave = 64;                 // batches per FFT wave when wave_batches = 0 (and the maximum)
+constexpr int kTcfBinsLen = kMA + 4;             // fast tensor-core form: R2C bins [skip, skip + 16384] per chunk,
+                                                 // padded to a 16-byte multiple
 
 // Packed spectrum nibble: bits 3..2 = real code, bits 1..0 = imag code, value = code - 2.
 constexpr uint32_t kMissingWord = 0xAAAAAAAAu;   // codes 2/2 = (0, 0) for all 8 channels

@@ -189,3 +189,44 @@ def test_tc_ingest_group_equals_process(S):
         assert np.array_equal(groups[0], want)
         got32, _ = f32.process(pk, G, spec.b_start + 1)
         assert float(np.mean(codes_of(groups[0]) == codes_of(got32))) >= AGREE_MIN
+
+
+@pytest.mark.parametrize("fill", [0x00, 0xFF])
+def test_tc_fast_saturated_spectra_stay_finite(S, fill):
+    """The fast form keeps its FP16 operands in range with fixed power-of-two
+    scales; the largest spectra stress them: every payload byte set to one
+    value (0x00: every channel -2 - 2i, 0xFF: +1 + 1i), so that each
+    snapshot's time series is one large impulse.  Stage A (float output) and
+    stages B + C (sdbe_resample_chunks, through the FP16 time series) against
+    the FP64 oracle: finite, relative RMS below the fast form's bound."""
+    import torch
+
+    from gpu_util import dev, empty, host, ptr, rel_rms, zeros
+    from sdbe_gb300 import Resampler
+    from sdbe_gb300 import _native as N
+
+    spec = S.config1()
+    nf = 2
+    p = S.generate(spec, frame_offset=0, n_frames=nf).copy()
+    p[:, 32:] = fill
+    snaps = nf * 128
+    words = empty(2 * snaps * 2048 * 4, "int32")
+    bitmap, counts, rej = zeros(nf * 256), zeros(nf * 4, "int32"), zeros(4, "int32")
+    lib = N.lib()
+    N.check(lib.sdbe_unpack(ptr(dev(p)), p.shape[0], spec.b_start, nf, 0, ptr(words), snaps * 2048, 0, ptr(bitmap),
+                            ptr(counts), ptr(rej), None))
+    beng = O.vdif_to_beng(p, spec.b_start, nf)
+    sp = O.beng_to_complex(beng[0].reshape(-1, 16384, 2))[:143]
+    ts_ref = O.swarm_c2r(sp).reshape(-1)
+    with Resampler(trim_mhz=150, max_frames=nf, precision=N.PRECISION_TC16_FAST) as rs:
+        ts = empty(143 * 32768 * 4, "float32")
+        y = empty(128 * 32768 * 4, "float32")
+        N.check(lib.sdbe_swarm_c2r(rs.handle, ptr(words), 143, ptr(ts), None), rs.handle)
+        N.check(lib.sdbe_resample_chunks(rs.handle, ptr(dev(ts_ref.astype(np.float32))), 128, ptr(y), None),
+                rs.handle)
+        ref = O.r2dbe_c2r(O.swarm_r2c(ts_ref), rs.skip_chan)
+        got_ts, got_y = host(ts).astype(np.float64), host(y).reshape(128, 32768).astype(np.float64)
+    torch.cuda.synchronize()
+    assert np.isfinite(got_ts).all() and np.isfinite(got_y).all()
+    assert rel_rms(got_ts, ts_ref) < 2e-3
+    assert rel_rms(got_y, ref) < 2e-3
