@@ -253,6 +253,21 @@ __device__ __forceinline__ uint32_t code2(float x, float th, float off) {
     return ((static_cast<uint32_t>(fabsf(v) >= th) | 2u) ^ (3u * static_cast<uint32_t>(v < 0.f))) & 3u;
 }
 
+// 8 x 8 transpose of 4-bit nibbles over the aligned groups of 8 lanes: on
+// return, nibble r of lane c is nibble c of lane r (c = lane & 7).  Step m
+// (1, 2, 4) swaps, between lanes c and c ^ m, the nibbles whose index bit m
+// differs from the lane's own bit m.
+__device__ __forceinline__ uint32_t nib_transpose8(uint32_t x, int c) {
+    constexpr uint32_t kKeep[3] = {0x0F0F0F0Fu, 0x00FF00FFu, 0x0000FFFFu};  // nibbles with index bit m clear
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int m = 1 << s, sh = 4 << s;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, m);
+        x = (c & m) ? ((x & ~kKeep[s]) | ((y >> sh) & kKeep[s])) : ((x & kKeep[s]) | ((y << sh) & ~kKeep[s]));
+    }
+    return x;
+}
+
 // ---- block reductions -------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -61,15 +61,17 @@ constexpr int kThreads = 32 + kEpiThreads;
 constexpr uint32_t kTmemCols = 512;
 
 // Scales (powers of two, exact).  Stage A stores its time series x 2^-2
-// (|x| <= 32768 * 2 sqrt 2 < 2^17); stage B's four stages scale by 2^-2,
-// 2^-1, 2^-2, 2^-3 (a stage of radix r multiplies the energy by r, and a
-// chunk's energy is at most 2 * 32768^2 * 8 before stage A's scale); stage C
-// halves its C2R pairing and scales its stages 1 and 2 by 2^-5.
+// (|x| <= 32768 * 2 sqrt 2 < 2^17).  Stage B scales by 2^-8 in its first
+// twiddle: a stage of radix r multiplies the energy by r, a chunk's energy is
+// at most 2 * 32768^2 * 8 before stage A's scale, so no value of its four
+// stages exceeds 2^15 (Cauchy-Schwarz), and typical ones stay near 10 - 100.
+// Its R2C bins carry a further 2^-1 (the C2R pairing's factor of two), and
+// stage C scales its stages 1 and 2 by 2^-5 each.
 constexpr float kScaleA = 0.25f;
-constexpr float kScaleB1 = 0.25f, kScaleB2 = 0.5f, kScaleB3 = 0.25f, kScaleB4 = 0.125f;
+constexpr float kScaleB = 1.f / 256.f;
 constexpr float kScaleC1 = 1.f / 32.f, kScaleC2 = 1.f / 32.f;
 // stage C output x 2^21 = back to the unnormalised value (2^-2 * 2^-8 * 2^-1 * 2^-10)
-constexpr float kUnscaleC = 2097152.f;
+constexpr float kUnscaleC = 2097152.f, kRescaleC = 1.f / 2097152.f;
 
 // ---- shared memory of k_tcf_inv (bytes from a 1024-byte aligned base) -----
 constexpr uint32_t kOpBytes = 65536;                // one operand buffer (16384 complex FP16)
@@ -78,8 +80,9 @@ constexpr uint32_t kG16Bytes = 64 * 32 * 2;         // DFT-16, [hi | lo] x K 32
 constexpr uint32_t kInvOffG = 2 * kOpBytes;
 constexpr uint32_t kInvOffStg = kInvOffG + kG32Bytes + kG16Bytes;
 // float2 tables: e^{2 pi i n1/64} (n1 <= 16, 32 slots), e^{2 pi i n'/32768} (512),
-// e^{2 pi i n'/16384} (512), e^{2 pi i n3/512} (16)
-constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 512, kInvTabLen = kTabC + 16;
+// e^{2 pi i n'/16384} (512, at n' + n'/16 so that 16 lanes with n' 16 apart
+// hit distinct banks), e^{2 pi i n3/512} (16)
+constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 544, kInvTabLen = kTabC + 16;
 constexpr uint32_t kStgPacked = 8192, kStgBins = kTcfBinsLen * 4;
 constexpr uint32_t inv_smem(bool bins) { return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + 1024; }
 
@@ -113,9 +116,9 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
     return __half22float2(h);
 }
 
-__device__ __forceinline__ float2 hilo(const uint32_t *hi, const uint32_t *lo, int i) {
-    return make_float2(__uint_as_float(hi[2 * i]) + __uint_as_float(lo[2 * i]),
-                       __uint_as_float(hi[2 * i + 1]) + __uint_as_float(lo[2 * i + 1]));
+// Complex value i of 16 loaded accumulator columns (re, im pairs), i < 8.
+__device__ __forceinline__ float2 acc2(const uint32_t *r, int i) {
+    return make_float2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]));
 }
 
 // Bulk copy global -> shared of `bytes` (multiple of 16), completing on mbar.
@@ -129,16 +132,17 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 // Common kernel state: barriers, tensor memory, error flag.
+constexpr int kSlots = 8;           // accumulator slots of 64 tensor-memory columns
 struct Ctl {
-    uint64_t full[4], empty[4], ready[2], done, stg;
+    uint64_t full[kSlots], empty[kSlots], ready[2], done, stg;
     uint32_t tmem_base;
     int err;
 };
 
 __device__ __forceinline__ void ctl_init(Ctl &c) {
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < kSlots; ++i) {
         mbar_init(&c.full[i], 1);
-        mbar_init(&c.empty[i], 4);
+        mbar_init(&c.empty[i], kEpiWarps);  // every epilogue warp's share of the slot drained
     }
     mbar_init(&c.ready[0], kEpiWarps);
     mbar_init(&c.ready[1], kEpiWarps);
@@ -156,23 +160,27 @@ struct Issuer {
     Ctl *c;
     uint32_t tb, T = 0, uses[2] = {0, 0};
     // One GEMM stage over `tiles` 128-row tiles of the operand in buffer buf
-    // (published on ready[buf]): per K-step one MMA of N columns into the
-    // tile's slot.
+    // (published on ready[buf]): per K-step two MMAs of N columns into the
+    // tile's slot, with the hi and the lo half of the DFT matrix (the lo half
+    // g_lo bytes after the hi half), both accumulating.
     __device__ void stage(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, int ksteps, uint32_t kstep_bytes,
-                          uint32_t lbo, uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, int n) {
+                          uint32_t lbo, uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo,
+                          int n) {
         if (!err_set(*c) && !mbar_wait(&c->ready[buf], uses[buf] & 1u)) raise_err(*c);
         ++uses[buf];
         fence_after();
         const uint32_t id = idesc_f16(128, n);
         for (int j = 0; j < tiles; ++j, ++T) {
-            const uint32_t slot = T & 3u;
-            if (T >= 4 && !err_set(*c) && !mbar_wait(&c->empty[slot], ((T >> 2) - 1) & 1u)) raise_err(*c);
+            const uint32_t slot = T & (kSlots - 1);
+            if (T >= kSlots && !err_set(*c) && !mbar_wait(&c->empty[slot], ((T / kSlots) - 1) & 1u)) raise_err(*c);
             fence_after();
             if (!err_set(*c)) {
-                const uint32_t d = tb + slot * 128;
-                for (int ks = 0; ks < ksteps; ++ks)
-                    mma_f16(d, desc(xa + j * tile_bytes + ks * kstep_bytes, lbo, sbo, layout),
-                            desc(g + ks * 256, 128, g_sbo, kNoSwizzle), id, ks > 0);
+                const uint32_t d = tb + slot * 64;
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint64_t xd = desc(xa + j * tile_bytes + ks * kstep_bytes, lbo, sbo, layout);
+                    mma_f16(d, xd, desc(g + ks * 256, 128, g_sbo, kNoSwizzle), id, ks > 0);
+                    mma_f16(d, xd, desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle), id, true);
+                }
             }
             commit(&c->full[slot]);
         }
@@ -183,21 +191,24 @@ struct Issuer {
     }
 };
 
-// Epilogue warp state.
+// Epilogue warp state.  A tile T in slot T % 8 is drained either by group
+// T % 4 alone (tiles(): each of its warps releases four shares of the slot)
+// or by all four groups, a quarter of its columns each (tiles_all()).
 struct Epi {
     Ctl *c;
     int lane, grp, q, et;
-    uint32_t tl;  // tensor-memory address of this warp's lane quarter in its group's slot
+    uint32_t tq;  // tensor-memory address of this warp's lane quarter, column 0
     uint32_t T = 0, stg_uses = 0;
     __device__ bool mine() const { return static_cast<int>(T & 3u) == grp; }
+    __device__ uint32_t taddr() const { return tq + (T & (kSlots - 1)) * 64; }
     __device__ void wait_tile() {
-        if (!err_set(*c) && !mbar_wait(&c->full[T & 3u], (T >> 2) & 1u)) raise_err(*c);
+        if (!err_set(*c) && !mbar_wait(&c->full[T & (kSlots - 1)], (T / kSlots) & 1u)) raise_err(*c);
         fence_after();
     }
-    __device__ void release_tile() {
+    __device__ void release_tile(uint32_t shares) {
         fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&c->empty[T & 3u]);
+        if (lane == 0) mbar_arrive_n(&c->empty[T & (kSlots - 1)], shares);
     }
     __device__ void publish(int buf) {  // this warp's part of an operand is written
         fence_async_smem();
@@ -208,15 +219,25 @@ struct Epi {
         if (!err_set(*c) && !mbar_wait(&c->stg, stg_uses & 1u)) raise_err(*c);
         ++stg_uses;
     }
-    // Runs f(j) on this group's tiles of a stage of n tiles.
+    // Runs f(j, accumulator address) on this group's tiles of a stage of n tiles.
     template <class F>
     __device__ void tiles(int n, F f) {
         for (int j = 0; j < n; ++j, ++T)
             if (mine()) {
                 wait_tile();
-                f(j);
-                release_tile();
+                f(j, taddr());
+                release_tile(4);
             }
+    }
+    // Runs f(j, accumulator address) on every tile of a stage of n tiles
+    // (f takes this group's quarter of the columns).
+    template <class F>
+    __device__ void tiles_all(int n, F f) {
+        for (int j = 0; j < n; ++j, ++T) {
+            wait_tile();
+            f(j, taddr());
+            release_tile(1);
+        }
     }
 };
 
@@ -243,12 +264,6 @@ __device__ __forceinline__ int seg_index(const A &a, int64_t item) {
     return j;
 }
 
-// 8 TMEM columns of this thread's lane, no wait.
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-}
 
 // ============================================================================
 // k_tcf_inv: 16384-point inverse transforms (stages A and C)
@@ -318,18 +333,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
             int p = 0;
             for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-                is.stage(p, smem_u32(X(p)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 128);
-                is.stage(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 128);
-                is.stage(p, smem_u32(X(p)), 8, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 64);
+                is.stage(p, smem_u32(X(p)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
+                is.stage(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
+                is.stage(p, smem_u32(X(p)), 8, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);
             }
             is.finish();
         }
         __syncwarp();
     } else {
         Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
-               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>((warp - 1) >> 2) * 128};
+               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
         const int e = warp - 1, q = ep.q, et = ep.et;
-        const uint32_t tl = ep.tl;
 
         // ---- input staging ---------------------------------------------------
         uint4 pre = make_uint4(0, 0, 0, 0);  // packed input: next snapshot, 16 bytes per thread
@@ -338,7 +352,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             const int64_t local = item - s.item0;
             const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
             if constexpr (kBins)
-                return static_cast<const uint32_t *>(s.in) + (pol * s.in_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen));
+                return static_cast<const uint32_t *>(s.in) +
+                       (pol * s.in_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen));
             else
                 return static_cast<const uint32_t *>(s.in) + pol * s.in_pol_stride + (s.first + loc) * kGroups;
         };
@@ -365,40 +380,82 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                 named_sync_epi();
             }
         };
+        auto nib = [](uint32_t w) {  // low nibble of w -> (real code - 2, imag code - 2)
+            const float re = __uint_as_float(0x4B400000u | ((w >> 2) & 3u)) - 12582914.0f;
+            const float im = __uint_as_float(0x4B400000u | (w & 3u)) - 12582914.0f;
+            return make_float2(re, im);
+        };
 
         // ---- input step: C2R pairing into the stage-1 operand -------------------
         // Packed input (stage A): row n' = 16 n2 + n3 at 32 n3 + n2; thread:
-        // n3 = its warp, (n2 % 8, n1 % 4) = its lane.  Bins input (stage C): rows
-        // in natural order n'; thread: n' = et, four consecutive n1 per store.
+        // n3 = its warp, (n2 % 8, n1 % 4) = its lane, so that its 16 pairs k =
+        // 512 (4 A + u) + 16 (8 B + a) + n3 (A, B < 4) have staging positions,
+        // shifts and store offsets that are per-lane constants plus
+        // compile-time ones.  Bins input (stage C): rows in natural order n';
+        // thread: n' = et, four consecutive n1 per 16-byte store.
         auto input = [&](int buf) {
             uint8_t *op = X(buf);
             if constexpr (!kBins) {
-                const int n3 = e;
-#pragma unroll 1
-                for (int it = 0; it < 16; ++it) {
-                    const int n1 = 4 * (it >> 2) + (lane >> 3), n2 = 8 * (it & 3) + (lane & 7);
-                    const int np = 16 * n2 + n3, k = 512 * n1 + np;
-                    float2 y = stg_value(stg, k);
-                    float2 ym = make_float2(0.f, 0.f);
-                    const int km = kMA - k;
-                    if (k == 0)
-                        y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
-                    else
-                        ym = stg_value(stg, km);
-                    float2 zk, zm;
-                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
-                    *reinterpret_cast<uint32_t *>(op + sw128_off(32 * n3 + n2, n1)) = pack_half2(zk.x, zk.y);
-                    if (k != 0) {
-                        const int n1m = km >> 9, npm = km & 511;
-                        *reinterpret_cast<uint32_t *>(op + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
-                            pack_half2(zm.x, zm.y);
+                const int n3 = e, av = lane & 7, u = lane >> 3;
+                if (n3 != 0) {
+                    const int u0 = u & 1, u1 = u >> 1;
+                    const int wl = 64 * u + 2 * av + ((n3 >> 3) ^ u0);
+                    const int L0 = wl + 16 * u1, L1 = wl + 16 * (1 - u1);
+                    const int sh = (n3 & 7) * 4, shm = ((8 - (n3 & 7)) & 7) * 4;
+                    uint8_t *S = op + 4096 * n3 + 128 * av + 4 * u;
+                    uint8_t *Sm = op + 4096 * (16 - n3) + 128 * (31 - av) + 12 - 4 * u;
+                    float2 tA[4], tB[4];
+                    int xA[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        tA[i] = tab[kTabA1 + 4 * i + u];
+                        tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
+                        xA[i] = 16 * (i ^ av);
                     }
-                }
-                if (et == 0) {  // k = 8192, its own mirror
-                    const float2 y = stg_value(stg, kMA / 2);
-                    float2 zk, zm;
-                    c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
-                    *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
+#pragma unroll
+                    for (int it = 0; it < 16; ++it) {
+                        const int A = it >> 2, B = it & 3;
+                        const int pos = 256 * A + 32 * (B >> 1) + ((B & 1) ? L1 : L0);
+                        const float2 y = nib(stg[pos] >> sh);
+                        float2 ym;
+                        if (n3 != 8) {
+                            ym = nib(stg[pos ^ 2030] >> shm);
+                        } else {  // k % 8 = 0: the mirror's word is 2048 - w
+                            const int k = 512 * (4 * A + u) + 16 * (8 * B + av) + 8;
+                            ym = stg_value(stg, kMA - k);
+                        }
+                        float2 zk, zm;
+                        c2r_pair(y, ym, cmul(tA[A], tB[B]), zk, zm);
+                        *reinterpret_cast<uint32_t *>(S + 1024 * B + xA[A]) = pack_half2(zk.x, zk.y);
+                        *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA[A]) = pack_half2(zm.x, zm.y);
+                    }
+                } else {
+#pragma unroll 1
+                    for (int it = 0; it < 16; ++it) {
+                        const int n1 = 4 * (it >> 2) + u, n2 = 8 * (it & 3) + av;
+                        const int np = 16 * n2, k = 512 * n1 + np;
+                        float2 y = stg_value(stg, k);
+                        float2 ym = make_float2(0.f, 0.f);
+                        const int km = kMA - k;
+                        if (k == 0)
+                            y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
+                        else
+                            ym = stg_value(stg, km);
+                        float2 zk, zm;
+                        c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
+                        *reinterpret_cast<uint32_t *>(op + sw128_off(n2, n1)) = pack_half2(zk.x, zk.y);
+                        if (k != 0) {
+                            const int n1m = km >> 9, npm = km & 511;
+                            *reinterpret_cast<uint32_t *>(op + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
+                                pack_half2(zm.x, zm.y);
+                        }
+                    }
+                    if (lane == 0) {  // k = 8192, its own mirror
+                        const float2 y = stg_value(stg, kMA / 2);
+                        float2 zk, zm;
+                        c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
+                        *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
+                    }
                 }
             } else {
                 const int np = et;
@@ -414,8 +471,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                             y.y = 0.f;
                             ym.y = 0.f;
                         }
-                        y = make_float2(0.5f * y.x, 0.5f * y.y);
-                        ym = make_float2(0.5f * ym.x, 0.5f * ym.y);
                         float2 a0, a1;
                         c2r_pair(y, ym, cmul(tab[kTabA1 + n1], wb), a0, a1);
                         zk[i] = pack_half2(a0.x, a0.y);
@@ -433,8 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                     }
                 }
                 if (et == 0) {  // k = 8192, its own mirror
-                    float2 y = h2f(stg[kMA / 2]);
-                    y = make_float2(0.5f * y.x, 0.5f * y.y);
+                    const float2 y = h2f(stg[kMA / 2]);
                     float2 zk, zm;
                     c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
                     *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
@@ -442,8 +496,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             }
         };
 
-        // ---- stage 1 -> stage-2 operand (row 16 k1 + n3, K n2) --------------------
-        auto epi1 = [&](int j, uint8_t *dst) {
+        // This group's 8 of a row's 32 DFT outputs (columns 16 grp .. +16),
+        // times w0 b^(8 grp + i): two interleaved twiddle chains (steps b^2)
+        // keep the multiplies independent.
+        auto twiddled8 = [&](uint32_t t, float2 b, float2 w0, uint8_t *d0) {
+            uint32_t r0[8], r1[8];
+            tmem_ld8(t + 16 * ep.grp, r0);
+            tmem_ld8(t + 16 * ep.grp + 8, r1);
+            const float2 b2 = cmul(b, b), b4 = cmul(b2, b2), b8 = cmul(b4, b4);
+            float2 w = w0;
+            for (int g = 0; g < ep.grp; ++g) w = cmul(w, b8);
+            float2 wa = w, wb = cmul(w, b);
+            tmem_wait<8>(r0, r1);
+#pragma unroll
+            for (int i = 0; i < 8; i += 2) {
+                const float2 y0 = cmul(acc2(i < 4 ? r0 : r1, i & 3), wa);
+                const float2 y1 = cmul(acc2(i < 4 ? r0 : r1, (i & 3) + 1), wb);
+                wa = cmul(wa, b2);
+                wb = cmul(wb, b2);
+                *reinterpret_cast<uint32_t *>(d0 + 2048 * (8 * ep.grp + i)) = pack_half2(y0.x, y0.y);
+                *reinterpret_cast<uint32_t *>(d0 + 2048 * (8 * ep.grp + i + 1)) = pack_half2(y1.x, y1.y);
+            }
+        };
+        // ---- stage 1 -> stage-2 operand: row 16 k1 + n3, K n2, at
+        // 2048 k1 + (offset of row n3, K n2) in the 128-byte swizzle
+        auto epi1 = [&](int j, uint32_t t, uint8_t *dst) {
             int n2, n3;
             if constexpr (!kBins) {  // row n' = 16 lane + n3, n3 = 4 j + q
                 n3 = 4 * j + q;
@@ -453,60 +530,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                 n3 = np & 15;
                 n2 = np >> 4;
             }
-            const float2 b = tab[kTabB + 16 * n2 + n3];
-            float2 w = make_float2(kBins ? kScaleC1 : 1.f, 0.f);
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {  // k1 in [8h, 8h + 8)
-                uint32_t hi[16], lo[16];
-                tmem_ld16(tl + 16 * h, hi);
-                tmem_ld16(tl + 64 + 16 * h, lo);
-                tmem_wait<16>(hi, lo);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k1 = 8 * h + i;
-                    const float2 y = cmul(hilo(hi, lo, i), w);
-                    w = cmul(w, b);
-                    *reinterpret_cast<uint32_t *>(dst + sw128_off(16 * k1 + n3, n2)) = pack_half2(y.x, y.y);
-                }
-            }
+            const int np = 16 * n2 + n3;
+            twiddled8(t, tab[kTabB + np + (np >> 4)], make_float2(kBins ? kScaleC1 : 1.f, 0.f),
+                      dst + sw128_off(n3, n2));
         };
-        // ---- stage 2 -> stage-3 operand (row 32 k2 + k1, K n3) --------------------
-        auto epi2 = [&](int j, uint8_t *dst) {
+        // ---- stage 2 -> stage-3 operand: row 32 k2 + k1, K n3, at
+        // 2048 k2 + (offset of row k1, K n3) in the 64-byte swizzle
+        auto epi2 = [&](int j, uint32_t t, uint8_t *dst) {
             const int r = 128 * j + 32 * q + lane, k1 = r >> 4, n3 = r & 15;
-            const float2 b = tab[kTabC + n3];
-            float2 w = make_float2(kBins ? kScaleC2 : 1.f, 0.f);
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                uint32_t hi[16], lo[16];
-                tmem_ld16(tl + 16 * h, hi);
-                tmem_ld16(tl + 64 + 16 * h, lo);
-                tmem_wait<16>(hi, lo);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k2 = 8 * h + i;
-                    const float2 y = cmul(hilo(hi, lo, i), w);
-                    w = cmul(w, b);
-                    *reinterpret_cast<uint32_t *>(dst + sw64_off(32 * k2 + k1, n3)) = pack_half2(y.x, y.y);
-                }
-            }
+            // stage A's FP16 time series is a quarter of the unnormalised value
+            twiddled8(t, tab[kTabC + n3], make_float2(kBins ? kScaleC2 : (OUT == OUT_TS_HALF ? kScaleA : 1.f), 0.f),
+                      dst + sw64_off(k1, n3));
         };
         // ---- stage 3 -> output.  Row 32 k2 + k1 = 128 j + 32 q + lane, column k3:
         // z[m], m = k1 + 32 k2 + 1024 k3, = samples (2m, 2m + 1); a warp covers 32
         // consecutive m.
-        float f1 = 0.f, f2 = 0.f;  // OUT_QUANT_SUMS: this thread's sums over the chunk
+        float f1 = 0.f, f2 = 0.f;  // OUT_QUANT_SUMS: this thread's sums over the chunk (scaled values)
         double d1 = 0.0, d2 = 0.0; // OUT_FLOAT_MOMENTS
-        auto epi3 = [&](int j, const SegInv &s, int64_t pol, int64_t loc) {
+        auto epi3 = [&](int j, uint32_t t, const SegInv &s, int64_t pol, int64_t loc) {
             const int r = 128 * j + 32 * q + lane;
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);
+            tmem_ld16(t + 16, r1);
+            tmem_wait<16>(r0, r1);
             float2 v[16];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                uint32_t hi[16], lo[16];
-                tmem_ld16(tl + 16 * h, hi);
-                tmem_ld16(tl + 32 + 16 * h, lo);
-                tmem_wait<16>(hi, lo);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[8 * h + i] = hilo(hi, lo, i);
-            }
+            for (int i = 0; i < 16; ++i) v[i] = acc2(i < 8 ? r0 : r1, i & 7);
             if constexpr (OUT == OUT_TS_HALF || OUT == OUT_TS_FLOAT) {
                 const int64_t off = pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA);
 #pragma unroll
@@ -514,7 +563,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                     const int m = r + 1024 * i;
                     if constexpr (OUT == OUT_TS_HALF)
                         __stcs(reinterpret_cast<unsigned int *>(static_cast<__half *>(s.out) + off) + m,
-                               pack_half2(kScaleA * v[i].x, kScaleA * v[i].y));
+                               pack_half2(v[i].x, v[i].y));
                     else
                         __stcs(reinterpret_cast<float2 *>(static_cast<float *>(s.out) + off) + m, v[i]);
                 }
@@ -529,23 +578,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                         d2 += static_cast<double>(x.x) * x.x + static_cast<double>(x.y) * x.y;
                     }
                 }
-            } else {  // 2-bit codes: sample 2m at bits 4 (m % 8) of word m / 8 (m % 8 = lane % 8)
+            } else {
+                // 2-bit codes against thresholds scaled like the values (powers
+                // of two: the same codes as on the unscaled values).  Word
+                // (r >> 3) + 128 k3 holds outputs r' + 1024 k3 of the 8 lanes
+                // r' = r & ~7 .. + 7 (lane c at bits 4c); each lane builds its
+                // codes of k3 < 8 and k3 >= 8 as two words (k3 at bits 4 (k3 % 8)),
+                // an 8 x 8 nibble transpose over the 8 lanes leaves lane c with
+                // the words of k3 = c and 8 + c.
                 uint32_t *words = reinterpret_cast<uint32_t *>(s.o.out + pol * s.o.out_pol_stride +
                                                                (s.o.pkt0 + loc) * s.o.pkt_stride + s.o.payload_off);
-                const float th = s.o.thr[pol], off = s.o.thr[2 + pol];
+                const float th = kRescaleC * s.o.thr[pol], off = kRescaleC * s.o.thr[2 + pol];
+                uint32_t wl = 0, wh = 0;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const float2 x = make_float2(kUnscaleC * v[i].x, kUnscaleC * v[i].y);
-                    if constexpr (OUT == OUT_QUANT_SUMS) {
-                        f1 += x.x + x.y;
-                        f2 = fmaf(x.x, x.x, fmaf(x.y, x.y, f2));
-                    }
-                    uint32_t nib = (code2(x.x, th, off) | (code2(x.y, th, off) << 2)) << (4 * (lane & 7));
-                    nib |= __shfl_xor_sync(0xffffffffu, nib, 1);
-                    nib |= __shfl_xor_sync(0xffffffffu, nib, 2);
-                    nib |= __shfl_xor_sync(0xffffffffu, nib, 4);
-                    if ((lane & 7) == 0) words[(r + 1024 * i) >> 3] = nib;
+                for (int i = 0; i < 8; ++i) {
+                    wl |= (code2(v[i].x, th, off) | (code2(v[i].y, th, off) << 2)) << (4 * i);
+                    wh |= (code2(v[8 + i].x, th, off) | (code2(v[8 + i].y, th, off) << 2)) << (4 * i);
                 }
+                if constexpr (OUT == OUT_QUANT_SUMS) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        f1 += v[i].x + v[i].y;
+                        f2 = fmaf(v[i].x, v[i].x, fmaf(v[i].y, v[i].y, f2));
+                    }
+                }
+                const int c = lane & 7;
+                wl = nib_transpose8(wl, c);
+                wh = nib_transpose8(wh, c);
+                words[(r >> 3) + 128 * c] = wl;
+                words[(r >> 3) + 128 * (8 + c)] = wh;
             }
         };
         // Per-chunk statistics of stage C (all epilogue warps, after stage 3).
@@ -556,9 +617,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                 if constexpr (OUT == OUT_FLOAT_MOMENTS) {
                     s1 = warp_sum(d1);
                     s2 = warp_sum(d2);
-                } else {
-                    s1 = static_cast<double>(warp_sum_f(f1));
-                    s2 = static_cast<double>(warp_sum_f(f2));
+                } else {  // sums of the scaled values: x 2^21 and x 2^42 (exact)
+                    s1 = static_cast<double>(warp_sum_f(f1)) * kUnscaleC;
+                    s2 = static_cast<double>(warp_sum_f(f2)) * kUnscaleC * kUnscaleC;
                 }
                 if (lane == 0) {
                     red[e] = s1;
@@ -598,9 +659,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             fetch(blockIdx.x + gridDim.x);
         }
         for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-            ep.tiles(4, [&](int j) { epi1(j, X(p ^ 1)); });
+            ep.tiles_all(4, [&](int j, uint32_t t) { epi1(j, t, X(p ^ 1)); });
             ep.publish(p ^ 1);
-            ep.tiles(4, [&](int j) { epi2(j, X(p)); });
+            ep.tiles_all(4, [&](int j, uint32_t t) { epi2(j, t, X(p)); });
             ep.publish(p);
             // every stage-2 MMA has retired (each group saw its tiles' commits),
             // so operand p ^ 1 takes the next item's input
@@ -616,7 +677,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             const SegInv &s = a.s[seg_index(a, item)];
             const int64_t local = item - s.item0;
             const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
-            ep.tiles(8, [&](int j) { epi3(j, s, pol, loc); });
+            ep.tiles(8, [&](int j, uint32_t t) { epi3(j, t, s, pol, loc); });
             chunk_stats(s, pol, loc);
         }
     }
@@ -686,19 +747,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             const uint32_t g16 = smem_u32(sm + kFwdOffG), g8 = g16 + kG16f, g11 = g8 + kG8f, g13 = g11 + kG11f;
             const uint32_t x0 = smem_u32(X0), x1 = smem_u32(X1);
             for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-                is.stage(1, x1, 9, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 64);     // DFT-16
-                is.stage(0, x0, 18, 4096, 1, 32, 16, 256, kSwizzle32, g8, 256, 32);     // DFT-8
-                is.stage(1, x1, 13, 6144, 2, 256, 128, 384, kNoSwizzle, g11, 512, 64);  // DFT-11
-                is.stage(0, x0, 11, 8192, 2, 32, 16, 512, kSwizzle64, g13, 512, 64);    // DFT-13
+                is.stage(1, x1, 9, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);     // DFT-16
+                is.stage(0, x0, 18, 4096, 1, 32, 16, 256, kSwizzle32, g8, 256, 512, 16);      // DFT-8
+                is.stage(1, x1, 13, 6144, 2, 256, 128, 384, kNoSwizzle, g11, 512, 2048, 32);  // DFT-11
+                is.stage(0, x0, 11, 8192, 2, 32, 16, 512, kSwizzle64, g13, 512, 2048, 32);    // DFT-13
             }
             is.finish();
         }
         __syncwarp();
     } else {
         Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
-               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>((warp - 1) >> 2) * 128};
+               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
         const int e = warp - 1, q = ep.q, et = ep.et;
-        const uint32_t tl = ep.tl;
         const uint32_t *raw = reinterpret_cast<const uint32_t *>(X0);
         uint32_t *Z = reinterpret_cast<uint32_t *>(X1);
 
@@ -730,108 +790,90 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                 nA -= nA >= 143 ? 143 : 0;
                 int base = 128 * nA + 143 * n8;
                 base -= base >= kMB ? kMB : 0;
-                const int row = 8 * nAp + n8;
+                uint8_t *rowp = X1 + 64 * (8 * nAp + n8);
+                const int rx = ((8 * nAp + n8) >> 1) & 3;
 #pragma unroll 4
                 for (int i = 0; i < 16; ++i) {
                     const int n16 = (i + (lane >> 3)) & 15;
                     int n = base + 1144 * n16;
                     n -= n >= kMB ? kMB : 0;
-                    *reinterpret_cast<uint32_t *>(X1 + sw64_off(row, n16)) = raw[n];
+                    *reinterpret_cast<uint32_t *>(rowp + ((((n16 >> 2) ^ rx) & 3) << 4) + (n16 & 3) * 4) = raw[n];
                 }
             }
         };
         // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row nA' + 143 k16, K n8
-        auto epi1 = [&](int j) {
+        // (the whole of stage B's 2^-8 in the twiddle's start value)
+        auto epi1 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
             const bool ok = nAp < 143;
-            const float2 b = tab[kTabW128 + n8];
-            float2 w = make_float2(kScaleB1, 0.f);
+            const float2 b = tab[kTabW128 + n8], b2 = cmul(b, b);
+            float2 wa = make_float2(kScaleB, 0.f), wb = make_float2(kScaleB * b.x, kScaleB * b.y);
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);
+            tmem_ld16(t + 16, r1);
+            tmem_wait<16>(r0, r1);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                uint32_t hi[16], lo[16];
-                tmem_ld16(tl + 16 * h, hi);
-                tmem_ld16(tl + 32 + 16 * h, lo);
-                tmem_wait<16>(hi, lo);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k16 = 8 * h + i;
-                    const float2 y = cmul(hilo(hi, lo, i), w);
-                    w = cmul(w, b);
-                    if (ok) *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y.x, y.y);
+            for (int k16 = 0; k16 < 16; k16 += 2) {  // two twiddle chains, steps b^2
+                const float2 y0 = cmul(acc2(k16 < 8 ? r0 : r1, k16 & 7), wa);
+                const float2 y1 = cmul(acc2(k16 < 8 ? r0 : r1, (k16 & 7) + 1), wb);
+                wa = cmul(wa, b2);
+                wb = cmul(wb, b2);
+                if (ok) {
+                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y0.x, y0.y);
+                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * (k16 + 1), n8)) = pack_half2(y1.x, y1.y);
                 }
             }
         };
-        // B2: DFT-8 out (k8), rows nA' + 143 k16 -> B3 operand row n13 + 13 (k16 + 16 k8), K n11
-        auto epi2 = [&](int j) {
+        // B2: DFT-8 out (k8), rows nA' + 143 k16 -> B3 operand row n13 + 13 (k16 + 16 k8), K n11:
+        // 208 rows (26 row groups of 384 bytes) per k8
+        auto epi2 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane;
             const bool ok = r < 2288;
             const int k16 = r / 143, nAp = r - 143 * k16, n11 = nAp / 13, n13 = nAp - 13 * n11;
-            uint32_t hi[16], lo[16];
-            tmem_ld16(tl, hi);
-            tmem_ld16(tl + 16, lo);
-            tmem_wait<16>(hi, lo);
+            uint32_t r0[16];
+            tmem_ld16(t, r0);
+            tmem_wait1<16>(r0);
+            uint8_t *d0 = X1 + k24_off(n13 + 13 * k16, n11);
 #pragma unroll
             for (int k8 = 0; k8 < 8; ++k8) {
-                const float2 v = hilo(hi, lo, k8);
-                if (ok)
-                    *reinterpret_cast<uint32_t *>(X1 + k24_off(n13 + 13 * (k16 + 16 * k8), n11)) =
-                        pack_half2(kScaleB2 * v.x, kScaleB2 * v.y);
+                const float2 v = acc2(r0, k8);
+                if (ok) *reinterpret_cast<uint32_t *>(d0 + 9984 * k8) = pack_half2(v.x, v.y);
             }
         };
         // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13
-        auto epi3 = [&](int j) {
+        auto epi3 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, kB = r / 13, n13 = r - 13 * kB;
-            uint32_t hi[16], lo[16];
-            tmem_ld16(tl, hi);        // hi: columns 0..21 (k11 < 8 here)
-            tmem_ld16(tl + 32, lo);   // lo: columns 32..53
-            tmem_wait<16>(hi, lo);
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);       // k11 = 0..7
+            tmem_ld16(t + 16, r1);  // k11 = 8..10 (+ zero columns)
+            tmem_wait<16>(r0, r1);
+            uint8_t *d0 = X0 + sw64_off(kB, n13);
 #pragma unroll
-            for (int k11 = 0; k11 < 8; ++k11) {
-                const float2 v = hilo(hi, lo, k11);
-                *reinterpret_cast<uint32_t *>(X0 + sw64_off(128 * k11 + kB, n13)) =
-                    pack_half2(kScaleB3 * v.x, kScaleB3 * v.y);
-            }
-            uint32_t hi2[8], lo2[8];
-            tmem_ld8(tl + 16, hi2);   // k11 = 8..11 (11 unused)
-            tmem_ld8(tl + 48, lo2);
-            tmem_wait<8>(hi2, lo2);
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                const float2 v = hilo(hi2, lo2, i);
-                *reinterpret_cast<uint32_t *>(X0 + sw64_off(128 * (8 + i) + kB, n13)) =
-                    pack_half2(kScaleB3 * v.x, kScaleB3 * v.y);
+            for (int k11 = 0; k11 < 11; ++k11) {
+                const float2 v = acc2(k11 < 8 ? r0 : r1, k11 & 7);
+                *reinterpret_cast<uint32_t *>(d0 + 8192 * k11) = pack_half2(v.x, v.y);
             }
         };
         // B4: DFT-13 out (k13), rows 128 k11 + kB -> Z[k], k = (2432 kA + 15873 kB) mod N,
         // kA = (78 k11 + 66 k13) mod 143: k advances by 14080 per k13.
-        auto epi4 = [&](int j) {
+        auto epi4 = [&](int j, uint32_t t) {
             const int kB = 32 * q + lane;
             const int kA0 = (78 * j) % 143;
             int k = (2432 * kA0 + 15873 * kB) % kMB;
-            uint32_t hi[16], lo[16];
-            tmem_ld16(tl, hi);        // hi: columns 0..25
-            tmem_ld16(tl + 32, lo);   // lo: columns 32..57
-            tmem_wait<16>(hi, lo);
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);
+            tmem_ld16(t + 16, r1);
+            tmem_wait<16>(r0, r1);
 #pragma unroll
-            for (int k13 = 0; k13 < 8; ++k13) {
-                const float2 v = hilo(hi, lo, k13);
-                Z[k] = pack_half2(kScaleB4 * v.x, kScaleB4 * v.y);
-                k += 14080;
-                k -= k >= kMB ? kMB : 0;
-            }
-            uint32_t hi2[16], lo2[16];
-            tmem_ld16(tl + 16, hi2);
-            tmem_ld16(tl + 48, lo2);
-            tmem_wait<16>(hi2, lo2);
-#pragma unroll
-            for (int i = 0; i < 5; ++i) {  // k13 = 8..12
-                const float2 v = hilo(hi2, lo2, i);
-                Z[k] = pack_half2(kScaleB4 * v.x, kScaleB4 * v.y);
+            for (int k13 = 0; k13 < 13; ++k13) {
+                const float2 v = acc2(k13 < 8 ? r0 : r1, k13 & 7);
+                Z[k] = pack_half2(v.x, v.y);
                 k += 14080;
                 k -= k >= kMB ? kMB : 0;
             }
         };
-        // R2C pairing: bins q = skip + jj, jj = 0..16384, from Z[q], Z[N - q]
+        // R2C pairing: bins q = skip + jj, jj = 0..16384, from Z[q], Z[N - q];
+        // half of each bin (stage C's C2R pairing factor), FP16 to global.
         auto pairing = [&](const SegFwd &s, int64_t pol, int64_t loc) {
             uint32_t *yo = s.out + pol * s.out_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen);
 #pragma unroll 1
@@ -840,12 +882,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                 float2 y;
                 if (qq == 0 || qq == kMB) {
                     const float2 z0 = h2f(Z[0]);
-                    y = make_float2(qq == 0 ? z0.x + z0.y : z0.x - z0.y, 0.f);
+                    y = make_float2(0.5f * (qq == 0 ? z0.x + z0.y : z0.x - z0.y), 0.f);
                 } else {
                     const float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
-                    float2 xq, xm;
-                    r2c_pair(h2f(Z[qq]), h2f(Z[kMB - qq]), w, xq, xm);
-                    y = xq;
+                    const float2 za = h2f(Z[qq]), zb = h2f(Z[kMB - qq]);
+                    const float2 sv = make_float2(za.x + zb.x, za.y - zb.y);
+                    const float2 tv = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
+                    y = make_float2(0.25f * (sv.x + tv.y), 0.25f * (sv.y - tv.x));
                 }
                 __stcs(yo + jj, pack_half2(y.x, y.y));
             }
@@ -856,13 +899,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             ep.wait_staging();
             input();
             ep.publish(1);
-            ep.tiles(9, [&](int j) { epi1(j); });
+            ep.tiles(9, [&](int j, uint32_t t) { epi1(j, t); });
             ep.publish(0);
-            ep.tiles(18, [&](int j) { epi2(j); });
+            ep.tiles(18, [&](int j, uint32_t t) { epi2(j, t); });
             ep.publish(1);
-            ep.tiles(13, [&](int j) { epi3(j); });
+            ep.tiles(13, [&](int j, uint32_t t) { epi3(j, t); });
             ep.publish(0);
-            ep.tiles(11, [&](int j) { epi4(j); });
+            ep.tiles(11, [&](int j, uint32_t t) { epi4(j, t); });
             named_sync_epi();  // Z complete; every DFT-13 MMA retired: X0 takes the next chunk
             fetch(item + gridDim.x);
             int64_t pol, loc;
@@ -941,7 +984,7 @@ std::vector<uint8_t> build_blob() {
     std::vector<float2> ti(kInvTabLen, make_float2(0.f, 0.f));
     for (int i = 0; i <= 16; ++i) ti[kTabA1 + i] = cis(i, 64);
     for (int i = 0; i < 512; ++i) ti[kTabA2 + i] = cis(i, 32768);
-    for (int i = 0; i < 512; ++i) ti[kTabB + i] = cis(i, 16384);
+    for (int i = 0; i < 512; ++i) ti[kTabB + i + (i >> 4)] = cis(i, 16384);
     for (int i = 0; i < 16; ++i) ti[kTabC + i] = cis(i, 512);
     append(blob, ti);
     append(blob, dft_matrix_hilo(16, -1, 32, 32, 64));

@@ -48,6 +48,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive_n(uint64_t *mbar, uint32_t n) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(n) : "memory");
+}
+
+// 8 TMEM columns of this thread's lane, no wait.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
 // Bounded wait for the phase with parity `parity`; false on time-out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int limit = 1 << 22) {
     uint32_t done = 0;
@@ -84,6 +95,14 @@ __device__ __forceinline__ void tmem_wait(uint32_t *a, uint32_t *b) {
         asm volatile("" : "+r"(a[i]), "+r"(a[i + 1]), "+r"(a[i + 2]), "+r"(a[i + 3]));
         asm volatile("" : "+r"(b[i]), "+r"(b[i + 1]), "+r"(b[i + 2]), "+r"(b[i + 3]));
     }
+}
+
+// The same for one array of N registers.
+template <int N>
+__device__ __forceinline__ void tmem_wait1(uint32_t *a) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < N; i += 4) asm volatile("" : "+r"(a[i]), "+r"(a[i + 1]), "+r"(a[i + 2]), "+r"(a[i + 3]));
 }
 
 // Byte offset of the complex element (row, kc) of a K-major FP16 operand whose
