@@ -92,8 +92,8 @@ constexpr uint32_t kFwdX1 = 80896;                  // DFT-16 operand, DFT-11 op
 constexpr uint32_t kG16f = 64 * 32 * 2, kG8f = 32 * 16 * 2, kG11f = 64 * 32 * 2, kG13f = 64 * 32 * 2;
 constexpr uint32_t kFwdOffG = kFwdX0 + kFwdX1;
 constexpr uint32_t kFwdOffTab = kFwdOffG + kG16f + kG8f + kG11f + kG13f;
-// float2 tables: W_128^n8 (8), W_36608^(128 a) (a <= 143, 144 slots), W_36608^b (b < 128)
-constexpr int kTabW128 = 0, kTabQHi = 8, kTabQLo = kTabQHi + 144, kFwdTabLen = kTabQLo + 128;
+// float2 tables: 2^-8 W_128^e (e < 128), W_36608^(128 a) (a <= 143, 144 slots), W_36608^b (b < 128)
+constexpr int kTabW128 = 0, kTabQHi = 128, kTabQLo = kTabQHi + 144, kFwdTabLen = kTabQLo + 128;
 constexpr uint32_t kFwdSmem = kFwdOffTab + kFwdTabLen * 8 + 1024;
 static_assert(kFwdSmem <= 232448 && inv_smem(true) <= 232448, "shared memory above 227 KB");
 
@@ -133,17 +133,16 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 
 // Common kernel state: barriers, tensor memory, error flag.
 constexpr int kSlots = 8;           // accumulator slots of 64 tensor-memory columns
+constexpr int kFull = 18;           // completion barriers: one per slot, or one per tile of a whole stage
 struct Ctl {
-    uint64_t full[kSlots], empty[kSlots], ready[2], done, stg;
+    uint64_t full[kFull], empty[kSlots], ready[2], done, stg;
     uint32_t tmem_base;
     int err;
 };
 
 __device__ __forceinline__ void ctl_init(Ctl &c) {
-    for (int i = 0; i < kSlots; ++i) {
-        mbar_init(&c.full[i], 1);
-        mbar_init(&c.empty[i], kEpiWarps);  // every epilogue warp's share of the slot drained
-    }
+    for (int i = 0; i < kFull; ++i) mbar_init(&c.full[i], 1);
+    for (int i = 0; i < kSlots; ++i) mbar_init(&c.empty[i], kEpiWarps);  // every epilogue warp's share drained
     mbar_init(&c.ready[0], kEpiWarps);
     mbar_init(&c.ready[1], kEpiWarps);
     mbar_init(&c.done, 1);
@@ -155,39 +154,93 @@ __device__ __forceinline__ void ctl_init(Ctl &c) {
 __device__ __forceinline__ bool err_set(const Ctl &c) { return *reinterpret_cast<const volatile int *>(&c.err) != 0; }
 __device__ __forceinline__ void raise_err(Ctl &c) { *reinterpret_cast<volatile int *>(&c.err) = 1; }
 
-// MMA issuer state (one thread).
+// MMA issuer state.  All of warp 0 runs the issuer (its values are warp
+// uniform, so descriptors stay in uniform registers and cost no issue slots
+// of the epilogue warps' pipes); one elected lane issues each MMA and commit.
 struct Issuer {
     Ctl *c;
-    uint32_t tb, T = 0, uses[2] = {0, 0};
+    uint32_t tb, T = 0, rphase = 0;  // bit b: phase parity of ready[b]
     // One GEMM stage over `tiles` 128-row tiles of the operand in buffer buf
     // (published on ready[buf]): per K-step two MMAs of N columns into the
     // tile's slot, with the hi and the lo half of the DFT matrix (the lo half
-    // g_lo bytes after the hi half), both accumulating.
-    __device__ void stage(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, int ksteps, uint32_t kstep_bytes,
-                          uint32_t lbo, uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo,
-                          int n) {
-        if (!err_set(*c) && !mbar_wait(&c->ready[buf], uses[buf] & 1u)) raise_err(*c);
-        ++uses[buf];
-        fence_after();
+    // g_lo bytes after the hi half), both accumulating.  The start-address
+    // field of a descriptor is its low 14 bits (address / 16, addresses below
+    // 256 KB), so tile and K-step offsets are added to a base descriptor.
+    template <int KSTEPS>
+    __device__ void stage(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, uint32_t kstep_bytes, uint32_t lbo,
+                          uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n) {
+        asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
+        uint64_t gh[KSTEPS], gl[KSTEPS];
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+            gh[ks] = desc(g + ks * 256, 128, g_sbo, kNoSwizzle);
+            gl[ks] = desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle);
+        }
+        const uint64_t x0 = desc(xa, lbo, sbo, layout);
         const uint32_t id = idesc_f16(128, n);
+        if (!err_set(*c) && !mbar_wait(&c->ready[buf], (rphase >> buf) & 1u)) raise_err(*c);
+        rphase ^= 1u << buf;
+        __syncwarp();
+        fence_after();
         for (int j = 0; j < tiles; ++j, ++T) {
             const uint32_t slot = T & (kSlots - 1);
             if (T >= kSlots && !err_set(*c) && !mbar_wait(&c->empty[slot], ((T / kSlots) - 1) & 1u)) raise_err(*c);
+            __syncwarp();
             fence_after();
             if (!err_set(*c)) {
                 const uint32_t d = tb + slot * 64;
-                for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint64_t xd = desc(xa + j * tile_bytes + ks * kstep_bytes, lbo, sbo, layout);
-                    mma_f16(d, xd, desc(g + ks * 256, 128, g_sbo, kNoSwizzle), id, ks > 0);
-                    mma_f16(d, xd, desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle), id, true);
+                const uint64_t xj = x0 + ((j * tile_bytes) >> 4);
+#pragma unroll
+                for (int ks = 0; ks < KSTEPS; ++ks) {
+                    const uint64_t xd = xj + ((ks * kstep_bytes) >> 4);
+                    mma_f16_elect(d, xd, gh[ks], id, ks > 0);
+                    mma_f16_elect(d, xd, gl[ks], id, true);
                 }
             }
-            commit(&c->full[slot]);
+            commit_elect(&c->full[slot]);
+        }
+    }
+    // The whole-stage form: every tile of the stage has its own accumulator
+    // (tile j at column j * col_w) and completion barrier full[j], so the
+    // stage issues without waiting; the epilogue's publish of the next
+    // operand (after its last tensor-memory read) orders the next stage's
+    // writes after this stage's reads.
+    template <int KSTEPS>
+    __device__ void stage_all(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, uint32_t kstep_bytes, uint32_t lbo,
+                              uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n,
+                              uint32_t col_w) {
+        asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
+        uint64_t gh[KSTEPS], gl[KSTEPS];
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+            gh[ks] = desc(g + ks * 256, 128, g_sbo, kNoSwizzle);
+            gl[ks] = desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle);
+        }
+        const uint64_t x0 = desc(xa, lbo, sbo, layout);
+        const uint32_t id = idesc_f16(128, n);
+        if (!err_set(*c) && !mbar_wait(&c->ready[buf], (rphase >> buf) & 1u)) raise_err(*c);
+        rphase ^= 1u << buf;
+        __syncwarp();
+        fence_after();
+        const bool ok = !err_set(*c);
+        for (int j = 0; j < tiles; ++j) {
+            if (ok) {
+                const uint32_t d = tb + j * col_w;
+                const uint64_t xj = x0 + ((j * tile_bytes) >> 4);
+#pragma unroll
+                for (int ks = 0; ks < KSTEPS; ++ks) {
+                    const uint64_t xd = xj + ((ks * kstep_bytes) >> 4);
+                    mma_f16_elect(d, xd, gh[ks], id, ks > 0);
+                    mma_f16_elect(d, xd, gl[ks], id, true);
+                }
+            }
+            commit_elect(&c->full[j]);
         }
     }
     __device__ void finish() {  // every MMA retired before tensor memory is freed
-        commit(&c->done);
+        commit_elect(&c->done);
         if (!mbar_wait(&c->done, 0)) raise_err(*c);
+        __syncwarp();
     }
 };
 
@@ -228,6 +281,38 @@ struct Epi {
                 f(j, taddr());
                 release_tile(4);
             }
+    }
+    // Whole-stage form: phase parity of full[j] in bit j, flipped for every
+    // tile of a stage when the stage is done (whether or not this warp waited).
+    uint32_t fbits = 0;
+    __device__ void wait_full(int j) {
+        if (!err_set(*c) && !mbar_wait(&c->full[j], (fbits >> j) & 1u)) raise_err(*c);
+        fence_after();
+    }
+    // Runs f(j, accumulator address of tile j) on every tile of a whole stage.
+    template <class F>
+    __device__ void stage_all(int n, uint32_t col_w, F f) {
+        for (int j = 0; j < n; ++j) {
+            wait_full(j);
+            f(j, tq + j * col_w);
+        }
+        fbits ^= (1u << n) - 1u;
+    }
+    // Runs f(j, ...) on the tiles j = grp + rot (mod 4) of a whole stage.
+    template <class F>
+    __device__ void stage_group(int n, uint32_t col_w, int rot, F f) {
+        for (int j = (grp + rot) & 3; j < n; j += 4) {
+            wait_full(j);
+            f(j, tq + j * col_w);
+        }
+        fbits ^= (1u << n) - 1u;
+    }
+    // The next operand is written and this warp's tensor-memory reads are done.
+    __device__ void publish_all(int buf) {
+        fence_before();
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&c->ready[buf]);
     }
     // Runs f(j, accumulator address) on every tile of a stage of n tiles
     // (f takes this group's quarter of the columns).
@@ -328,18 +413,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
     const uint32_t tb = ctl.tmem_base;
 
     if (warp == 0) {
-        if (lane == 0) {
-            Issuer is{&ctl, tb};
-            const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
-            int p = 0;
-            for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-                is.stage(p, smem_u32(X(p)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
-                is.stage(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 4, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
-                is.stage(p, smem_u32(X(p)), 8, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);
-            }
-            is.finish();
+        Issuer is{&ctl, tb};
+        const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
+        int p = 0;
+        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
+            is.stage<4>(p, smem_u32(X(p)), 4, 16384, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
+            is.stage<4>(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
+            is.stage<2>(p, smem_u32(X(p)), 8, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);
         }
-        __syncwarp();
+        is.finish();
     } else {
         Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
                tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
@@ -742,19 +824,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
     const uint32_t tb = ctl.tmem_base;
 
     if (warp == 0) {
-        if (lane == 0) {
-            Issuer is{&ctl, tb};
-            const uint32_t g16 = smem_u32(sm + kFwdOffG), g8 = g16 + kG16f, g11 = g8 + kG8f, g13 = g11 + kG11f;
-            const uint32_t x0 = smem_u32(X0), x1 = smem_u32(X1);
-            for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-                is.stage(1, x1, 9, 8192, 2, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);     // DFT-16
-                is.stage(0, x0, 18, 4096, 1, 32, 16, 256, kSwizzle32, g8, 256, 512, 16);      // DFT-8
-                is.stage(1, x1, 13, 6144, 2, 256, 128, 384, kNoSwizzle, g11, 512, 2048, 32);  // DFT-11
-                is.stage(0, x0, 11, 8192, 2, 32, 16, 512, kSwizzle64, g13, 512, 2048, 32);    // DFT-13
-            }
-            is.finish();
+        Issuer is{&ctl, tb};
+        const uint32_t g16 = smem_u32(sm + kFwdOffG), g8 = g16 + kG16f, g11 = g8 + kG8f, g13 = g11 + kG11f;
+        const uint32_t x0 = smem_u32(X0), x1 = smem_u32(X1);
+        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+            is.stage_all<2>(1, x1, 9, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);     // DFT-16
+            is.stage_all<1>(0, x0, 18, 4096, 32, 16, 256, kSwizzle32, g8, 256, 512, 16, 16);      // DFT-8
+            is.stage_all<2>(1, x1, 13, 6144, 256, 128, 384, kNoSwizzle, g11, 512, 2048, 32, 32);  // DFT-11
+            is.stage_all<2>(0, x0, 11, 8192, 32, 16, 512, kSwizzle64, g13, 512, 2048, 32, 32);    // DFT-13
         }
-        __syncwarp();
+        is.finish();
     } else {
         Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
                tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
@@ -776,51 +855,63 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             fence_async_smem();
             bulk_g2s(X0, s.in + pol * s.in_pol_stride + loc * static_cast<int64_t>(kNB), kNB * 2, &ctl.stg);
         };
-        // input step: raw (natural order) -> DFT-16 operand.  Thread: row
-        // (nA' = 4 w + lane / 8, n8 = lane % 8); its 16 gathers start at
-        // n16 = lane / 8 so that a warp's loads and stores hit 32 banks.
+        // input step: raw (natural order) -> DFT-16 operand.  A warp writes the
+        // 512-byte row group of one nA' (rows 8 nA' + n8): lane = (n8, 16-byte
+        // chunk c of n16 = 4c .. 4c + 3).  Its i-th gather takes n16 = 4c +
+        // (i + c) % 4, so that the 32 lanes' addresses (15 n8 + 24 ((i + c) % 4)
+        // mod 32) fall in 32 banks; two conditional rotations put the four
+        // values back in n16 order for one 16-byte store.
         auto input = [&]() {
+            const int n8 = lane >> 2, c = lane & 3;
 #pragma unroll 1
-            for (int w = e; w < 36; w += kEpiWarps) {
-                const int nAp = 4 * w + (lane >> 3), n8 = lane & 7;
-                if (nAp >= 143) continue;
+            for (int nAp = e; nAp < 143; nAp += kEpiWarps) {
                 const int n11 = nAp / 13, n13 = nAp - 13 * n11;
                 int nA = 13 * n11 + 11 * n13;
                 nA -= nA >= 143 ? 143 : 0;
                 nA -= nA >= 143 ? 143 : 0;
-                int base = 128 * nA + 143 * n8;
+                int base = 128 * nA + 143 * n8 + 4576 * c;
                 base -= base >= kMB ? kMB : 0;
-                uint8_t *rowp = X1 + 64 * (8 * nAp + n8);
-                const int rx = ((8 * nAp + n8) >> 1) & 3;
-#pragma unroll 4
-                for (int i = 0; i < 16; ++i) {
-                    const int n16 = (i + (lane >> 3)) & 15;
-                    int n = base + 1144 * n16;
+                base -= base >= kMB ? kMB : 0;
+                uint32_t v[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    int n = base + 1144 * ((i + c) & 3);
                     n -= n >= kMB ? kMB : 0;
-                    *reinterpret_cast<uint32_t *>(rowp + ((((n16 >> 2) ^ rx) & 3) << 4) + (n16 & 3) * 4) = raw[n];
+                    v[i] = raw[n];
                 }
+                if (c & 1) {
+                    const uint32_t t = v[3];
+                    v[3] = v[2];
+                    v[2] = v[1];
+                    v[1] = v[0];
+                    v[0] = t;
+                }
+                if (c & 2) {
+                    uint32_t t = v[0];
+                    v[0] = v[2];
+                    v[2] = t;
+                    t = v[1];
+                    v[1] = v[3];
+                    v[3] = t;
+                }
+                *reinterpret_cast<uint4 *>(X1 + 512 * nAp + 64 * n8 + ((c ^ (n8 >> 1)) << 4)) =
+                    make_uint4(v[0], v[1], v[2], v[3]);
             }
         };
-        // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row nA' + 143 k16, K n8
-        // (the whole of stage B's 2^-8 in the twiddle's start value)
+        // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row nA' + 143 k16, K n8.
+        // Group g takes k16 = 4g .. 4g + 3 of every tile; twiddle 2^-8 W_128^(n8 k16)
+        // from the table (8 distinct entries per load, 4 lanes each).
         auto epi1 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
-            const bool ok = nAp < 143;
-            const float2 b = tab[kTabW128 + n8], b2 = cmul(b, b);
-            float2 wa = make_float2(kScaleB, 0.f), wb = make_float2(kScaleB * b.x, kScaleB * b.y);
-            uint32_t r0[16], r1[16];
-            tmem_ld16(t, r0);
-            tmem_ld16(t + 16, r1);
-            tmem_wait<16>(r0, r1);
+            uint32_t r0[8];
+            tmem_ld8(t + 8 * ep.grp, r0);
+            tmem_wait1<8>(r0);
+            if (nAp < 143) {
 #pragma unroll
-            for (int k16 = 0; k16 < 16; k16 += 2) {  // two twiddle chains, steps b^2
-                const float2 y0 = cmul(acc2(k16 < 8 ? r0 : r1, k16 & 7), wa);
-                const float2 y1 = cmul(acc2(k16 < 8 ? r0 : r1, (k16 & 7) + 1), wb);
-                wa = cmul(wa, b2);
-                wb = cmul(wb, b2);
-                if (ok) {
-                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y0.x, y0.y);
-                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * (k16 + 1), n8)) = pack_half2(y1.x, y1.y);
+                for (int i = 0; i < 4; ++i) {
+                    const int k16 = 4 * ep.grp + i;
+                    const float2 y = cmul(acc2(r0, i), tab[kTabW128 + ((n8 * k16) & 127)]);
+                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y.x, y.y);
                 }
             }
         };
@@ -834,25 +925,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             tmem_ld16(t, r0);
             tmem_wait1<16>(r0);
             uint8_t *d0 = X1 + k24_off(n13 + 13 * k16, n11);
+            if (ok) {
 #pragma unroll
-            for (int k8 = 0; k8 < 8; ++k8) {
-                const float2 v = acc2(r0, k8);
-                if (ok) *reinterpret_cast<uint32_t *>(d0 + 9984 * k8) = pack_half2(v.x, v.y);
+                for (int k8 = 0; k8 < 8; ++k8) {
+                    const float2 v = acc2(r0, k8);
+                    *reinterpret_cast<uint32_t *>(d0 + 9984 * k8) = pack_half2(v.x, v.y);
+                }
             }
         };
-        // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13
+        // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13.
+        // Group g takes k11 = g, g + 4, g + 8 (< 11) of every tile.
         auto epi3 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, kB = r / 13, n13 = r - 13 * kB;
-            uint32_t r0[16], r1[16];
-            tmem_ld16(t, r0);       // k11 = 0..7
-            tmem_ld16(t + 16, r1);  // k11 = 8..10 (+ zero columns)
-            tmem_wait<16>(r0, r1);
-            uint8_t *d0 = X0 + sw64_off(kB, n13);
-#pragma unroll
-            for (int k11 = 0; k11 < 11; ++k11) {
-                const float2 v = acc2(k11 < 8 ? r0 : r1, k11 & 7);
-                *reinterpret_cast<uint32_t *>(d0 + 8192 * k11) = pack_half2(v.x, v.y);
-            }
+            const int g = ep.grp;
+            uint32_t r0[2], r1[2], r2[2];
+            tmem_ld2(t + 2 * g, r0);
+            tmem_ld2(t + 2 * g + 8, r1);
+            tmem_ld2(t + 2 * g + 16, r2);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            asm volatile("" : "+r"(r0[0]), "+r"(r0[1]), "+r"(r1[0]), "+r"(r1[1]));
+            asm volatile("" : "+r"(r2[0]), "+r"(r2[1]));
+            uint8_t *d0 = X0 + sw64_off(kB, n13) + 8192 * g;
+            *reinterpret_cast<uint32_t *>(d0) = pack_half2(__uint_as_float(r0[0]), __uint_as_float(r0[1]));
+            *reinterpret_cast<uint32_t *>(d0 + 8192 * 4) = pack_half2(__uint_as_float(r1[0]), __uint_as_float(r1[1]));
+            if (g < 3)
+                *reinterpret_cast<uint32_t *>(d0 + 8192 * 8) =
+                    pack_half2(__uint_as_float(r2[0]), __uint_as_float(r2[1]));
         };
         // B4: DFT-13 out (k13), rows 128 k11 + kB -> Z[k], k = (2432 kA + 15873 kB) mod N,
         // kA = (78 k11 + 66 k13) mod 143: k advances by 14080 per k13.
@@ -873,24 +971,39 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             }
         };
         // R2C pairing: bins q = skip + jj, jj = 0..16384, from Z[q], Z[N - q];
-        // half of each bin (stage C's C2R pairing factor), FP16 to global.
+        // half of each bin (stage C's C2R pairing factor), FP16 to global.  A
+        // thread takes two consecutive bins per step (one 8-byte store); the
+        // second twiddle is the first times W_36608.
+        auto pair1 = [&](int qq) -> float2 {  // bin qq in {0, N}: real
+            const float2 z0 = h2f(Z[0]);
+            return make_float2(0.5f * (qq == 0 ? z0.x + z0.y : z0.x - z0.y), 0.f);
+        };
+        auto pairw = [&](float2 za, float2 zb, float2 w) -> float2 {
+            const float2 sv = make_float2(za.x + zb.x, za.y - zb.y);
+            const float2 tv = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
+            return make_float2(0.25f * (sv.x + tv.y), 0.25f * (sv.y - tv.x));
+        };
         auto pairing = [&](const SegFwd &s, int64_t pol, int64_t loc) {
             uint32_t *yo = s.out + pol * s.out_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen);
+            const float2 w1 = tab[kTabQLo + 1];
 #pragma unroll 1
-            for (int jj = et; jj <= kMA; jj += kEpiThreads) {
-                const int qq = s.skip + jj;
+            for (int jj = 2 * et; jj < kMA; jj += 2 * kEpiThreads) {
+                const int qq = s.skip + jj;  // qq + 1 < N (skip <= 1920)
+                const float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
+                const float2 za0 = h2f(Z[qq]), za1 = h2f(Z[qq + 1]);
+                const float2 zb1 = h2f(Z[kMB - 1 - qq]);
+                const float2 y0 = qq == 0 ? pair1(0) : pairw(za0, h2f(Z[kMB - qq]), w);
+                const float2 y1 = pairw(za1, zb1, cmul(w, w1));
+                __stcs(reinterpret_cast<uint2 *>(yo + jj), make_uint2(pack_half2(y0.x, y0.y), pack_half2(y1.x, y1.y)));
+            }
+            if (et == 0) {  // bin 16384
+                const int qq = s.skip + kMA;
                 float2 y;
-                if (qq == 0 || qq == kMB) {
-                    const float2 z0 = h2f(Z[0]);
-                    y = make_float2(0.5f * (qq == 0 ? z0.x + z0.y : z0.x - z0.y), 0.f);
-                } else {
-                    const float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
-                    const float2 za = h2f(Z[qq]), zb = h2f(Z[kMB - qq]);
-                    const float2 sv = make_float2(za.x + zb.x, za.y - zb.y);
-                    const float2 tv = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
-                    y = make_float2(0.25f * (sv.x + tv.y), 0.25f * (sv.y - tv.x));
-                }
-                __stcs(yo + jj, pack_half2(y.x, y.y));
+                if (qq == kMB)
+                    y = pair1(qq);
+                else
+                    y = pairw(h2f(Z[qq]), h2f(Z[kMB - qq]), cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]));
+                __stcs(yo + kMA, pack_half2(y.x, y.y));
             }
         };
 
@@ -898,14 +1011,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
         for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
             ep.wait_staging();
             input();
-            ep.publish(1);
-            ep.tiles(9, [&](int j, uint32_t t) { epi1(j, t); });
-            ep.publish(0);
-            ep.tiles(18, [&](int j, uint32_t t) { epi2(j, t); });
-            ep.publish(1);
-            ep.tiles(13, [&](int j, uint32_t t) { epi3(j, t); });
-            ep.publish(0);
-            ep.tiles(11, [&](int j, uint32_t t) { epi4(j, t); });
+            ep.publish_all(1);
+            ep.stage_all(9, 32, [&](int j, uint32_t t) { epi1(j, t); });
+            ep.publish_all(0);
+            ep.stage_group(18, 16, 0, [&](int j, uint32_t t) { epi2(j, t); });
+            ep.publish_all(1);
+            ep.stage_all(13, 32, [&](int j, uint32_t t) { epi3(j, t); });
+            ep.publish_all(0);
+            ep.stage_group(11, 32, 2, [&](int j, uint32_t t) { epi4(j, t); });
+            fence_before();
             named_sync_epi();  // Z complete; every DFT-13 MMA retired: X0 takes the next chunk
             fetch(item + gridDim.x);
             int64_t pol, loc;
@@ -992,7 +1106,10 @@ std::vector<uint8_t> build_blob() {
     append(blob, dft_matrix_hilo(11, -1, 32, 32, 64));
     append(blob, dft_matrix_hilo(13, -1, 32, 32, 64));
     std::vector<float2> tf(kFwdTabLen, make_float2(0.f, 0.f));
-    for (int i = 0; i < 8; ++i) tf[kTabW128 + i] = cis(i, 128, -1);
+    for (int i = 0; i < 128; ++i) {
+        const float2 w = cis(i, 128, -1);
+        tf[kTabW128 + i] = make_float2(kScaleB * w.x, kScaleB * w.y);
+    }
     for (int i = 0; i < 144; ++i) tf[kTabQHi + i] = cis(128.0 * i, 36608, -1);
     for (int i = 0; i < 128; ++i) tf[kTabQLo + i] = cis(i, 36608, -1);
     append(blob, tf);

@@ -34,10 +34,27 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b,
         "l"(a), "l"(b), "r"(idesc), "r"(acc ? 1u : 0u));
 }
 
+// The same, issued by one elected lane of a converged warp (the lowest active
+// lane, the same one every time).
+__device__ __forceinline__ void mma_f16_elect(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, bool acc) {
+    asm volatile(
+        "{\n .reg .pred p, e;\n setp.ne.b32 p, %4, 0;\n elect.sync _|e, 0xffffffff;\n"
+        " @e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc ? 1u : 0u));
+}
+
 // The barrier completes when every tcgen05 operation this thread issued so far has.
 __device__ __forceinline__ void commit(uint64_t *mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
                  : "memory");
+}
+
+// commit() by the elected lane of a converged warp (the lane that issued the MMAs).
+__device__ __forceinline__ void commit_elect(uint64_t *mbar) {
+    asm volatile(
+        "{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n"
+        " @e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}\n" ::"r"(smem_u32(mbar))
+        : "memory");
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
@@ -52,6 +69,11 @@ __device__ __forceinline__ void mbar_arrive_n(uint64_t *mbar, uint32_t n) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(n) : "memory");
 }
 
+// 2 TMEM columns of this thread's lane, no wait.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+}
+
 // 8 TMEM columns of this thread's lane, no wait.
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -59,16 +81,34 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
                  : "r"(taddr));
 }
 
-// Bounded wait for the phase with parity `parity`; false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int limit = 1 << 22) {
-    uint32_t done = 0;
-    for (int it = 0; it < limit && !done; ++it)
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(smem_u32(mbar)), "r"(parity & 1u)
-            : "memory");
-    return done != 0;
+// One try_wait on the phase with parity `parity`: the thread may sleep in it
+// until the phase completes, for at most `hint_ns`.
+__device__ __forceinline__ uint32_t mbar_try(uint64_t *mbar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity & 1u), "r"(hint_ns)
+        : "memory");
+    return done;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase with parity `parity`: sleeps in try_wait rather
+// than spinning (so waiting warps take no issue slots from working ones) and
+// gives up after `limit_ns` of global time; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint64_t limit_ns = 1000000000ull) {
+    if (mbar_try(mbar, parity, 100000u)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try(mbar, parity, 100000u)) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
