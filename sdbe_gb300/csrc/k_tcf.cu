@@ -4,15 +4,17 @@
 //
 // Every GEMM stage is D[row][col] = sum_k X[row][k] G[col][k]: X holds the
 // data as FP16 (re, im) pairs along K (the A operand, 128 rows per MMA), G
-// the real form of the complex DFT matrix split into FP16 hi and lo halves
-// stacked along N ([hi | lo], so the data is read from shared memory once per
-// K-step), and D accumulates in FP32 in tensor memory.  The epilogue adds the
-// hi and lo halves, applies the twiddles in FP32 and rounds to FP16 into the
-// next stage's operand: a transposition in which each thread's row scatters
-// into the next stage's rows.  Row orders are chosen so that most scatters
-// take one shared-memory wavefront per warp.
+// the real form of the complex DFT matrix split into FP16 hi and lo halves,
+// and D accumulates in FP32 in tensor memory: per K-step one MMA with the hi
+// half and one with the lo half into the same accumulator, so the epilogue
+// reads the compensated product directly.  The epilogue applies the
+// twiddles in FP32 and rounds to FP16 into the next stage's operand: a
+// transposition in which each thread's row scatters into the next stage's
+// rows.  Row orders are chosen so that most scatters take one shared-memory
+// wavefront per warp.  A whole stage's tiles accumulate side by side in
+// tensor memory, so the MMAs of a stage issue back to back.
 //
-// Kernels (one CTA per SM, persistent over items):
+// Kernels (persistent over items):
 //  * k_tcf_inv: a 16384-point inverse transform, radices 32 x 32 x 16 in
 //    decimation in time (k = 512 n1 + 16 n2 + n3, m = k1 + 32 k2 + 1024 k3):
 //      stage 1  rows n' = 16 n2 + n3 (512), DFT-32 over n1, twiddle W^(n' k1)
@@ -21,19 +23,21 @@
 //    Stage A's C2R 32768 per snapshot (input: the packed 2-bit spectrum) and
 //    stage C's C2R 32768 per chunk (input: the R2C bins [skip, skip + 16384]
 //    of stage B); the C2R pairing of the 16385 bins into 16384 complex values
-//    is folded into the input step.
+//    is folded into the input step.  Two teams per CTA (an issuer warp and 8
+//    epilogue warps each) take alternate items, each in its own operand
+//    buffer and half of tensor memory, rewriting the operand in place stage
+//    by stage; one team's CUDA-core steps overlap the other's MMAs.
 //  * k_tcf_fwd: stage B's R2C 36608 per chunk, an 18304-point forward
 //    transform of z[p] = x[2p] + i x[2p + 1] in the prime-factor map
 //    18304 = 143 x 128 (143 = 11 x 13, 128 = 16 x 8): four stages DFT-16,
 //    DFT-8, DFT-11, DFT-13 with one twiddle, W_128^(n8 k16), after the first;
-//    then the R2C pairing and the trim to bins [skip, skip + 16384].
+//    then the R2C pairing and the trim to bins [skip, skip + 16384].  Warp 0
+//    issues; warps 1-16 are four epilogue groups of four warps (one per
+//    tensor-memory lane quarter); two operand buffers alternate by stage.
 //
-// Warp 0 issues the MMAs (one thread); warps 1-16 are four epilogue groups of
-// four warps, one per tensor-memory lane quarter; group g drains accumulator
-// slot g (128 columns), tiles taking the slots in turn.  Two operand buffers
-// alternate so that the tensor cores run one stage while the CUDA cores write
-// the next.  Every mbarrier wait is bounded: on time-out the kernel records
-// the failure in `status`, stops waiting and completes.
+// MMAs are issued by an elected lane of a converged issuer warp.  Every
+// mbarrier wait is bounded: on time-out the kernel records the failure in
+// `status`, stops waiting and completes.
 //
 // Fixed power-of-two scales keep every FP16 operand below 2^16 in magnitude
 // for any 2-bit input (per-stage bounds from the input energy: Parseval and
@@ -43,6 +47,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 #include <cstring>
 #include <vector>
 
@@ -83,7 +88,7 @@ constexpr uint32_t kInvOffStg = kInvOffG + kG32Bytes + kG16Bytes;
 // e^{2 pi i n'/16384} (512, at n' + n'/16 so that 16 lanes with n' 16 apart
 // hit distinct banks), e^{2 pi i n3/512} (16)
 constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 544, kInvTabLen = kTabC + 16;
-constexpr uint32_t kStgPacked = 8192, kStgBins = kTcfBinsLen * 4;
+constexpr uint32_t kStgPacked = 2 * 8192, kStgBins = kTcfBinsLen * 4;  // packed: one snapshot per team
 constexpr uint32_t inv_smem(bool bins) { return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + 1024; }
 
 // ---- shared memory of k_tcf_fwd --------------------------------------------
@@ -132,17 +137,15 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 // Common kernel state: barriers, tensor memory, error flag.
-constexpr int kSlots = 8;           // accumulator slots of 64 tensor-memory columns
-constexpr int kFull = 18;           // completion barriers: one per slot, or one per tile of a whole stage
+constexpr int kFull = 18;           // completion barriers, one per tile of a whole stage
 struct Ctl {
-    uint64_t full[kFull], empty[kSlots], ready[2], done, stg;
+    uint64_t full[kFull], ready[2], done, stg;
     uint32_t tmem_base;
     int err;
 };
 
 __device__ __forceinline__ void ctl_init(Ctl &c) {
     for (int i = 0; i < kFull; ++i) mbar_init(&c.full[i], 1);
-    for (int i = 0; i < kSlots; ++i) mbar_init(&c.empty[i], kEpiWarps);  // every epilogue warp's share drained
     mbar_init(&c.ready[0], kEpiWarps);
     mbar_init(&c.ready[1], kEpiWarps);
     mbar_init(&c.done, 1);
@@ -159,48 +162,8 @@ __device__ __forceinline__ void raise_err(Ctl &c) { *reinterpret_cast<volatile i
 // of the epilogue warps' pipes); one elected lane issues each MMA and commit.
 struct Issuer {
     Ctl *c;
-    uint32_t tb, T = 0, rphase = 0;  // bit b: phase parity of ready[b]
-    // One GEMM stage over `tiles` 128-row tiles of the operand in buffer buf
-    // (published on ready[buf]): per K-step two MMAs of N columns into the
-    // tile's slot, with the hi and the lo half of the DFT matrix (the lo half
-    // g_lo bytes after the hi half), both accumulating.  The start-address
-    // field of a descriptor is its low 14 bits (address / 16, addresses below
-    // 256 KB), so tile and K-step offsets are added to a base descriptor.
-    template <int KSTEPS>
-    __device__ void stage(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, uint32_t kstep_bytes, uint32_t lbo,
-                          uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n) {
-        asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
-        uint64_t gh[KSTEPS], gl[KSTEPS];
-#pragma unroll
-        for (int ks = 0; ks < KSTEPS; ++ks) {
-            gh[ks] = desc(g + ks * 256, 128, g_sbo, kNoSwizzle);
-            gl[ks] = desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle);
-        }
-        const uint64_t x0 = desc(xa, lbo, sbo, layout);
-        const uint32_t id = idesc_f16(128, n);
-        if (!err_set(*c) && !mbar_wait(&c->ready[buf], (rphase >> buf) & 1u)) raise_err(*c);
-        rphase ^= 1u << buf;
-        __syncwarp();
-        fence_after();
-        for (int j = 0; j < tiles; ++j, ++T) {
-            const uint32_t slot = T & (kSlots - 1);
-            if (T >= kSlots && !err_set(*c) && !mbar_wait(&c->empty[slot], ((T / kSlots) - 1) & 1u)) raise_err(*c);
-            __syncwarp();
-            fence_after();
-            if (!err_set(*c)) {
-                const uint32_t d = tb + slot * 64;
-                const uint64_t xj = x0 + ((j * tile_bytes) >> 4);
-#pragma unroll
-                for (int ks = 0; ks < KSTEPS; ++ks) {
-                    const uint64_t xd = xj + ((ks * kstep_bytes) >> 4);
-                    mma_f16_elect(d, xd, gh[ks], id, ks > 0);
-                    mma_f16_elect(d, xd, gl[ks], id, true);
-                }
-            }
-            commit_elect(&c->full[slot]);
-        }
-    }
-    // The whole-stage form: every tile of the stage has its own accumulator
+    uint32_t tb, rphase = 0;  // bit b: phase parity of ready[b]
+    // One GEMM stage: every tile of the stage has its own accumulator
     // (tile j at column j * col_w) and completion barrier full[j], so the
     // stage issues without waiting; the epilogue's publish of the next
     // operand (after its last tensor-memory read) orders the next stage's
@@ -244,46 +207,20 @@ struct Issuer {
     }
 };
 
-// Epilogue warp state.  A tile T in slot T % 8 is drained either by group
-// T % 4 alone (tiles(): each of its warps releases four shares of the slot)
-// or by all four groups, a quarter of its columns each (tiles_all()).
+// Epilogue warp state of k_tcf_fwd: group grp (four warps, one per lane
+// quarter) takes either its share of a stage's tiles (stage_group) or its
+// share of every tile's columns (stage_all).
 struct Epi {
     Ctl *c;
     int lane, grp, q, et;
     uint32_t tq;  // tensor-memory address of this warp's lane quarter, column 0
-    uint32_t T = 0, stg_uses = 0;
-    __device__ bool mine() const { return static_cast<int>(T & 3u) == grp; }
-    __device__ uint32_t taddr() const { return tq + (T & (kSlots - 1)) * 64; }
-    __device__ void wait_tile() {
-        if (!err_set(*c) && !mbar_wait(&c->full[T & (kSlots - 1)], (T / kSlots) & 1u)) raise_err(*c);
-        fence_after();
-    }
-    __device__ void release_tile(uint32_t shares) {
-        fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive_n(&c->empty[T & (kSlots - 1)], shares);
-    }
-    __device__ void publish(int buf) {  // this warp's part of an operand is written
-        fence_async_smem();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&c->ready[buf]);
-    }
+    uint32_t stg_uses = 0;
     __device__ void wait_staging() {
         if (!err_set(*c) && !mbar_wait(&c->stg, stg_uses & 1u)) raise_err(*c);
         ++stg_uses;
     }
-    // Runs f(j, accumulator address) on this group's tiles of a stage of n tiles.
-    template <class F>
-    __device__ void tiles(int n, F f) {
-        for (int j = 0; j < n; ++j, ++T)
-            if (mine()) {
-                wait_tile();
-                f(j, taddr());
-                release_tile(4);
-            }
-    }
-    // Whole-stage form: phase parity of full[j] in bit j, flipped for every
-    // tile of a stage when the stage is done (whether or not this warp waited).
+    // Phase parity of full[j] in bit j, flipped for every tile of a stage
+    // when the stage is done (whether or not this warp waited on it).
     uint32_t fbits = 0;
     __device__ void wait_full(int j) {
         if (!err_set(*c) && !mbar_wait(&c->full[j], (fbits >> j) & 1u)) raise_err(*c);
@@ -313,16 +250,6 @@ struct Epi {
         fence_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive(&c->ready[buf]);
-    }
-    // Runs f(j, accumulator address) on every tile of a stage of n tiles
-    // (f takes this group's quarter of the columns).
-    template <class F>
-    __device__ void tiles_all(int n, F f) {
-        for (int j = 0; j < n; ++j, ++T) {
-            wait_tile();
-            f(j, taddr());
-            release_tile(1);
-        }
     }
 };
 
@@ -386,49 +313,130 @@ __device__ __forceinline__ float2 stg_value(const uint32_t *stg, int k) {
     return make_float2(re, im);
 }
 
+// Two teams per CTA, each of one MMA-issuer warp and 8 epilogue warps (two
+// per tensor-memory lane quarter), work on alternate items: team t owns
+// operand buffer t, tensor-memory columns [256 t, 256 t + 256) and its own
+// barriers, so one team's CUDA-core steps run while the other's MMAs do.
+// Within a team a stage's four or eight tiles accumulate side by side in its
+// 256 columns, one commit per stage, and the epilogue rewrites the operand
+// buffer in place once the stage's MMAs have all completed.
+constexpr int kTeamEpiWarps = 8, kTeamEpiThreads = 32 * kTeamEpiWarps;
+constexpr int kInvThreads = 2 * (32 + kTeamEpiThreads);
+constexpr uint32_t kStgTeam = kStgPacked / 2;  // packed staging per team (bytes)
+static_assert(kStgPacked == 2 * 8192, "packed staging: one 8 KB snapshot per team");
+
+struct CtlInv {
+    uint64_t ready[2], mma[2], stg[2], done[2];
+    uint32_t tmem_base;
+    int err;
+};
+
 template <int IN, int OUT>
-__global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
+__global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
     constexpr bool kBins = IN == IN_BINS;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    auto X = [sm](int buf) { return sm + (buf ? kOpBytes : 0u); };
-    uint32_t *stg = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
+    uint32_t *stg_all = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
     float2 *tab = reinterpret_cast<float2 *>(sm + kInvOffStg + (kBins ? kStgBins : kStgPacked));
-    __shared__ __align__(8) Ctl ctl;
-    __shared__ double red[2 * kEpiWarps];
+    __shared__ __align__(8) CtlInv ctl;
+    __shared__ double red[2][2 * kTeamEpiWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int t = warp >= 9 ? 1 : 0;          // team
+    const int tw = warp - 9 * t;              // warp within the team: 0 issuer, 1-8 epilogue
+    uint8_t *const X = sm + t * kOpBytes;     // this team's operand
 
-    if (tid == 0) ctl_init(ctl);
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&ctl.ready[i], kTeamEpiWarps);
+            mbar_init(&ctl.mma[i], 1);
+            mbar_init(&ctl.stg[i], 1);
+            mbar_init(&ctl.done[i], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        ctl.err = 0;
+    }
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.g);
         uint4 *dst = reinterpret_cast<uint4 *>(sm + kInvOffG);
-        for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kThreads) dst[i] = __ldg(src + i);
-        for (int i = tid; i < kInvTabLen; i += kThreads) tab[i] = __ldg(a.tab + i);
+        for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kInvThreads) dst[i] = __ldg(src + i);
+        for (int i = tid; i < kInvTabLen; i += kInvThreads) tab[i] = __ldg(a.tab + i);
     }
-    tmem_alloc_all(ctl, warp);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ctl.tmem_base)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tb = ctl.tmem_base;
+    const uint32_t tb = ctl.tmem_base + 256u * t;
+    auto err_on = [&]() { return *reinterpret_cast<const volatile int *>(&ctl.err) != 0; };
+    auto raise = [&]() { *reinterpret_cast<volatile int *>(&ctl.err) = 1; };
+    auto item_of = [&](int64_t m) { return static_cast<int64_t>(blockIdx.x) + m * gridDim.x; };
 
-    if (warp == 0) {
-        Issuer is{&ctl, tb};
+    if (tw == 0) {
+        // ---- MMA issuer of team t (whole warp; an elected lane issues) ----
         const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
-        int p = 0;
-        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-            is.stage<4>(p, smem_u32(X(p)), 4, 16384, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
-            is.stage<4>(p ^ 1, smem_u32(X(p ^ 1)), 4, 16384, 32, 16, 1024, kSwizzle128, g32, 1024, 8192, 64);
-            is.stage<2>(p, smem_u32(X(p)), 8, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32);
+        uint32_t rph = 0;
+        auto stage = [&](auto ksteps_c, int tiles, uint32_t tile_bytes, uint32_t lbo, uint32_t sbo, uint32_t layout,
+                         uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n, uint32_t col_w) {
+            constexpr int KSTEPS = decltype(ksteps_c)::value;
+            uint32_t xa = smem_u32(X);
+            asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
+            uint64_t gh[KSTEPS], gl[KSTEPS];
+#pragma unroll
+            for (int ks = 0; ks < KSTEPS; ++ks) {
+                gh[ks] = desc(g + ks * 256, 128, g_sbo, kNoSwizzle);
+                gl[ks] = desc(g + g_lo + ks * 256, 128, g_sbo, kNoSwizzle);
+            }
+            const uint64_t x0 = desc(xa, lbo, sbo, layout);
+            const uint32_t id = idesc_f16(128, n);
+            if (!err_on() && !mbar_wait(&ctl.ready[t], rph)) raise();
+            rph ^= 1u;
+            __syncwarp();
+            fence_after();
+            if (!err_on()) {
+                for (int j = 0; j < tiles; ++j) {
+                    const uint64_t xj = x0 + ((j * tile_bytes) >> 4);
+#pragma unroll
+                    for (int ks = 0; ks < KSTEPS; ++ks) {
+                        const uint64_t xd = xj + ((ks * 32) >> 4);
+                        mma_f16_elect(tb + j * col_w, xd, gh[ks], id, ks > 0);
+                        mma_f16_elect(tb + j * col_w, xd, gl[ks], id, true);
+                    }
+                }
+            }
+            commit_elect(&ctl.mma[t]);
+        };
+        for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
+            stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64);
+            stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64);
+            stage(std::integral_constant<int, 2>{}, 8, 8192, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);
         }
-        is.finish();
+        commit_elect(&ctl.done[t]);  // every MMA of the team retired before tensor memory is freed
+        if (!mbar_wait(&ctl.done[t], 0)) raise();
+        __syncwarp();
     } else {
-        Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
-               tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
-        const int e = warp - 1, q = ep.q, et = ep.et;
-
-        // ---- input staging ---------------------------------------------------
-        uint4 pre = make_uint4(0, 0, 0, 0);  // packed input: next snapshot, 16 bytes per thread
+        // ---- epilogue warps of team t ----------------------------------------
+        const int e = tw - 1;                       // 0..7
+        const int q = warp & 3, h = e >> 2;         // lane quarter, which of its two warps
+        const int et = e * 32 + lane;               // 0..255
+        const uint32_t tq = tb + (static_cast<uint32_t>(q * 32) << 16);
+        uint32_t mph = 0, sph = 0;
+        uint32_t *stg = kBins ? stg_all : stg_all + t * (kStgTeam / 4);
+        auto team_sync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + t), "r"(kTeamEpiThreads) : "memory"); };
+        auto wait_mma = [&]() {
+            if (!err_on() && !mbar_wait(&ctl.mma[t], mph)) raise();
+            mph ^= 1u;
+            fence_after();
+        };
+        auto publish = [&]() {  // this warp's part of the operand written, its tensor-memory reads done
+            fence_before();
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.ready[t]);
+        };
         auto item_in = [&](int64_t item) -> const void * {
             const SegInv &s = a.s[seg_index(a, item)];
             const int64_t local = item - s.item0;
@@ -439,27 +447,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
             else
                 return static_cast<const uint32_t *>(s.in) + pol * s.in_pol_stride + (s.first + loc) * kGroups;
         };
-        auto fetch = [&](int64_t item) {  // start bringing the item's input in
-            if (item >= a.n_items) return;
-            if constexpr (kBins) {
-                if (et == 0) {
-                    fence_async_smem();
-                    bulk_g2s(stg, item_in(item), kStgBins, &ctl.stg);
-                }
-            } else {
-                pre = __ldg(reinterpret_cast<const uint4 *>(item_in(item)) + et);
-            }
+        // bins input: one staging buffer, filled in item order (the team that
+        // has read item m's bins starts the copy of item m + 1's)
+        auto fetch_bins = [&](int64_t m) {
+            if (item_of(m) >= a.n_items) return;
+            fence_async_smem();
+            bulk_g2s(stg_all, item_in(item_of(m)), kStgBins, &ctl.stg[m & 1]);
         };
-        auto land = [&]() {  // the fetched input is in shared memory (all epilogue threads)
-            if constexpr (kBins) {
-                ep.wait_staging();
-            } else {
-                const uint32_t w = 4u * static_cast<uint32_t>(et);
+        // packed input: each thread holds 32 bytes of the team's next snapshot
+        uint4 pre0 = make_uint4(0, 0, 0, 0), pre1 = pre0;
+        auto prefetch = [&](int64_t m) {
+            if (item_of(m) >= a.n_items) return;
+            const uint4 *src = reinterpret_cast<const uint4 *>(item_in(item_of(m)));
+            pre0 = __ldg(src + 2 * et);
+            pre1 = __ldg(src + 2 * et + 1);
+        };
+        auto land = [&]() {  // staged word w at stg_pos(w)
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const uint4 p = i ? pre1 : pre0;
+                const uint32_t w = 8u * static_cast<uint32_t>(et) + 4u * i;
                 const uint32_t u0 = (w >> 6) & 1u, u1 = (w >> 7) & 1u;
-                uint4 v = pre;
-                if (u0) v = make_uint4(pre.y, pre.x, pre.w, pre.z);
+                const uint4 v = u0 ? make_uint4(p.y, p.x, p.w, p.z) : p;
                 *reinterpret_cast<uint4 *>(stg + (w ^ (u1 << 4))) = v;
-                named_sync_epi();
             }
         };
         auto nib = [](uint32_t w) {  // low nibble of w -> (real code - 2, imag code - 2)
@@ -469,140 +479,137 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
         };
 
         // ---- input step: C2R pairing into the stage-1 operand -------------------
-        // Packed input (stage A): row n' = 16 n2 + n3 at 32 n3 + n2; thread:
-        // n3 = its warp, (n2 % 8, n1 % 4) = its lane, so that its 16 pairs k =
+        // Packed input (stage A): row n' = 16 n2 + n3 at 32 n3 + n2; a warp takes
+        // n3 = e and 15 - e, (n2 % 8, n1 % 4) = its lane, so that its 16 pairs k =
         // 512 (4 A + u) + 16 (8 B + a) + n3 (A, B < 4) have staging positions,
-        // shifts and store offsets that are per-lane constants plus
-        // compile-time ones.  Bins input (stage C): rows in natural order n';
-        // thread: n' = et, four consecutive n1 per 16-byte store.
-        auto input = [&](int buf) {
-            uint8_t *op = X(buf);
-            if constexpr (!kBins) {
-                const int n3 = e, av = lane & 7, u = lane >> 3;
-                if (n3 != 0) {
-                    const int u0 = u & 1, u1 = u >> 1;
-                    const int wl = 64 * u + 2 * av + ((n3 >> 3) ^ u0);
-                    const int L0 = wl + 16 * u1, L1 = wl + 16 * (1 - u1);
-                    const int sh = (n3 & 7) * 4, shm = ((8 - (n3 & 7)) & 7) * 4;
-                    uint8_t *S = op + 4096 * n3 + 128 * av + 4 * u;
-                    uint8_t *Sm = op + 4096 * (16 - n3) + 128 * (31 - av) + 12 - 4 * u;
-                    float2 tA[4], tB[4];
-                    int xA[4];
+        // shifts and store offsets that are per-lane constants plus compile-time
+        // ones.  Bins input (stage C): rows in natural order n'; a thread takes
+        // n' = et and et + 256, four consecutive n1 per 16-byte store.
+        auto input_n3 = [&](int n3) {
+            const int av = lane & 7, u = lane >> 3;
+            if (n3 != 0) {
+                const int u0 = u & 1, u1 = u >> 1;
+                const int wl = 64 * u + 2 * av + ((n3 >> 3) ^ u0);
+                const int L0 = wl + 16 * u1, L1 = wl + 16 * (1 - u1);
+                const int sh = (n3 & 7) * 4, shm = ((8 - (n3 & 7)) & 7) * 4;
+                uint8_t *S = X + 4096 * n3 + 128 * av + 4 * u;
+                uint8_t *Sm = X + 4096 * (16 - n3) + 128 * (31 - av) + 12 - 4 * u;
+                float2 tA[4], tB[4];
+                int xA[4];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        tA[i] = tab[kTabA1 + 4 * i + u];
-                        tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
-                        xA[i] = 16 * (i ^ av);
-                    }
+                for (int i = 0; i < 4; ++i) {
+                    tA[i] = tab[kTabA1 + 4 * i + u];
+                    tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
+                    xA[i] = 16 * (i ^ av);
+                }
 #pragma unroll
-                    for (int it = 0; it < 16; ++it) {
-                        const int A = it >> 2, B = it & 3;
-                        const int pos = 256 * A + 32 * (B >> 1) + ((B & 1) ? L1 : L0);
-                        const float2 y = nib(stg[pos] >> sh);
-                        float2 ym;
-                        if (n3 != 8) {
-                            ym = nib(stg[pos ^ 2030] >> shm);
-                        } else {  // k % 8 = 0: the mirror's word is 2048 - w
-                            const int k = 512 * (4 * A + u) + 16 * (8 * B + av) + 8;
-                            ym = stg_value(stg, kMA - k);
-                        }
-                        float2 zk, zm;
-                        c2r_pair(y, ym, cmul(tA[A], tB[B]), zk, zm);
-                        *reinterpret_cast<uint32_t *>(S + 1024 * B + xA[A]) = pack_half2(zk.x, zk.y);
-                        *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA[A]) = pack_half2(zm.x, zm.y);
+                for (int it = 0; it < 16; ++it) {
+                    const int A = it >> 2, B = it & 3;
+                    const int pos = 256 * A + 32 * (B >> 1) + ((B & 1) ? L1 : L0);
+                    const float2 y = nib(stg[pos] >> sh);
+                    float2 ym;
+                    if (n3 != 8) {
+                        ym = nib(stg[pos ^ 2030] >> shm);
+                    } else {  // k % 8 = 0: the mirror's word is 2048 - w
+                        const int k = 512 * (4 * A + u) + 16 * (8 * B + av) + 8;
+                        ym = stg_value(stg, kMA - k);
                     }
-                } else {
-#pragma unroll 1
-                    for (int it = 0; it < 16; ++it) {
-                        const int n1 = 4 * (it >> 2) + u, n2 = 8 * (it & 3) + av;
-                        const int np = 16 * n2, k = 512 * n1 + np;
-                        float2 y = stg_value(stg, k);
-                        float2 ym = make_float2(0.f, 0.f);
-                        const int km = kMA - k;
-                        if (k == 0)
-                            y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
-                        else
-                            ym = stg_value(stg, km);
-                        float2 zk, zm;
-                        c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
-                        *reinterpret_cast<uint32_t *>(op + sw128_off(n2, n1)) = pack_half2(zk.x, zk.y);
-                        if (k != 0) {
-                            const int n1m = km >> 9, npm = km & 511;
-                            *reinterpret_cast<uint32_t *>(op + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
-                                pack_half2(zm.x, zm.y);
-                        }
-                    }
-                    if (lane == 0) {  // k = 8192, its own mirror
-                        const float2 y = stg_value(stg, kMA / 2);
-                        float2 zk, zm;
-                        c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
-                        *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
-                    }
+                    float2 zk, zm;
+                    c2r_pair(y, ym, cmul(tA[A], tB[B]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(S + 1024 * B + xA[A]) = pack_half2(zk.x, zk.y);
+                    *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA[A]) = pack_half2(zm.x, zm.y);
                 }
             } else {
-                const int np = et;
-                const float2 wb = tab[kTabA2 + np];
 #pragma unroll 1
-                for (int c = 0; c < 4; ++c) {
-                    uint32_t zk[4], zm[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int n1 = 4 * c + i, k = 512 * n1 + np;
-                        float2 y = h2f(stg[k]), ym = h2f(stg[kMA - k]);
-                        if (k == 0) {  // Im of bins 0 and 16384 are ignored (C2R)
-                            y.y = 0.f;
-                            ym.y = 0.f;
-                        }
-                        float2 a0, a1;
-                        c2r_pair(y, ym, cmul(tab[kTabA1 + n1], wb), a0, a1);
-                        zk[i] = pack_half2(a0.x, a0.y);
-                        zm[i] = pack_half2(a1.x, a1.y);
-                    }
-                    *reinterpret_cast<uint4 *>(op + sw128_off(np, 4 * c)) = make_uint4(zk[0], zk[1], zk[2], zk[3]);
-                    if (np != 0) {  // mirrors 16384 - k: row 512 - n', K 31 - n1 (a 4-aligned group, reversed)
-                        *reinterpret_cast<uint4 *>(op + sw128_off(512 - np, 28 - 4 * c)) =
-                            make_uint4(zm[3], zm[2], zm[1], zm[0]);
-                    } else {  // row 0: 16384 - 512 n1 lies at K 32 - n1; n1 = 0 mirrors the Nyquist bin
-#pragma unroll
-                        for (int i = 0; i < 4; ++i)
-                            if (4 * c + i > 0)
-                                *reinterpret_cast<uint32_t *>(op + sw128_off(0, 32 - 4 * c - i)) = zm[i];
+                for (int it = 0; it < 16; ++it) {
+                    const int n1 = 4 * (it >> 2) + u, n2 = 8 * (it & 3) + av;
+                    const int np = 16 * n2, k = 512 * n1 + np;
+                    float2 y = stg_value(stg, k);
+                    float2 ym = make_float2(0.f, 0.f);
+                    const int km = kMA - k;
+                    if (k == 0)
+                        y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
+                    else
+                        ym = stg_value(stg, km);
+                    float2 zk, zm;
+                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(X + sw128_off(n2, n1)) = pack_half2(zk.x, zk.y);
+                    if (k != 0) {
+                        const int n1m = km >> 9, npm = km & 511;
+                        *reinterpret_cast<uint32_t *>(X + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
+                            pack_half2(zm.x, zm.y);
                     }
                 }
-                if (et == 0) {  // k = 8192, its own mirror
-                    const float2 y = h2f(stg[kMA / 2]);
+                if (lane == 0) {  // k = 8192, its own mirror
+                    const float2 y = stg_value(stg, kMA / 2);
                     float2 zk, zm;
                     c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
-                    *reinterpret_cast<uint32_t *>(op + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
+                    *reinterpret_cast<uint32_t *>(X + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
                 }
+            }
+        };
+        auto input_row = [&](int np) {
+            const float2 wb = tab[kTabA2 + np];
+#pragma unroll 1
+            for (int c = 0; c < 4; ++c) {
+                uint32_t zk[4], zm[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int n1 = 4 * c + i, k = 512 * n1 + np;
+                    float2 y = h2f(stg[k]), ym = h2f(stg[kMA - k]);
+                    if (k == 0) {  // Im of bins 0 and 16384 are ignored (C2R)
+                        y.y = 0.f;
+                        ym.y = 0.f;
+                    }
+                    float2 a0, a1;
+                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], wb), a0, a1);
+                    zk[i] = pack_half2(a0.x, a0.y);
+                    zm[i] = pack_half2(a1.x, a1.y);
+                }
+                *reinterpret_cast<uint4 *>(X + sw128_off(np, 4 * c)) = make_uint4(zk[0], zk[1], zk[2], zk[3]);
+                if (np != 0) {  // mirrors 16384 - k: row 512 - n', K 31 - n1 (a 4-aligned group, reversed)
+                    *reinterpret_cast<uint4 *>(X + sw128_off(512 - np, 28 - 4 * c)) =
+                        make_uint4(zm[3], zm[2], zm[1], zm[0]);
+                } else {  // row 0: 16384 - 512 n1 lies at K 32 - n1; n1 = 0 mirrors the Nyquist bin
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (4 * c + i > 0) *reinterpret_cast<uint32_t *>(X + sw128_off(0, 32 - 4 * c - i)) = zm[i];
+                }
+            }
+            if (np == 0) {  // k = 8192, its own mirror
+                const float2 y = h2f(stg[kMA / 2]);
+                float2 zk, zm;
+                c2r_pair(y, y, cmul(tab[kTabA1 + 16], tab[kTabA2]), zk, zm);
+                *reinterpret_cast<uint32_t *>(X + sw128_off(0, 16)) = pack_half2(zk.x, zk.y);
             }
         };
 
-        // This group's 8 of a row's 32 DFT outputs (columns 16 grp .. +16),
-        // times w0 b^(8 grp + i): two interleaved twiddle chains (steps b^2)
-        // keep the multiplies independent.
-        auto twiddled8 = [&](uint32_t t, float2 b, float2 w0, uint8_t *d0) {
-            uint32_t r0[8], r1[8];
-            tmem_ld8(t + 16 * ep.grp, r0);
-            tmem_ld8(t + 16 * ep.grp + 8, r1);
-            const float2 b2 = cmul(b, b), b4 = cmul(b2, b2), b8 = cmul(b4, b4);
-            float2 w = w0;
-            for (int g = 0; g < ep.grp; ++g) w = cmul(w, b8);
-            float2 wa = w, wb = cmul(w, b);
-            tmem_wait<8>(r0, r1);
+        // The 32 DFT outputs of this thread's row (tile at tensor-memory address
+        // t), times w0 b^k: two interleaved twiddle chains (steps b^2); output k
+        // goes to d0 + 2048 k.
+        auto twiddled32 = [&](uint32_t taddr, float2 b, float2 w0, uint8_t *d0) {
+            const float2 b2 = cmul(b, b);
+            float2 wa = w0, wb = cmul(w0, b);
 #pragma unroll
-            for (int i = 0; i < 8; i += 2) {
-                const float2 y0 = cmul(acc2(i < 4 ? r0 : r1, i & 3), wa);
-                const float2 y1 = cmul(acc2(i < 4 ? r0 : r1, (i & 3) + 1), wb);
-                wa = cmul(wa, b2);
-                wb = cmul(wb, b2);
-                *reinterpret_cast<uint32_t *>(d0 + 2048 * (8 * ep.grp + i)) = pack_half2(y0.x, y0.y);
-                *reinterpret_cast<uint32_t *>(d0 + 2048 * (8 * ep.grp + i + 1)) = pack_half2(y1.x, y1.y);
+            for (int hf = 0; hf < 2; ++hf) {
+                uint32_t r0[16], r1[16];
+                tmem_ld16(taddr + 32 * hf, r0);
+                tmem_ld16(taddr + 32 * hf + 16, r1);
+                tmem_wait<16>(r0, r1);
+#pragma unroll
+                for (int i = 0; i < 16; i += 2) {
+                    const float2 y0 = cmul(acc2(i < 8 ? r0 : r1, i & 7), wa);
+                    const float2 y1 = cmul(acc2(i < 8 ? r0 : r1, (i & 7) + 1), wb);
+                    wa = cmul(wa, b2);
+                    wb = cmul(wb, b2);
+                    *reinterpret_cast<uint32_t *>(d0 + 2048 * (16 * hf + i)) = pack_half2(y0.x, y0.y);
+                    *reinterpret_cast<uint32_t *>(d0 + 2048 * (16 * hf + i + 1)) = pack_half2(y1.x, y1.y);
+                }
             }
         };
-        // ---- stage 1 -> stage-2 operand: row 16 k1 + n3, K n2, at
+        // ---- stage 1 -> stage-2 operand (in place): row 16 k1 + n3, K n2, at
         // 2048 k1 + (offset of row n3, K n2) in the 128-byte swizzle
-        auto epi1 = [&](int j, uint32_t t, uint8_t *dst) {
+        auto epi1 = [&](int j) {
             int n2, n3;
             if constexpr (!kBins) {  // row n' = 16 lane + n3, n3 = 4 j + q
                 n3 = 4 * j + q;
@@ -613,27 +620,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                 n2 = np >> 4;
             }
             const int np = 16 * n2 + n3;
-            twiddled8(t, tab[kTabB + np + (np >> 4)], make_float2(kBins ? kScaleC1 : 1.f, 0.f),
-                      dst + sw128_off(n3, n2));
+            twiddled32(tq + 64 * j, tab[kTabB + np + (np >> 4)], make_float2(kBins ? kScaleC1 : 1.f, 0.f),
+                       X + sw128_off(n3, n2));
         };
-        // ---- stage 2 -> stage-3 operand: row 32 k2 + k1, K n3, at
+        // ---- stage 2 -> stage-3 operand (in place): row 32 k2 + k1, K n3, at
         // 2048 k2 + (offset of row k1, K n3) in the 64-byte swizzle
-        auto epi2 = [&](int j, uint32_t t, uint8_t *dst) {
+        auto epi2 = [&](int j) {
             const int r = 128 * j + 32 * q + lane, k1 = r >> 4, n3 = r & 15;
             // stage A's FP16 time series is a quarter of the unnormalised value
-            twiddled8(t, tab[kTabC + n3], make_float2(kBins ? kScaleC2 : (OUT == OUT_TS_HALF ? kScaleA : 1.f), 0.f),
-                      dst + sw64_off(k1, n3));
+            twiddled32(tq + 64 * j, tab[kTabC + n3],
+                       make_float2(kBins ? kScaleC2 : (OUT == OUT_TS_HALF ? kScaleA : 1.f), 0.f), X + sw64_off(k1, n3));
         };
         // ---- stage 3 -> output.  Row 32 k2 + k1 = 128 j + 32 q + lane, column k3:
         // z[m], m = k1 + 32 k2 + 1024 k3, = samples (2m, 2m + 1); a warp covers 32
         // consecutive m.
         float f1 = 0.f, f2 = 0.f;  // OUT_QUANT_SUMS: this thread's sums over the chunk (scaled values)
         double d1 = 0.0, d2 = 0.0; // OUT_FLOAT_MOMENTS
-        auto epi3 = [&](int j, uint32_t t, const SegInv &s, int64_t pol, int64_t loc) {
+        auto epi3 = [&](int j, const SegInv &s, int64_t pol, int64_t loc) {
             const int r = 128 * j + 32 * q + lane;
             uint32_t r0[16], r1[16];
-            tmem_ld16(t, r0);
-            tmem_ld16(t + 16, r1);
+            tmem_ld16(tq + 32 * j, r0);
+            tmem_ld16(tq + 32 * j + 16, r1);
             tmem_wait<16>(r0, r1);
             float2 v[16];
 #pragma unroll
@@ -691,7 +698,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                 words[(r >> 3) + 128 * (8 + c)] = wh;
             }
         };
-        // Per-chunk statistics of stage C (all epilogue warps, after stage 3).
+        // Per-chunk statistics of stage C (the team's 8 warps, after stage 3).
         auto chunk_stats = [&](const SegInv &s, int64_t pol, int64_t loc) {
             if constexpr (OUT == OUT_FLOAT_MOMENTS || OUT == OUT_QUANT_SUMS) {
                 if (s.o.partials == nullptr) return;
@@ -704,15 +711,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                     s2 = static_cast<double>(warp_sum_f(f2)) * kUnscaleC * kUnscaleC;
                 }
                 if (lane == 0) {
-                    red[e] = s1;
-                    red[kEpiWarps + e] = s2;
+                    red[t][e] = s1;
+                    red[t][kTeamEpiWarps + e] = s2;
                 }
-                named_sync_epi();
+                team_sync();
                 if (et == 0) {
                     double t1 = 0.0, t2 = 0.0;
-                    for (int w = 0; w < kEpiWarps; ++w) {
-                        t1 += red[w];
-                        t2 += red[kEpiWarps + w];
+                    for (int w = 0; w < kTeamEpiWarps; ++w) {
+                        t1 += red[t][w];
+                        t2 += red[t][kTeamEpiWarps + w];
                     }
                     double *pp = s.o.partials + (pol * s.n + loc) * 3;
                     const double nn = static_cast<double>(kNC);
@@ -725,45 +732,58 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_inv(const __grid_constant__
                         pp[2] = t2;
                     }
                 }
-                named_sync_epi();  // red reusable
+                team_sync();  // red reusable
                 d1 = d2 = 0.0;
                 f1 = f2 = 0.f;
             }
         };
 
-        int p = 0;
-        if (blockIdx.x < a.n_items) {
-            fetch(blockIdx.x);
-            land();
-            input(0);
-            ep.publish(0);
-            named_sync_epi();  // the staging buffer is free again
-            fetch(blockIdx.x + gridDim.x);
+        if constexpr (kBins) {
+            if (t == 0 && et == 0) fetch_bins(0);
+        } else {
+            prefetch(t);
         }
-        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x, p ^= 1) {
-            ep.tiles_all(4, [&](int j, uint32_t t) { epi1(j, t, X(p ^ 1)); });
-            ep.publish(p ^ 1);
-            ep.tiles_all(4, [&](int j, uint32_t t) { epi2(j, t, X(p)); });
-            ep.publish(p);
-            // every stage-2 MMA has retired (each group saw its tiles' commits),
-            // so operand p ^ 1 takes the next item's input
-            named_sync_epi();
-            const int64_t next = item + gridDim.x;
-            if (next < a.n_items) {
+        for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
+            const int64_t item = item_of(m);
+            if constexpr (kBins) {
+                if (!err_on() && !mbar_wait(&ctl.stg[t], sph)) raise();
+                sph ^= 1u;
+                input_row(et);
+                input_row(et + 256);
+                team_sync();  // staging read: it takes the next item's bins
+                if (et == 0) fetch_bins(m + 1);
+            } else {
                 land();
-                input(p ^ 1);
-                ep.publish(p ^ 1);
-                named_sync_epi();
-                fetch(next + gridDim.x);
+                team_sync();
+                prefetch(m + 2);
+                input_n3(e);
+                input_n3(15 - e);
             }
+            publish();
+            wait_mma();
+            epi1(h);
+            epi1(h + 2);
+            publish();
+            wait_mma();
+            epi2(h);
+            epi2(h + 2);
+            publish();
             const SegInv &s = a.s[seg_index(a, item)];
             const int64_t local = item - s.item0;
             const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
-            ep.tiles(8, [&](int j, uint32_t t) { epi3(j, t, s, pol, loc); });
+            wait_mma();
+#pragma unroll 1
+            for (int j = h; j < 8; j += 2) epi3(j, s, pol, loc);
             chunk_stats(s, pol, loc);
+            fence_before();  // tensor-memory reads done before the next item's stage-1 MMAs (after its publish)
         }
     }
-    teardown(ctl, a.status, warp);
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && *reinterpret_cast<const volatile int *>(&ctl.err) != 0)
+        *reinterpret_cast<volatile int *>(a.status) = 1;
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(ctl.tmem_base), "r"(kTmemCols));
 }
 
 // ============================================================================
@@ -978,31 +998,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             const float2 z0 = h2f(Z[0]);
             return make_float2(0.5f * (qq == 0 ? z0.x + z0.y : z0.x - z0.y), 0.f);
         };
-        auto pairw = [&](float2 za, float2 zb, float2 w) -> float2 {
-            const float2 sv = make_float2(za.x + zb.x, za.y - zb.y);
-            const float2 tv = cmul(w, make_float2(za.x - zb.x, za.y + zb.y));
-            return make_float2(0.25f * (sv.x + tv.y), 0.25f * (sv.y - tv.x));
+        // y = (za + conj zb) / 4 - i w (za - conj zb) / 4 with w4 = w / 4
+        auto pairw = [&](float2 za, float2 zb, float2 w4) -> float2 {
+            const float s1 = za.x + zb.x, s2 = za.y - zb.y, d1 = za.x - zb.x, d2 = za.y + zb.y;
+            return make_float2(fmaf(w4.x, d2, fmaf(w4.y, d1, 0.25f * s1)), fmaf(-w4.x, d1, fmaf(w4.y, d2, 0.25f * s2)));
         };
         auto pairing = [&](const SegFwd &s, int64_t pol, int64_t loc) {
             uint32_t *yo = s.out + pol * s.out_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen);
             const float2 w1 = tab[kTabQLo + 1];
+            // W_36608^1024, the step of the twiddle recurrence between a thread's bins
+            const float2 wstep = cmul(tab[kTabQHi + 8], make_float2(1.f, 0.f));
+            int qq = s.skip + 2 * et;  // qq + 1 < N (skip <= 1920)
+            float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
+            w = make_float2(0.25f * w.x, 0.25f * w.y);
 #pragma unroll 1
-            for (int jj = 2 * et; jj < kMA; jj += 2 * kEpiThreads) {
-                const int qq = s.skip + jj;  // qq + 1 < N (skip <= 1920)
-                const float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
+            for (int jj = 2 * et; jj < kMA; jj += 2 * kEpiThreads, qq += 2 * kEpiThreads) {
                 const float2 za0 = h2f(Z[qq]), za1 = h2f(Z[qq + 1]);
                 const float2 zb1 = h2f(Z[kMB - 1 - qq]);
                 const float2 y0 = qq == 0 ? pair1(0) : pairw(za0, h2f(Z[kMB - qq]), w);
                 const float2 y1 = pairw(za1, zb1, cmul(w, w1));
                 __stcs(reinterpret_cast<uint2 *>(yo + jj), make_uint2(pack_half2(y0.x, y0.y), pack_half2(y1.x, y1.y)));
+                w = cmul(w, wstep);
             }
             if (et == 0) {  // bin 16384
-                const int qq = s.skip + kMA;
+                const int q1 = s.skip + kMA;
                 float2 y;
-                if (qq == kMB)
-                    y = pair1(qq);
-                else
-                    y = pairw(h2f(Z[qq]), h2f(Z[kMB - qq]), cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]));
+                if (q1 == kMB) {
+                    y = pair1(q1);
+                } else {
+                    const float2 w0 = cmul(tab[kTabQHi + (q1 >> 7)], tab[kTabQLo + (q1 & 127)]);
+                    y = pairw(h2f(Z[q1]), h2f(Z[kMB - q1]), make_float2(0.25f * w0.x, 0.25f * w0.y));
+                }
                 __stcs(yo + kMA, pack_half2(y.x, y.y));
             }
         };
@@ -1124,16 +1150,22 @@ cudaError_t grid_for(int64_t n_items, unsigned *grid) {
     return e;
 }
 
+// Inverse transforms: two items per CTA at a time (one per team).
+cudaError_t grid_for_teams(int64_t n_items, unsigned *grid) {
+    cudaError_t e = grid_for((n_items + 1) / 2, grid);
+    return e;
+}
+
 template <int IN, int OUT>
 cudaError_t launch_inv(const ArgsInv &args, cudaStream_t st) {
     if (args.n_items <= 0) return cudaSuccess;
     unsigned grid = 0;
-    cudaError_t e = grid_for(args.n_items, &grid);
+    cudaError_t e = grid_for_teams(args.n_items, &grid);
     constexpr uint32_t smem = inv_smem(IN == IN_BINS);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_tcf_inv<IN, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k_tcf_inv<IN, OUT><<<grid, kThreads, smem, st>>>(args);
+    k_tcf_inv<IN, OUT><<<grid, kInvThreads, smem, st>>>(args);
     return cudaGetLastError();
 }
 

@@ -99,11 +99,24 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// Bounded wait for the phase with parity `parity`: sleeps in try_wait rather
-// than spinning (so waiting warps take no issue slots from working ones) and
-// gives up after `limit_ns` of global time; false on time-out.
+// One try_wait without a time hint: returns at once when the phase has
+// completed (the common case in a pipelined consumer, about 20 cycles).
+__device__ __forceinline__ uint32_t mbar_poll(uint64_t *mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity & 1u)
+        : "memory");
+    return done;
+}
+
+// Bounded wait for the phase with parity `parity`: a quick poll first, then
+// sleeps in try_wait rather than spinning (so waiting warps take no issue
+// slots from working ones) and gives up after `limit_ns` of global time;
+// false on time-out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint64_t limit_ns = 1000000000ull) {
-    if (mbar_try(mbar, parity, 100000u)) return true;
+    if (mbar_poll(mbar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
         if (mbar_try(mbar, parity, 100000u)) return true;
