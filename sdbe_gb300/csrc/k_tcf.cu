@@ -89,7 +89,11 @@ constexpr uint32_t kInvOffStg = kInvOffG + kG32Bytes + kG16Bytes;
 // hit distinct banks), e^{2 pi i n3/512} (16)
 constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 544, kInvTabLen = kTabC + 16;
 constexpr uint32_t kStgPacked = 2 * 8192, kStgBins = kTcfBinsLen * 4;  // packed: one snapshot per team
-constexpr uint32_t inv_smem(bool bins) { return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + 1024; }
+// packed input: a 256-entry float4 table (e, d) of a code pair, after the tables
+constexpr uint32_t kPairLutBytes = 256 * 16;
+constexpr uint32_t inv_smem(bool bins) {
+    return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + (bins ? 0u : kPairLutBytes) + 1024;
+}
 
 // ---- shared memory of k_tcf_fwd --------------------------------------------
 constexpr uint32_t kFwdX0 = 90112;                  // raw chunk, DFT-8 operand, DFT-13 operand
@@ -135,6 +139,17 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         "l"(src), "r"(bytes), "r"(smem_u32(mbar))
         : "memory");
 }
+
+// Bulk copy shared -> global of `bytes` (multiple of 16) in this thread's
+// bulk group; the source may be rewritten after bulk_wait_read().
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Common kernel state: barriers, tensor memory, error flag.
 constexpr int kFull = 18;           // completion barriers, one per tile of a whole stage
@@ -338,6 +353,9 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
     uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint32_t *stg_all = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
     float2 *tab = reinterpret_cast<float2 *>(sm + kInvOffStg + (kBins ? kStgBins : kStgPacked));
+    // C2R pairing of two 2-bit code nibbles (y at bits 4-7, the mirror ym at
+    // bits 0-3): (e, d) = (y + conj ym, y - conj ym), exact small integers
+    float4 *pair_lut = reinterpret_cast<float4 *>(tab + kInvTabLen);
     __shared__ __align__(8) CtlInv ctl;
     __shared__ double red[2][2 * kTeamEpiWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -360,6 +378,11 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
         uint4 *dst = reinterpret_cast<uint4 *>(sm + kInvOffG);
         for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kInvThreads) dst[i] = __ldg(src + i);
         for (int i = tid; i < kInvTabLen; i += kInvThreads) tab[i] = __ldg(a.tab + i);
+        if (!kBins && tid < 256) {
+            const float yr = static_cast<float>((tid >> 6) & 3) - 2.f, yi = static_cast<float>((tid >> 4) & 3) - 2.f;
+            const float mr = static_cast<float>((tid >> 2) & 3) - 2.f, mi = static_cast<float>(tid & 3) - 2.f;
+            pair_lut[tid] = make_float4(yr + mr, yi - mi, yr - mr, yi + mi);
+        }
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ctl.tmem_base)),
@@ -494,30 +517,28 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 const int sh = (n3 & 7) * 4, shm = ((8 - (n3 & 7)) & 7) * 4;
                 uint8_t *S = X + 4096 * n3 + 128 * av + 4 * u;
                 uint8_t *Sm = X + 4096 * (16 - n3) + 128 * (31 - av) + 12 - 4 * u;
-                float2 tA[4], tB[4];
-                int xA[4];
+                float2 tB[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    tA[i] = tab[kTabA1 + 4 * i + u];
-                    tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
-                    xA[i] = 16 * (i ^ av);
-                }
+                for (int i = 0; i < 4; ++i) tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
 #pragma unroll
                 for (int it = 0; it < 16; ++it) {
                     const int A = it >> 2, B = it & 3;
+                    const float2 tA = tab[kTabA1 + 4 * A + u];
+                    const int xA = 16 * (A ^ av);
                     const int pos = 256 * A + 32 * (B >> 1) + ((B & 1) ? L1 : L0);
-                    const float2 y = nib(stg[pos] >> sh);
-                    float2 ym;
+                    float2 zk, zm;
                     if (n3 != 8) {
-                        ym = nib(stg[pos ^ 2030] >> shm);
+                        const uint32_t idx = ((stg[pos] >> sh) & 15u) << 4 | ((stg[pos ^ 2030] >> shm) & 15u);
+                        const float4 ed = pair_lut[idx];
+                        const float2 tt = cmul(make_float2(ed.z, ed.w), cmul(tA, tB[B]));
+                        zk = make_float2(ed.x - tt.y, ed.y + tt.x);
+                        zm = make_float2(ed.x + tt.y, tt.x - ed.y);
                     } else {  // k % 8 = 0: the mirror's word is 2048 - w
                         const int k = 512 * (4 * A + u) + 16 * (8 * B + av) + 8;
-                        ym = stg_value(stg, kMA - k);
+                        c2r_pair(nib(stg[pos] >> sh), stg_value(stg, kMA - k), cmul(tA, tB[B]), zk, zm);
                     }
-                    float2 zk, zm;
-                    c2r_pair(y, ym, cmul(tA[A], tB[B]), zk, zm);
-                    *reinterpret_cast<uint32_t *>(S + 1024 * B + xA[A]) = pack_half2(zk.x, zk.y);
-                    *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA[A]) = pack_half2(zm.x, zm.y);
+                    *reinterpret_cast<uint32_t *>(S + 1024 * B + xA) = pack_half2(zk.x, zk.y);
+                    *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA) = pack_half2(zm.x, zm.y);
                 }
             } else {
 #pragma unroll 1
@@ -645,17 +666,15 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             float2 v[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) v[i] = acc2(i < 8 ? r0 : r1, i & 7);
-            if constexpr (OUT == OUT_TS_HALF || OUT == OUT_TS_FLOAT) {
+            if constexpr (OUT == OUT_TS_HALF) {  // into the operand buffer, then one bulk store
+#pragma unroll
+                for (int i = 0; i < 16; ++i)
+                    reinterpret_cast<uint32_t *>(X)[r + 1024 * i] = pack_half2(v[i].x, v[i].y);
+            } else if constexpr (OUT == OUT_TS_FLOAT) {
                 const int64_t off = pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int m = r + 1024 * i;
-                    if constexpr (OUT == OUT_TS_HALF)
-                        __stcs(reinterpret_cast<unsigned int *>(static_cast<__half *>(s.out) + off) + m,
-                               pack_half2(v[i].x, v[i].y));
-                    else
-                        __stcs(reinterpret_cast<float2 *>(static_cast<float *>(s.out) + off) + m, v[i]);
-                }
+                for (int i = 0; i < 16; ++i)
+                    __stcs(reinterpret_cast<float2 *>(static_cast<float *>(s.out) + off) + r + 1024 * i, v[i]);
             } else if constexpr (OUT == OUT_FLOAT || OUT == OUT_FLOAT_MOMENTS) {
                 float2 *fo = reinterpret_cast<float2 *>(s.o.fout + pol * s.o.fout_pol_stride + loc * kNC);
 #pragma unroll
@@ -742,6 +761,9 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             if (t == 0 && et == 0) fetch_bins(0);
         } else {
             prefetch(t);
+            // team 1 starts once team 0 has written its first operand, so that
+            // the teams' MMA waits fall in each other's CUDA-core steps
+            if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0)) raise();
         }
         for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
             const int64_t item = item_of(m);
@@ -753,9 +775,9 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 team_sync();  // staging read: it takes the next item's bins
                 if (et == 0) fetch_bins(m + 1);
             } else {
+                if (OUT == OUT_TS_HALF && et == 0) bulk_wait_read();  // the last item's series has left X
                 land();
                 team_sync();
-                prefetch(m + 2);
                 input_n3(e);
                 input_n3(15 - e);
             }
@@ -772,11 +794,20 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             const int64_t local = item - s.item0;
             const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
             wait_mma();
+            if constexpr (!kBins) prefetch(m + 2);  // consumed by the next item's land()
 #pragma unroll 1
             for (int j = h; j < 8; j += 2) epi3(j, s, pol, loc);
+            if constexpr (OUT == OUT_TS_HALF) {  // the time series (64 KB, natural order) to global
+                fence_async_smem();
+                team_sync();
+                if (et == 0)
+                    bulk_s2g(static_cast<__half *>(s.out) + pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA), X,
+                             kNA * 2);
+            }
             chunk_stats(s, pol, loc);
             fence_before();  // tensor-memory reads done before the next item's stage-1 MMAs (after its publish)
         }
+        if (OUT == OUT_TS_HALF && et == 0) bulk_wait_all();
     }
     fence_before();
     __syncthreads();
@@ -796,7 +827,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
 // nA' = 13 n11 + n13 (a relabelling of nA).
 //   B1  DFT-16 over n16: rows 8 nA' + n8        (1144 in 9 tiles), K n16 (64-byte swizzle)
 //       twiddle W_128^(n8 k16)
-//   B2  DFT-8 over n8:   rows nA' + 143 k16     (2288 in 18 tiles), K n8 (32-byte swizzle)
+//   B2  DFT-8 over n8:   rows 144 k16 + nA'     (2304 in 18 tiles, nA' = 143 unused), K n8 (32-byte swizzle)
 //   B3  DFT-11 over n11: rows n13 + 13 kB       (1664 in 13 tiles), K n11 (3 core matrices)
 //   B4  DFT-13 over n13: rows 128 k11 + kB      (1408 in 11 tiles), K n13 (64-byte swizzle)
 //   Z[k] in natural order -> R2C pairing -> bins [skip, skip + 16384] (FP16) to global.
@@ -918,34 +949,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                     make_uint4(v[0], v[1], v[2], v[3]);
             }
         };
-        // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row nA' + 143 k16, K n8.
-        // Group g takes k16 = 4g .. 4g + 3 of every tile; twiddle 2^-8 W_128^(n8 k16)
-        // from the table (8 distinct entries per load, 4 lanes each).
+        // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row 144 k16 + nA', K n8:
+        // a thread's 16 stores are one address plus 4608 k16.  Twiddle 2^-8
+        // W_128^(n8 k16) from the table (8 distinct entries per load, 4 lanes each).
         auto epi1 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
-            uint32_t r0[8];
-            tmem_ld8(t + 8 * ep.grp, r0);
-            tmem_wait1<8>(r0);
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);
+            tmem_ld16(t + 16, r1);
+            tmem_wait<16>(r0, r1);
             if (nAp < 143) {
+                uint8_t *d0 = X0 + sw32_off(nAp, n8);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int k16 = 4 * ep.grp + i;
-                    const float2 y = cmul(acc2(r0, i), tab[kTabW128 + ((n8 * k16) & 127)]);
-                    *reinterpret_cast<uint32_t *>(X0 + sw32_off(nAp + 143 * k16, n8)) = pack_half2(y.x, y.y);
+                for (int k16 = 0; k16 < 16; ++k16) {
+                    const float2 y = cmul(acc2(k16 < 8 ? r0 : r1, k16 & 7), tab[kTabW128 + ((n8 * k16) & 127)]);
+                    *reinterpret_cast<uint32_t *>(d0 + 4608 * k16) = pack_half2(y.x, y.y);
                 }
             }
         };
-        // B2: DFT-8 out (k8), rows nA' + 143 k16 -> B3 operand row n13 + 13 (k16 + 16 k8), K n11:
+        // B2: DFT-8 out (k8), rows 144 k16 + nA' -> B3 operand row n13 + 13 (k16 + 16 k8), K n11:
         // 208 rows (26 row groups of 384 bytes) per k8
         auto epi2 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane;
-            const bool ok = r < 2288;
-            const int k16 = r / 143, nAp = r - 143 * k16, n11 = nAp / 13, n13 = nAp - 13 * n11;
+            const int k16 = r / 144, nAp = r - 144 * k16, n11 = nAp / 13, n13 = nAp - 13 * n11;
             uint32_t r0[16];
             tmem_ld16(t, r0);
             tmem_wait1<16>(r0);
             uint8_t *d0 = X1 + k24_off(n13 + 13 * k16, n11);
-            if (ok) {
+            if (nAp < 143) {
 #pragma unroll
                 for (int k8 = 0; k8 < 8; ++k8) {
                     const float2 v = acc2(r0, k8);
@@ -953,24 +984,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                 }
             }
         };
-        // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13.
-        // Group g takes k11 = g, g + 4, g + 8 (< 11) of every tile.
+        // B3: DFT-11 out (k11), rows n13 + 13 kB -> B4 operand row 128 k11 + kB, K n13
         auto epi3 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, kB = r / 13, n13 = r - 13 * kB;
-            const int g = ep.grp;
-            uint32_t r0[2], r1[2], r2[2];
-            tmem_ld2(t + 2 * g, r0);
-            tmem_ld2(t + 2 * g + 8, r1);
-            tmem_ld2(t + 2 * g + 16, r2);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            asm volatile("" : "+r"(r0[0]), "+r"(r0[1]), "+r"(r1[0]), "+r"(r1[1]));
-            asm volatile("" : "+r"(r2[0]), "+r"(r2[1]));
-            uint8_t *d0 = X0 + sw64_off(kB, n13) + 8192 * g;
-            *reinterpret_cast<uint32_t *>(d0) = pack_half2(__uint_as_float(r0[0]), __uint_as_float(r0[1]));
-            *reinterpret_cast<uint32_t *>(d0 + 8192 * 4) = pack_half2(__uint_as_float(r1[0]), __uint_as_float(r1[1]));
-            if (g < 3)
-                *reinterpret_cast<uint32_t *>(d0 + 8192 * 8) =
-                    pack_half2(__uint_as_float(r2[0]), __uint_as_float(r2[1]));
+            uint32_t r0[16], r1[16];
+            tmem_ld16(t, r0);       // k11 = 0..7
+            tmem_ld16(t + 16, r1);  // k11 = 8..10 (+ zero columns)
+            tmem_wait<16>(r0, r1);
+            uint8_t *d0 = X0 + sw64_off(kB, n13);
+#pragma unroll
+            for (int k11 = 0; k11 < 11; ++k11) {
+                const float2 v = acc2(k11 < 8 ? r0 : r1, k11 & 7);
+                *reinterpret_cast<uint32_t *>(d0 + 8192 * k11) = pack_half2(v.x, v.y);
+            }
         };
         // B4: DFT-13 out (k13), rows 128 k11 + kB -> Z[k], k = (2432 kA + 15873 kB) mod N,
         // kA = (78 k11 + 66 k13) mod 143: k advances by 14080 per k13.
@@ -1011,7 +1037,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             int qq = s.skip + 2 * et;  // qq + 1 < N (skip <= 1920)
             float2 w = cmul(tab[kTabQHi + (qq >> 7)], tab[kTabQLo + (qq & 127)]);
             w = make_float2(0.25f * w.x, 0.25f * w.y);
-#pragma unroll 1
+#pragma unroll 2
             for (int jj = 2 * et; jj < kMA; jj += 2 * kEpiThreads, qq += 2 * kEpiThreads) {
                 const float2 za0 = h2f(Z[qq]), za1 = h2f(Z[qq + 1]);
                 const float2 zb1 = h2f(Z[kMB - 1 - qq]);
@@ -1038,11 +1064,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             ep.wait_staging();
             input();
             ep.publish_all(1);
-            ep.stage_all(9, 32, [&](int j, uint32_t t) { epi1(j, t); });
+            ep.stage_group(9, 32, 0, [&](int j, uint32_t t) { epi1(j, t); });
             ep.publish_all(0);
-            ep.stage_group(18, 16, 0, [&](int j, uint32_t t) { epi2(j, t); });
+            ep.stage_group(18, 16, 1, [&](int j, uint32_t t) { epi2(j, t); });
             ep.publish_all(1);
-            ep.stage_all(13, 32, [&](int j, uint32_t t) { epi3(j, t); });
+            ep.stage_group(13, 32, 3, [&](int j, uint32_t t) { epi3(j, t); });
             ep.publish_all(0);
             ep.stage_group(11, 32, 2, [&](int j, uint32_t t) { epi4(j, t); });
             fence_before();
