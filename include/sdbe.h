@@ -433,6 +433,16 @@ int sdbe_reorder_mar2015(const uint32_t *spec_in, int32_t n_frames, uint32_t *sp
  * FP32 radix kernels, which are bound by FP32 issue. */
 int sdbe_fp32_fma_rate(int32_t device, double *tflops, double *ms);
 
+/* ---- test hook: bounded mbarrier waits (no counterpart in the reference) - */
+/* Arms the next SDBE_PRECISION_TC16_FAST call of h to withhold one MMA
+ * completion signal in its first inverse-transform launch and to bound every
+ * mbarrier wait of that launch by limit_ns nanoseconds.  The wait that
+ * depends on the withheld signal runs out; the kernel records the time-out
+ * in h's status flag, stops waiting, frees its tensor memory and returns, so
+ * the context stays usable.  The call after it returns SDBE_ERR_CUDA.  Used
+ * by the tests of the failure path; limit_ns must be in [1e3, 1e9]. */
+int sdbe_test_tc_timeout(sdbe_resampler *h, int64_t limit_ns);
+
 #ifdef __cplusplus
 }
 #endif

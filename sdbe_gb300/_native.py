@@ -129,6 +129,7 @@ SIGNATURES = {
     "sdbe_vdif_headers": (C.c_int, [vp, i64, i64, u32, u32, u64, u32, u32, u32, u32, vp]),
     "sdbe_reorder_mar2015": (C.c_int, [vp, i32, vp, vp]),
     "sdbe_fp32_fma_rate": (C.c_int, [i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "sdbe_test_tc_timeout": (C.c_int, [vp, i64]),
 }
 
 SYNTH_SIGNATURES = {

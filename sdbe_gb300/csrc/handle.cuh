@@ -90,6 +90,7 @@ struct sdbe_resampler {
     int64_t tcf_half_bytes = 0;
     int *tc_status_host = nullptr;  // 1 after a tensor-core barrier time-out (pinned, mapped)
     int *tc_status = nullptr;       // its device address
+    int64_t tc_test_timeout_ns = 0; // > 0: the next fast tensor-core launch withholds a signal (test hook)
     // Mar-2015 format: unpacked frames land here first; the last one is held
     // for the next call because output frame f needs input frame f+1.
     uint32_t *raw = nullptr;      // [2][max_frames+1][128][2048]

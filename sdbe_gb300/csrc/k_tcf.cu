@@ -155,11 +155,13 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 constexpr int kFull = 18;           // completion barriers, one per tile of a whole stage
 struct Ctl {
     uint64_t full[kFull], ready[2], done, stg;
+    uint64_t lim;  // bound of every mbarrier wait (ns)
     uint32_t tmem_base;
     int err;
 };
 
-__device__ __forceinline__ void ctl_init(Ctl &c) {
+__device__ __forceinline__ void ctl_init(Ctl &c, uint64_t lim) {
+    c.lim = lim;
     for (int i = 0; i < kFull; ++i) mbar_init(&c.full[i], 1);
     mbar_init(&c.ready[0], kEpiWarps);
     mbar_init(&c.ready[1], kEpiWarps);
@@ -196,7 +198,7 @@ struct Issuer {
         }
         const uint64_t x0 = desc(xa, lbo, sbo, layout);
         const uint32_t id = idesc_f16(128, n);
-        if (!err_set(*c) && !mbar_wait(&c->ready[buf], (rphase >> buf) & 1u)) raise_err(*c);
+        if (!err_set(*c) && !mbar_wait(&c->ready[buf], (rphase >> buf) & 1u, c->lim)) raise_err(*c);
         rphase ^= 1u << buf;
         __syncwarp();
         fence_after();
@@ -217,7 +219,7 @@ struct Issuer {
     }
     __device__ void finish() {  // every MMA retired before tensor memory is freed
         commit_elect(&c->done);
-        if (!mbar_wait(&c->done, 0)) raise_err(*c);
+        if (!mbar_wait(&c->done, 0)) raise_err(*c);  // real completion of issued MMAs: the default bound
         __syncwarp();
     }
 };
@@ -231,14 +233,14 @@ struct Epi {
     uint32_t tq;  // tensor-memory address of this warp's lane quarter, column 0
     uint32_t stg_uses = 0;
     __device__ void wait_staging() {
-        if (!err_set(*c) && !mbar_wait(&c->stg, stg_uses & 1u)) raise_err(*c);
+        if (!err_set(*c) && !mbar_wait(&c->stg, stg_uses & 1u, c->lim)) raise_err(*c);
         ++stg_uses;
     }
     // Phase parity of full[j] in bit j, flipped for every tile of a stage
     // when the stage is done (whether or not this warp waited on it).
     uint32_t fbits = 0;
     __device__ void wait_full(int j) {
-        if (!err_set(*c) && !mbar_wait(&c->full[j], (fbits >> j) & 1u)) raise_err(*c);
+        if (!err_set(*c) && !mbar_wait(&c->full[j], (fbits >> j) & 1u, c->lim)) raise_err(*c);
         fence_after();
     }
     // Runs f(j, accumulator address of tile j) on every tile of a whole stage.
@@ -314,6 +316,8 @@ struct ArgsInv {
     const uint8_t *g;        // inverse DFT-32 then DFT-16 matrices, pre-tiled
     const float2 *tab;       // the kInvTabLen twiddle values
     int *status;             // set to 1 on a barrier time-out (host-mapped)
+    uint64_t wait_ns;        // bound of every mbarrier wait
+    int withhold;            // 1: team 0 withholds its first stage commit (test of the time-out path)
 };
 
 // Staged packed spectrum: word w at w ^ ((w >> 6) & 1) ^ (((w >> 7) & 1) << 4),
@@ -397,11 +401,13 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
     auto err_on = [&]() { return *reinterpret_cast<const volatile int *>(&ctl.err) != 0; };
     auto raise = [&]() { *reinterpret_cast<volatile int *>(&ctl.err) = 1; };
     auto item_of = [&](int64_t m) { return static_cast<int64_t>(blockIdx.x) + m * gridDim.x; };
+    const uint64_t lim = a.wait_ns;
 
     if (tw == 0) {
         // ---- MMA issuer of team t (whole warp; an elected lane issues) ----
         const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
         uint32_t rph = 0;
+        bool withhold = a.withhold != 0 && t == 0;
         auto stage = [&](auto ksteps_c, int tiles, uint32_t tile_bytes, uint32_t lbo, uint32_t sbo, uint32_t layout,
                          uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n, uint32_t col_w) {
             constexpr int KSTEPS = decltype(ksteps_c)::value;
@@ -415,7 +421,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             }
             const uint64_t x0 = desc(xa, lbo, sbo, layout);
             const uint32_t id = idesc_f16(128, n);
-            if (!err_on() && !mbar_wait(&ctl.ready[t], rph)) raise();
+            if (!err_on() && !mbar_wait(&ctl.ready[t], rph, lim)) raise();
             rph ^= 1u;
             __syncwarp();
             fence_after();
@@ -430,7 +436,10 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                     }
                 }
             }
-            commit_elect(&ctl.mma[t]);
+            if (withhold)
+                withhold = false;  // test of the time-out path: this stage's completion is never signalled
+            else
+                commit_elect(&ctl.mma[t]);
         };
         for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
             stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64);
@@ -438,7 +447,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             stage(std::integral_constant<int, 2>{}, 8, 8192, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);
         }
         commit_elect(&ctl.done[t]);  // every MMA of the team retired before tensor memory is freed
-        if (!mbar_wait(&ctl.done[t], 0)) raise();
+        if (!mbar_wait(&ctl.done[t], 0)) raise();  // real completion of issued MMAs: the default bound
         __syncwarp();
     } else {
         // ---- epilogue warps of team t ----------------------------------------
@@ -450,7 +459,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
         uint32_t *stg = kBins ? stg_all : stg_all + t * (kStgTeam / 4);
         auto team_sync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + t), "r"(kTeamEpiThreads) : "memory"); };
         auto wait_mma = [&]() {
-            if (!err_on() && !mbar_wait(&ctl.mma[t], mph)) raise();
+            if (!err_on() && !mbar_wait(&ctl.mma[t], mph, lim)) raise();
             mph ^= 1u;
             fence_after();
         };
@@ -763,12 +772,12 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             prefetch(t);
             // team 1 starts once team 0 has written its first operand, so that
             // the teams' MMA waits fall in each other's CUDA-core steps
-            if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0)) raise();
+            if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0, lim)) raise();
         }
         for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
             const int64_t item = item_of(m);
             if constexpr (kBins) {
-                if (!err_on() && !mbar_wait(&ctl.stg[t], sph)) raise();
+                if (!err_on() && !mbar_wait(&ctl.stg[t], sph, lim)) raise();
                 sph ^= 1u;
                 input_row(et);
                 input_row(et + 256);
@@ -846,6 +855,7 @@ struct ArgsFwd {
     const uint8_t *g;        // forward DFT-16, DFT-8, DFT-11, DFT-13 matrices, pre-tiled
     const float2 *tab;       // the kFwdTabLen twiddle values
     int *status;
+    uint64_t wait_ns;        // bound of every mbarrier wait
 };
 
 __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__ ArgsFwd a) {
@@ -856,7 +866,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
     __shared__ __align__(8) Ctl ctl;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    if (tid == 0) ctl_init(ctl);
+    if (tid == 0) ctl_init(ctl, a.wait_ns);
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.g);
         uint4 *dst = reinterpret_cast<uint4 *>(sm + kFwdOffG);
@@ -1208,6 +1218,8 @@ cudaError_t launch_fwd(const ArgsFwd &args, cudaStream_t st) {
 
 const uint8_t *blob_of(const sdbe_resampler *h) { return static_cast<const uint8_t *>(h->tcf_tabs); }
 
+constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s: far above any legitimate wait
+
 }  // namespace
 
 // Tables of the fast tensor-core kernels and the time-out flag, on first use.
@@ -1256,6 +1268,12 @@ int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, 
     A.g = blob_of(h);
     A.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
     A.status = h->tc_status;
+    A.wait_ns = kWaitNs;
+    if (h->tc_test_timeout_ns > 0) {  // test hook: one withheld signal, short waits
+        A.wait_ns = static_cast<uint64_t>(h->tc_test_timeout_ns);
+        A.withhold = 1;
+        h->tc_test_timeout_ns = 0;
+    }
     SDBE_CK(h, (half_out ? launch_inv<IN_PACKED, OUT_TS_HALF>(A, st) : launch_inv<IN_PACKED, OUT_TS_FLOAT>(A, st)));
     return SDBE_OK;
 }
@@ -1287,9 +1305,11 @@ int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols
     B.g = blob_of(h) + kBlobFwdG;
     B.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobFwdTab);
     B.status = h->tc_status;
+    B.wait_ns = kWaitNs;
     C.g = blob_of(h);
     C.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
     C.status = h->tc_status;
+    C.wait_ns = kWaitNs;
     SDBE_CK(h, launch_fwd(B, st));
     switch (mode) {
         case 0: SDBE_CK(h, (launch_inv<IN_BINS, OUT_QUANT>(C, st))); break;
@@ -1391,3 +1411,14 @@ cudaError_t tcf_to_half(const float *in, void *out, int64_t n_floats, cudaStream
 }
 
 }  // namespace sdbe
+
+using namespace sdbe;
+
+extern "C" int sdbe_test_tc_timeout(sdbe_resampler *h, int64_t limit_ns) {
+    if (!h) return SDBE_ERR_ARG;
+    if (limit_ns < 1000 || limit_ns > 1000000000) return fail(h, SDBE_ERR_ARG, "limit_ns must be in [1e3, 1e9]");
+    if (h->cfg.precision != SDBE_PRECISION_TC16_FAST)
+        return fail(h, SDBE_ERR_STATE, "the time-out test hook needs SDBE_PRECISION_TC16_FAST");
+    h->tc_test_timeout_ns = limit_ns;
+    return SDBE_OK;
+}
