@@ -575,6 +575,7 @@ class IngestState:
         self.ref = 0                       # index of the oldest open group
         self.count = {}                    # group -> packets inserted
         self.fcount = {}                   # group -> per-frame packets inserted
+        self.shipped = []                  # (group, packets held) of every shipped group, in order
         self.stats = dict(packets=0, invalid=0, before_start=0, too_far_ahead=0, used=0, overflow=0,
                           groups_shipped=0, groups_incomplete=0)
 
@@ -589,8 +590,8 @@ def ingest_policy(packets, st: IngestState, flush=False):
     batch is sorted invalid-first then by b (``compar_beng``, ``:48-68``); the
     first valid b of the stream fixes the groups at b_first+1+143k (``:317-337``);
     per packet ``get_beng_group_index_offset`` (``vdif_in_databuf.c:96-124``)
-    returns invalid / before start / too far ahead (beyond the 4th group by
-    more than 4*143 frames) or the group offset; an offset above
+    returns invalid / before start / too far ahead (beyond the group after the
+    4th by more than 4*143 frames) or the group offset; an offset above
     MAX_INDEX_LOOK_AHEAD ships the oldest group incomplete and the packet is
     examined again (``:393-401``); otherwise it is inserted
     (``insert_vdif_in_beng_group_buffer``, ``vdif_in_databuf.c:126-156``: at most
@@ -615,6 +616,7 @@ def ingest_policy(packets, st: IngestState, flush=False):
     def ship():
         g = st.ref
         ships.append(g)
+        st.shipped.append((g, st.count.get(g, 0)))
         st.stats["groups_shipped"] += 1
         if st.count.get(g, 0) < GROUP_PACKETS:
             st.stats["groups_incomplete"] += 1
@@ -641,7 +643,9 @@ def ingest_policy(packets, st: IngestState, flush=False):
                 break
             off = (bi - lo) // BENG_FRAMES_PER_GROUP
             if off >= BENG_GROUPS_IN_BUFFER:
-                lu_last = st.start(st.ref + BENG_GROUPS_IN_BUFFER) - 1
+                # the search (:107-116) leaves its upper bound at the last
+                # frame of the group after the four it checked
+                lu_last = st.start(st.ref + BENG_GROUPS_IN_BUFFER + 1) - 1
                 if bi > lu_last + BENG_GROUPS_IN_BUFFER * BENG_FRAMES_PER_GROUP:
                     st.stats["too_far_ahead"] += 1
                     break

@@ -112,7 +112,9 @@ void run_policy(Policy &p, const HdrView &hv, int64_t n, std::vector<uint8_t> &a
             }
             int64_t off = (b - lo) / kGroupFrames;
             if (off >= kRing) {
-                const int64_t lu_last = group_start(p, p.ref + kRing) - 1;
+                // vdif_in_databuf.c:107-120: the search ends with its upper
+                // bound at the last frame of the group after the four it checked
+                const int64_t lu_last = group_start(p, p.ref + kRing + 1) - 1;
                 if (b > lu_last + int64_t(kRing) * kGroupFrames) {
                     p.st.too_far_ahead += 1;
                     break;

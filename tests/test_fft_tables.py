@@ -139,7 +139,8 @@ def test_nibble_transpose_model():
     """nib_transpose8: step m (1, 2, 4) swaps between lanes c and c ^ m the
     nibbles whose index bit m differs from the lane's bit m; the result is
     the transpose of the 8 x 8 nibble matrix."""
-    src = _source()
+    with open(os.path.join(os.path.dirname(SRC), "fft_core.cuh")) as f:
+        src = f.read()
     assert "kKeep[3] = {0x0F0F0F0Fu, 0x00FF00FFu, 0x0000FFFFu}" in src
     keep = [0x0F0F0F0F, 0x00FF00FF, 0x0000FFFF]
     rng = np.random.default_rng(9)

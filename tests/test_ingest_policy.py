@@ -58,7 +58,7 @@ def test_look_ahead_ships_oldest_incomplete_and_retries():
     acc, ships = O.ingest_policy(headers([start(6)]), st)
     assert ships == [1, 2, 3] and acc.tolist() == [True] and st.ref == 4
     # late packet, packet too far ahead, invalid packet
-    far = start(st.ref + 4) - 1 + 4 * G + 1
+    far = start(st.ref + 5) - 1 + 4 * G + 1  # past the group after the four searched, by 4 groups
     acc, ships = O.ingest_policy(headers([start(0) + 3, far, start(3)], invalid=[0, 0, 1]), st)
     assert ships == [] and not acc.any()
     s = st.stats
