@@ -977,6 +977,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                 }
             }
         };
+        // The same for k16 = 4 g .. 4 g + 3 only (group g's quarter of a tile's columns).
+        auto epi1q = [&](int j, uint32_t t) {
+            const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
+            uint32_t r0[8];
+            tmem_ld8(t + 8 * ep.grp, r0);
+            tmem_wait1<8>(r0);
+            if (nAp < 143) {
+                uint8_t *d0 = X0 + sw32_off(nAp, n8) + 4608 * 4 * ep.grp;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int k16 = 4 * ep.grp + i;
+                    const float2 y = cmul(acc2(r0, i), tab[kTabW128 + ((n8 * k16) & 127)]);
+                    *reinterpret_cast<uint32_t *>(d0 + 4608 * i) = pack_half2(y.x, y.y);
+                }
+            }
+        };
         // B2: DFT-8 out (k8), rows 144 k16 + nA' -> B3 operand row n13 + 13 (k16 + 16 k8), K n11:
         // 208 rows (26 row groups of 384 bytes) per k8
         auto epi2 = [&](int j, uint32_t t) {
@@ -1074,7 +1090,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             ep.wait_staging();
             input();
             ep.publish_all(1);
-            ep.stage_group(9, 32, 0, [&](int j, uint32_t t) { epi1(j, t); });
+            // B1: tiles 0-7 two per group, the ninth split by columns
+            for (int j = ep.grp; j < 8; j += 4) {
+                ep.wait_full(j);
+                epi1(j, ep.tq + 32 * j);
+            }
+            ep.wait_full(8);
+            epi1q(8, ep.tq + 32 * 8);
+            ep.fbits ^= (1u << 9) - 1u;
             ep.publish_all(0);
             ep.stage_group(18, 16, 1, [&](int j, uint32_t t) { epi2(j, t); });
             ep.publish_all(1);
