@@ -109,7 +109,7 @@ def _load_peaks():
 _DTYPE = {"fp32": "f32", "tc16": "f16 hi+lo x f16 hi+lo tensor (f32 accumulate)",
           "tc16fast": "f16 x f16 hi+lo tensor (f32 accumulate)"}
 _PATH = {"fp32": "FP32 radix", "tc16": "FP16 tensor-core (data and DFT hi+lo) four-step",
-         "tc16fast": "FP16 tensor-core (DFT hi+lo, data FP16) four-step"}
+         "tc16fast": "FP16 tensor-core (DFT hi+lo, data FP16) mixed-radix DFT-GEMM chain"}
 
 
 def _load_tensor_peak():
@@ -129,19 +129,40 @@ def _tc_flops(n2, splits=3):
     return (8 + np_ // 16) * 4 * splits * 2 * 128 * np_ * 16
 
 
+def _mma_flops(tiles, ksteps, n):
+    """FLOPs of one GEMM stage of the fast form: per tile of 128 rows and K-step
+    of 16, one hi and one lo MMA of 128 x n x 16."""
+    return tiles * ksteps * 2 * (2 * 128 * n * 16)
+
+
+# Tensor FLOPs the fast form (k_tcf.cu) issues per unit, from its tile plans:
+# inverse 16384 = DFT-32 (4 tiles x 4 K-steps, N 64) twice, then DFT-16 (8 x 2,
+# N 32); forward 18304 = DFT-16 (9 x 2, N 32), DFT-8 (18 x 1, N 16), DFT-11
+# (13 x 2, N 32), DFT-13 (11 x 2, N 32).
+TCF_INV_FLOPS = 2 * _mma_flops(4, 4, 64) + _mma_flops(8, 2, 32)                                      # 20,971,520
+TCF_FWD_FLOPS = _mma_flops(9, 2, 32) + _mma_flops(18, 1, 16) + _mma_flops(13, 2, 32) + _mma_flops(11, 2, 32)  # 19,660,800
+
+
 def _tc_roofline(prof, steps, splits):
-    """Tensor roofline of the TC form: MMA FLOPs issued per span / span time.
-    Span A = pairing + TC inverse 16384 per snapshot; span BC = TC forward
-    18304 + pairings + TC inverse 16384 + 2-bit packing per chunk."""
+    """Tensor roofline of a TC form: MMA FLOPs issued per span / span time.
+    Span A = the inverse 16384 per snapshot; span BC = the forward 18304 and
+    the inverse 16384 per chunk.  splits = 2 is the fast form (k_tcf_inv,
+    k_tcf_fwd), splits = 3 the four-step form (k_tc_fft)."""
     peak, kind = _load_tensor_peak()
-    fa = prof.stage_a_snapshots * _tc_flops(128, splits)
-    fbc = prof.stage_bc_chunks * (_tc_flops(143, splits) + _tc_flops(128, splits))
+    if splits == 2:
+        fa = prof.stage_a_snapshots * TCF_INV_FLOPS
+        fbc = prof.stage_bc_chunks * (TCF_FWD_FLOPS + TCF_INV_FLOPS)
+        names = ("k_tcf_inv (stage A)", "k_tcf_fwd + k_tcf_inv (stages B, C)")
+    else:
+        fa = prof.stage_a_snapshots * _tc_flops(128, splits)
+        fbc = prof.stage_bc_chunks * (_tc_flops(143, splits) + _tc_flops(128, splits))
+        names = ("k_tc_fft span A", "k_tc_fft span B+C")
     ta = fa / (prof.stage_a_ms * 1e-3) / 1e12 if prof.stage_a_ms else 0.0
     tbc = fbc / (prof.stage_bc_ms * 1e-3) / 1e12 if prof.stage_bc_ms else 0.0
     dom_bc = prof.stage_bc_ms >= prof.stage_a_ms
     ach = tbc if dom_bc else ta
     n = max(prof.stage_bc_launches if dom_bc else prof.stage_a_launches, 1)
-    return {"bound": "tensor", "kernel": "k_tc_fft span " + ("B+C" if dom_bc else "A"), "achieved": ach,
+    return {"bound": "tensor", "kernel": names[1] if dom_bc else names[0], "achieved": ach,
             "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None, "peak_kind": kind,
             "ms_per_launch": (prof.stage_bc_ms if dom_bc else prof.stage_a_ms) / n,
             "flops_per_launch": (fbc if dom_bc else fa) / n,
@@ -525,7 +546,8 @@ def run_ours(args):
             for prec in PRECS:
                 if prec == args.precision:
                     continue
-                ors, o = _group_arm(prec, frames, spec, pkts, d_pkts, min(args.steps, 10), 3, local_rank, 1, 3)
+                ors, o = _group_arm(prec, frames, spec, pkts, d_pkts, min(args.steps, 10), 3, local_rank, 1,
+                                     max(3, min(args.steps, 10)))
                 others[prec] = (ors, o)
         cpu = refs = None
         if world == 1 and not args.no_cpu:

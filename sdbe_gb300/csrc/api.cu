@@ -672,8 +672,8 @@ int sdbe_process(sdbe_resampler *h, const void *packets, int64_t n_packets, int3
     int rc = plan_call(h, packets, n_packets, n_frames, b_zero, out, out_bytes, flags, pick(h, stream), c);
     if (!rc) rc = prepare_call(c);
     if (!rc && h->cfg.precision != SDBE_PRECISION_FP32) {
-        rc = tc_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st);
-        if (!rc && !c.aligned) rc = ship_call(c, 0, c.n_out);
+        rc = tc_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st,
+                      [&](int64_t lo, int64_t hi) { return c.aligned ? SDBE_OK : ship_call(c, lo, hi); });
     } else if (!rc) {
         rc = fft_chain(h, h->spec, h->spec_pol_stride, c.n_batches, c.pt, c.st,
                        [&](int64_t lo, int64_t hi) { return c.aligned ? SDBE_OK : ship_call(c, lo, hi); });

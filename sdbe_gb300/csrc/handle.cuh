@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -182,9 +183,10 @@ inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t 
 }
 
 // The FFT chain of sdbe_process on a tensor-core handle (k_tc.cu): same
-// arguments as fft_chain, payload complete when it returns (queued on st).
+// arguments as fft_chain (on_wave(lo, hi) after the wave that completes
+// payload packets [lo, hi) is queued), payload complete when it returns.
 int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
-             const PayloadTarget &tgt, cudaStream_t st);
+             const PayloadTarget &tgt, cudaStream_t st, const std::function<int(int64_t, int64_t)> &on_wave);
 
 // Batches [b0, b0 + nb) of one handle's packed spectra in a tensor-core wave.
 struct TcWaveItem {

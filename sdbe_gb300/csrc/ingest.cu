@@ -196,7 +196,8 @@ int run_device(sdbe_resampler *h, const Policy &after, const uint8_t *dev_pkts, 
             }
             PayloadTarget pt{gout, gbytes / 2, framed ? kOutPkt : kOutPktData, framed ? 32 : 0};
             int rc = h->cfg.precision != SDBE_PRECISION_FP32
-                         ? tc_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st)
+                         ? tc_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st,
+                                    [](int64_t, int64_t) { return SDBE_OK; })
                          : fft_chain(h, spec, pol_stride, kGroupSnaps / kBatchSnaps, pt, st,
                                      [](int64_t, int64_t) { return SDBE_OK; });
             if (rc) return rc;

@@ -844,11 +844,12 @@ int tc_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st)
 // The FFT chain of sdbe_process in the tensor-core form: the first batch of a
 // stream alone (it sets the thresholds), then waves of up to `wave` batches.
 int tc_chain(sdbe_resampler *h, const uint32_t *spec, int64_t spec_pol_stride, int64_t n_batches,
-             const PayloadTarget &tgt, cudaStream_t st) {
+             const PayloadTarget &tgt, cudaStream_t st, const std::function<int(int64_t, int64_t)> &on_wave) {
     for (int64_t b = 0; b < n_batches;) {
         const bool first = !h->thresholds_set;
         const int64_t nb = first ? 1 : wave_len(h, h->wave, n_batches - b);
         if (int rc = tc_wave_multi({TcWaveItem{h, spec, spec_pol_stride, b, nb, tgt}}, first, st)) return rc;
+        if (int rc = on_wave(b * kChunks, (b + nb) * kChunks)) return rc;
         b += nb;
     }
     return SDBE_OK;

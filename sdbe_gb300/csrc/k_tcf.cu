@@ -89,8 +89,8 @@ constexpr uint32_t kInvOffStg = kInvOffG + kG32Bytes + kG16Bytes;
 // hit distinct banks), e^{2 pi i n3/512} (16)
 constexpr int kTabA1 = 0, kTabA2 = 32, kTabB = kTabA2 + 512, kTabC = kTabB + 544, kInvTabLen = kTabC + 16;
 constexpr uint32_t kStgPacked = 2 * 8192, kStgBins = kTcfBinsLen * 4;  // packed: one snapshot per team
-// packed input: a 256-entry float4 table (e, d) of a code pair, after the tables
-constexpr uint32_t kPairLutBytes = 256 * 16;
+// packed input: two 16-entry float2 tables of a code pair's (e, d) parts, after the tables
+constexpr uint32_t kPairLutBytes = 32 * 8;
 constexpr uint32_t inv_smem(bool bins) {
     return kInvOffStg + (bins ? kStgBins : kStgPacked) + kInvTabLen * 8 + (bins ? 0u : kPairLutBytes) + 1024;
 }
@@ -101,7 +101,8 @@ constexpr uint32_t kFwdX1 = 80896;                  // DFT-16 operand, DFT-11 op
 constexpr uint32_t kG16f = 64 * 32 * 2, kG8f = 32 * 16 * 2, kG11f = 64 * 32 * 2, kG13f = 64 * 32 * 2;
 constexpr uint32_t kFwdOffG = kFwdX0 + kFwdX1;
 constexpr uint32_t kFwdOffTab = kFwdOffG + kG16f + kG8f + kG11f + kG13f;
-// float2 tables: 2^-8 W_128^e (e < 128), W_36608^(128 a) (a <= 143, 144 slots), W_36608^b (b < 128)
+// float2 tables: 2^-8 W_128^(n8 k16) at 8 k16 + n8 (the 8 lanes of a row group read 8
+// consecutive entries), W_36608^(128 a) (a <= 143, 144 slots), W_36608^b (b < 128)
 constexpr int kTabW128 = 0, kTabQHi = 128, kTabQLo = kTabQHi + 144, kFwdTabLen = kTabQLo + 128;
 constexpr uint32_t kFwdSmem = kFwdOffTab + kFwdTabLen * 8 + 1024;
 static_assert(kFwdSmem <= 232448 && inv_smem(true) <= 232448, "shared memory above 227 KB");
@@ -147,6 +148,16 @@ __device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t by
                  "r"(bytes)
                  : "memory");
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Piece i (at most 16 KB) of an L2 prefetch of `bytes` (a multiple of 16) at
+// the 16-byte aligned src; the calling threads take i = 0, 1, ... .
+__device__ __forceinline__ void l2_prefetch_piece(const void *src, uint32_t bytes, int i) {
+    const uint32_t off = 16384u * static_cast<uint32_t>(i);
+    if (off < bytes) {
+        const uint32_t n = bytes - off < 16384u ? bytes - off : 16384u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(static_cast<const char *>(src) + off), "r"(n)
+                     : "memory");
+    }
 }
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
@@ -357,9 +368,13 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
     uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint32_t *stg_all = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
     float2 *tab = reinterpret_cast<float2 *>(sm + kInvOffStg + (kBins ? kStgBins : kStgPacked));
-    // C2R pairing of two 2-bit code nibbles (y at bits 4-7, the mirror ym at
-    // bits 0-3): (e, d) = (y + conj ym, y - conj ym), exact small integers
-    float4 *pair_lut = reinterpret_cast<float4 *>(tab + kInvTabLen);
+    // C2R pairing of two 2-bit code nibbles y and ym (re code at bits 2-3, im
+    // code at bits 0-1): (e, d) = (y + conj ym, y - conj ym), exact small
+    // integers, as two tables of 16 entries (128 bytes each, so a half-warp's
+    // loads hit distinct banks or broadcast): entry (yr << 2 | mr) holds
+    // (Re e, Re d) = (yr + mr, yr - mr), entry 16 + (yi << 2 | mi) holds
+    // (Im e, Im d) = (yi - mi, yi + mi)
+    float2 *pair_lut = tab + kInvTabLen;
     __shared__ __align__(8) CtlInv ctl;
     __shared__ double red[2][2 * kTeamEpiWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -382,10 +397,9 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
         uint4 *dst = reinterpret_cast<uint4 *>(sm + kInvOffG);
         for (int i = tid; i < static_cast<int>((kG32Bytes + kG16Bytes) / 16); i += kInvThreads) dst[i] = __ldg(src + i);
         for (int i = tid; i < kInvTabLen; i += kInvThreads) tab[i] = __ldg(a.tab + i);
-        if (!kBins && tid < 256) {
-            const float yr = static_cast<float>((tid >> 6) & 3) - 2.f, yi = static_cast<float>((tid >> 4) & 3) - 2.f;
-            const float mr = static_cast<float>((tid >> 2) & 3) - 2.f, mi = static_cast<float>(tid & 3) - 2.f;
-            pair_lut[tid] = make_float4(yr + mr, yi - mi, yr - mr, yi + mi);
+        if (!kBins && tid < 32) {
+            const float y = static_cast<float>((tid >> 2) & 3) - 2.f, m = static_cast<float>(tid & 3) - 2.f;
+            pair_lut[tid] = tid < 16 ? make_float2(y + m, y - m) : make_float2(y - m, y + m);
         }
     }
     if (warp == 0) {
@@ -537,11 +551,12 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                     const int pos = 256 * A + 32 * (B >> 1) + ((B & 1) ? L1 : L0);
                     float2 zk, zm;
                     if (n3 != 8) {
-                        const uint32_t idx = ((stg[pos] >> sh) & 15u) << 4 | ((stg[pos ^ 2030] >> shm) & 15u);
-                        const float4 ed = pair_lut[idx];
-                        const float2 tt = cmul(make_float2(ed.z, ed.w), cmul(tA, tB[B]));
-                        zk = make_float2(ed.x - tt.y, ed.y + tt.x);
-                        zm = make_float2(ed.x + tt.y, tt.x - ed.y);
+                        const uint32_t yn = stg[pos] >> sh, mn = stg[pos ^ 2030] >> shm;
+                        const float2 lr = pair_lut[(yn & 12u) | ((mn >> 2) & 3u)];
+                        const float2 li = pair_lut[16u | ((yn << 2) & 12u) | (mn & 3u)];
+                        const float2 tt = cmul(make_float2(lr.y, li.y), cmul(tA, tB[B]));
+                        zk = make_float2(lr.x - tt.y, li.x + tt.x);
+                        zm = make_float2(lr.x + tt.y, tt.x - li.x);
                     } else {  // k % 8 = 0: the mirror's word is 2048 - w
                         const int k = 512 * (4 * A + u) + 16 * (8 * B + av) + 8;
                         c2r_pair(nib(stg[pos] >> sh), stg_value(stg, kMA - k), cmul(tA, tB[B]), zk, zm);
@@ -783,9 +798,14 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 input_row(et + 256);
                 team_sync();  // staging read: it takes the next item's bins
                 if (et == 0) fetch_bins(m + 1);
+                // this team's next bins to L2, so that their copy into the staging
+                // (once the other team has read item m + 1's) reads L2, not HBM
+                if (et < 5 && item_of(m + 2) < a.n_items) l2_prefetch_piece(item_in(item_of(m + 2)), kStgBins, et);
             } else {
                 if (OUT == OUT_TS_HALF && et == 0) bulk_wait_read();  // the last item's series has left X
                 land();
+                // the team's next snapshot into registers now, a whole item ahead of its use
+                prefetch(m + 2);
                 team_sync();
                 input_n3(e);
                 input_n3(15 - e);
@@ -803,7 +823,6 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             const int64_t local = item - s.item0;
             const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
             wait_mma();
-            if constexpr (!kBins) prefetch(m + 2);  // consumed by the next item's land()
 #pragma unroll 1
             for (int j = h; j < 8; j += 2) epi3(j, s, pol, loc);
             if constexpr (OUT == OUT_TS_HALF) {  // the time series (64 KB, natural order) to global
@@ -961,7 +980,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
         };
         // B1: DFT-16 out (k16), rows 8 nA' + n8 -> B2 operand row 144 k16 + nA', K n8:
         // a thread's 16 stores are one address plus 4608 k16.  Twiddle 2^-8
-        // W_128^(n8 k16) from the table (8 distinct entries per load, 4 lanes each).
+        // W_128^(n8 k16) from the table: per load 8 consecutive entries (64 bytes,
+        // distinct banks), 4 lanes each.
         auto epi1 = [&](int j, uint32_t t) {
             const int r = 128 * j + 32 * q + lane, nAp = r >> 3, n8 = r & 7;
             uint32_t r0[16], r1[16];
@@ -972,7 +992,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
                 uint8_t *d0 = X0 + sw32_off(nAp, n8);
 #pragma unroll
                 for (int k16 = 0; k16 < 16; ++k16) {
-                    const float2 y = cmul(acc2(k16 < 8 ? r0 : r1, k16 & 7), tab[kTabW128 + ((n8 * k16) & 127)]);
+                    const float2 y = cmul(acc2(k16 < 8 ? r0 : r1, k16 & 7), tab[kTabW128 + 8 * k16 + n8]);
                     *reinterpret_cast<uint32_t *>(d0 + 4608 * k16) = pack_half2(y.x, y.y);
                 }
             }
@@ -988,7 +1008,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     const int k16 = 4 * ep.grp + i;
-                    const float2 y = cmul(acc2(r0, i), tab[kTabW128 + ((n8 * k16) & 127)]);
+                    const float2 y = cmul(acc2(r0, i), tab[kTabW128 + 8 * k16 + n8]);
                     *reinterpret_cast<uint32_t *>(d0 + 4608 * i) = pack_half2(y.x, y.y);
                 }
             }
@@ -1065,7 +1085,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             w = make_float2(0.25f * w.x, 0.25f * w.y);
 #pragma unroll 2
             for (int jj = 2 * et; jj < kMA; jj += 2 * kEpiThreads, qq += 2 * kEpiThreads) {
-                const float2 za0 = h2f(Z[qq]), za1 = h2f(Z[qq + 1]);
+                float2 za0, za1;
+                if ((qq & 1) == 0) {  // skip = 8 trim_mhz is even: one 8-byte load
+                    const uint2 za = *reinterpret_cast<const uint2 *>(Z + qq);
+                    za0 = h2f(za.x);
+                    za1 = h2f(za.y);
+                } else {
+                    za0 = h2f(Z[qq]);
+                    za1 = h2f(Z[qq + 1]);
+                }
                 const float2 zb1 = h2f(Z[kMB - 1 - qq]);
                 const float2 y0 = qq == 0 ? pair1(0) : pairw(za0, h2f(Z[kMB - qq]), w);
                 const float2 y1 = pairw(za1, zb1, cmul(w, w1));
@@ -1088,6 +1116,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
         if (blockIdx.x < a.n_items) fetch(blockIdx.x);
         for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
             ep.wait_staging();
+            // the CTA's next chunk to L2 (five pieces), so that its copy into X0
+            // after this chunk's DFT-13 reads L2, not HBM
+            if (et < 5 && item + gridDim.x < a.n_items) {
+                int64_t pn, ln;
+                const SegFwd &sn = a.s[item_pos(item + gridDim.x, pn, ln)];
+                l2_prefetch_piece(sn.in + pn * sn.in_pol_stride + ln * static_cast<int64_t>(kNB), kNB * 2, et);
+            }
             input();
             ep.publish_all(1);
             // B1: tiles 0-7 two per group, the ninth split by columns
@@ -1191,10 +1226,11 @@ std::vector<uint8_t> build_blob() {
     append(blob, dft_matrix_hilo(11, -1, 32, 32, 64));
     append(blob, dft_matrix_hilo(13, -1, 32, 32, 64));
     std::vector<float2> tf(kFwdTabLen, make_float2(0.f, 0.f));
-    for (int i = 0; i < 128; ++i) {
-        const float2 w = cis(i, 128, -1);
-        tf[kTabW128 + i] = make_float2(kScaleB * w.x, kScaleB * w.y);
-    }
+    for (int k16 = 0; k16 < 16; ++k16)
+        for (int n8 = 0; n8 < 8; ++n8) {
+            const float2 w = cis((n8 * k16) % 128, 128, -1);
+            tf[kTabW128 + 8 * k16 + n8] = make_float2(kScaleB * w.x, kScaleB * w.y);
+        }
     for (int i = 0; i < 144; ++i) tf[kTabQHi + i] = cis(128.0 * i, 36608, -1);
     for (int i = 0; i < 128; ++i) tf[kTabQLo + i] = cis(i, 36608, -1);
     append(blob, tf);
