@@ -364,6 +364,7 @@ struct CtlInv {
 template <int IN, int OUT>
 __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
     constexpr bool kBins = IN == IN_BINS;
+    constexpr bool kQuant = OUT == OUT_QUANT || OUT == OUT_QUANT_SUMS;  // 2-bit payload out, bulk-stored
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint32_t *stg_all = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
@@ -531,18 +532,18 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
         // shifts and store offsets that are per-lane constants plus compile-time
         // ones.  Bins input (stage C): rows in natural order n'; a thread takes
         // n' = et and et + 256, four consecutive n1 per 16-byte store.
-        auto input_n3 = [&](int n3) {
+        auto input_n3 = [&](int n3, auto may_be_0) {  // may_be_0: std::bool_constant, n3 = 0 possible
             const int av = lane & 7, u = lane >> 3;
-            if (n3 != 0) {
+            float2 tB[4];  // W_32768^n', n' = 16 (8 B + av) + n3
+#pragma unroll
+            for (int i = 0; i < 4; ++i) tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
+            if (!decltype(may_be_0)::value || n3 != 0) {
                 const int u0 = u & 1, u1 = u >> 1;
                 const int wl = 64 * u + 2 * av + ((n3 >> 3) ^ u0);
                 const int L0 = wl + 16 * u1, L1 = wl + 16 * (1 - u1);
                 const int sh = (n3 & 7) * 4, shm = ((8 - (n3 & 7)) & 7) * 4;
                 uint8_t *S = X + 4096 * n3 + 128 * av + 4 * u;
                 uint8_t *Sm = X + 4096 * (16 - n3) + 128 * (31 - av) + 12 - 4 * u;
-                float2 tB[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) tB[i] = tab[kTabA2 + 16 * (8 * i + av) + n3];
 #pragma unroll
                 for (int it = 0; it < 16; ++it) {
                     const int A = it >> 2, B = it & 3;
@@ -565,25 +566,30 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                     *reinterpret_cast<uint32_t *>(Sm - 1024 * B + xA) = pack_half2(zm.x, zm.y);
                 }
             } else {
-#pragma unroll 1
+                // n3 = 0: k = 512 n1 + 16 n2 is nibble 0 of word w = k / 8, and its
+                // mirror 16384 - k (word 2048 - w) lies in the same row group, at
+                // (31 - n1, 32 - n2) for n2 > 0 and at (32 - n1, 0) for n2 = 0.
+                // k = 0 (lane 0, first pair) drops Im X[0] and pairs with the zero
+                // bin 16384; k = 8192, its own mirror, follows the loop.
+#pragma unroll 2
                 for (int it = 0; it < 16; ++it) {
-                    const int n1 = 4 * (it >> 2) + u, n2 = 8 * (it & 3) + av;
-                    const int np = 16 * n2, k = 512 * n1 + np;
-                    float2 y = stg_value(stg, k);
-                    float2 ym = make_float2(0.f, 0.f);
-                    const int km = kMA - k;
-                    if (k == 0)
-                        y.y = 0.f;  // the DC bin's imaginary part is ignored; X[16384] is zero
-                    else
-                        ym = stg_value(stg, km);
-                    float2 zk, zm;
-                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + np]), zk, zm);
-                    *reinterpret_cast<uint32_t *>(X + sw128_off(n2, n1)) = pack_half2(zk.x, zk.y);
-                    if (k != 0) {
-                        const int n1m = km >> 9, npm = km & 511;
-                        *reinterpret_cast<uint32_t *>(X + sw128_off(32 * (npm & 15) + (npm >> 4), n1m)) =
-                            pack_half2(zm.x, zm.y);
+                    const int A = it >> 2, B = it & 3;
+                    const int n1 = 4 * A + u, n2 = 8 * B + av;
+                    const uint32_t w = static_cast<uint32_t>(64 * n1 + 2 * n2);
+                    float2 y = nib(stg[stg_pos(w)]);
+                    float2 ym = nib(stg[stg_pos((2048u - w) & 2047u)]);
+                    const bool dc = it == 0 && lane == 0;
+                    if (dc) {
+                        y.y = 0.f;
+                        ym = make_float2(0.f, 0.f);
                     }
+                    float2 zk, zm;
+                    c2r_pair(y, ym, cmul(tab[kTabA1 + n1], tab[kTabA2 + 16 * n2]), zk, zm);
+                    *reinterpret_cast<uint32_t *>(X + sw128_off(n2, n1)) = pack_half2(zk.x, zk.y);
+                    const bool n2z = B == 0 && av == 0;
+                    if (!dc)
+                        *reinterpret_cast<uint32_t *>(X + sw128_off(n2z ? 0 : 32 - n2, n2z ? 32 - n1 : 31 - n1)) =
+                            pack_half2(zm.x, zm.y);
                 }
                 if (lane == 0) {  // k = 8192, its own mirror
                     const float2 y = stg_value(stg, kMA / 2);
@@ -718,8 +724,9 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 // codes of k3 < 8 and k3 >= 8 as two words (k3 at bits 4 (k3 % 8)),
                 // an 8 x 8 nibble transpose over the 8 lanes leaves lane c with
                 // the words of k3 = c and 8 + c.
-                uint32_t *words = reinterpret_cast<uint32_t *>(s.o.out + pol * s.o.out_pol_stride +
-                                                               (s.o.pkt0 + loc) * s.o.pkt_stride + s.o.payload_off);
+                // the chunk's 8192-byte payload is staged in the (consumed) operand
+                // buffer and leaves in one bulk store after the stage
+                uint32_t *words = reinterpret_cast<uint32_t *>(X);
                 const float th = kRescaleC * s.o.thr[pol], off = kRescaleC * s.o.thr[2 + pol];
                 uint32_t wl = 0, wh = 0;
 #pragma unroll
@@ -794,6 +801,10 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             if constexpr (kBins) {
                 if (!err_on() && !mbar_wait(&ctl.stg[t], sph, lim)) raise();
                 sph ^= 1u;
+                if constexpr (kQuant) {  // the last item's payload has left X
+                    if (et == 0) bulk_wait_read();
+                    team_sync();
+                }
                 input_row(et);
                 input_row(et + 256);
                 team_sync();  // staging read: it takes the next item's bins
@@ -807,8 +818,8 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 // the team's next snapshot into registers now, a whole item ahead of its use
                 prefetch(m + 2);
                 team_sync();
-                input_n3(e);
-                input_n3(15 - e);
+                input_n3(e, std::true_type{});
+                input_n3(15 - e, std::false_type{});
             }
             publish();
             wait_mma();
@@ -832,10 +843,17 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                     bulk_s2g(static_cast<__half *>(s.out) + pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA), X,
                              kNA * 2);
             }
+            if constexpr (kQuant) {  // the payload (8192 bytes, natural order) to global
+                fence_async_smem();
+                team_sync();
+                if (et == 0)
+                    bulk_s2g(s.o.out + pol * s.o.out_pol_stride + (s.o.pkt0 + loc) * s.o.pkt_stride + s.o.payload_off,
+                             X, 8192);
+            }
             chunk_stats(s, pol, loc);
             fence_before();  // tensor-memory reads done before the next item's stage-1 MMAs (after its publish)
         }
-        if (OUT == OUT_TS_HALF && et == 0) bulk_wait_all();
+        if ((OUT == OUT_TS_HALF || kQuant) && et == 0) bulk_wait_all();
     }
     fence_before();
     __syncthreads();
