@@ -149,6 +149,15 @@ def _tc_roofline(prof, steps, splits):
     the inverse 16384 per chunk.  splits = 2 is the fast form (k_tcf_inv,
     k_tcf_fwd), splits = 3 the four-step form (k_tc_fft)."""
     peak, kind = _load_tensor_peak()
+    if splits == 2 and prof.fused_launches:
+        # one launch per wave (k_tcf_chain): stages A, B and C together
+        chunks = prof.fused_chunks
+        f = chunks * 143 // 128 * TCF_INV_FLOPS + chunks * (TCF_FWD_FLOPS + TCF_INV_FLOPS)
+        ach = f / (prof.fused_ms * 1e-3) / 1e12 if prof.fused_ms else 0.0
+        return {"bound": "tensor", "kernel": "k_tcf_chain (stages A, B, C in one launch per wave)", "achieved": ach,
+                "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None, "peak_kind": kind,
+                "ms_per_launch": prof.fused_ms / prof.fused_launches, "flops_per_launch": f / prof.fused_launches,
+                "stage_ms_per_step": _stage_ms(prof, steps)}
     if splits == 2:
         fa = prof.stage_a_snapshots * TCF_INV_FLOPS
         fbc = prof.stage_bc_chunks * (TCF_FWD_FLOPS + TCF_INV_FLOPS)
@@ -166,8 +175,16 @@ def _tc_roofline(prof, steps, splits):
             "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "traffic": None, "peak_kind": kind,
             "ms_per_launch": (prof.stage_bc_ms if dom_bc else prof.stage_a_ms) / n,
             "flops_per_launch": (fbc if dom_bc else fa) / n,
-            "stage_ms_per_step": {"stage_a": prof.stage_a_ms / steps, "stage_bc": prof.stage_bc_ms / steps},
+            "stage_ms_per_step": _stage_ms(prof, steps),
             "tensor_tflops": {"span_a": ta, "span_bc": tbc}}
+
+
+def _stage_ms(prof, steps):
+    """Per-step device time of the stage launches (CUDA events)."""
+    d = {"stage_a": prof.stage_a_ms / steps, "stage_bc": prof.stage_bc_ms / steps}
+    if prof.fused_launches:
+        d["fused_abc"] = prof.fused_ms / steps
+    return d
 
 
 def cufft_library_baseline(n_batches, samples_per_step, skip):
@@ -338,6 +355,7 @@ def run_reference(args):
 
 
 PRECS = ("fp32", "tc16", "tc16fast")
+STAGES = {"default": 0, "fused": 1, "split": 3}
 
 
 def _prec_code(name):
@@ -375,7 +393,8 @@ FLOP_A = 2.5 * 32768 * 15
 FLOP_BC = 2.5 * 36608 * float(np.log2(36608)) + 2.5 * 32768 * 15
 
 
-def _group_arm(prec, frames, spec, pkts, d_pkts, steps, warmup, local_rank, world, e2e_steps, clocks=None, wave=0):
+def _group_arm(prec, frames, spec, pkts, d_pkts, steps, warmup, local_rank, world, e2e_steps, clocks=None, wave=0,
+               stages=0):
     """One precision on the group512 workload: device-resident timing (value,
     per-stage CUDA events), then end to end through the C ABI with pinned
     host buffers (e2e).  Returns the figures and the open handle."""
@@ -385,7 +404,7 @@ def _group_arm(prec, frames, spec, pkts, d_pkts, steps, warmup, local_rank, worl
     from sdbe_gb300 import Resampler, host_buffer
 
     rs = Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=frames, wave_batches=wave,
-                   precision=_prec_code(prec))
+                   precision=_prec_code(prec), stage_launches=stages)
     out_bytes = rs.output_bytes(frames)
     n_batches = out_bytes // (2 * 128 * 8192)
     samples = n_batches * OUT_SAMPLES_PER_BATCH * 2
@@ -486,7 +505,8 @@ def run_ours(args):
 
     # ---- headline arm: the precision asked for (FP32 by default) -----------
     rs, main = _group_arm(args.precision, frames, spec, pkts, d_pkts, args.steps, args.warmup, local_rank, world,
-                          max(3, min(args.steps, 10)), clocks=ClockSampler(gpu), wave=args.wave)
+                          max(3, min(args.steps, 10)), clocks=ClockSampler(gpu), wave=args.wave,
+                          stages=STAGES[args.stages])
     prof = main["prof"]
     samples_per_step = main["samples_per_step"]
     n_batches = main["n_batches"]
@@ -566,8 +586,7 @@ def run_ours(args):
             op = o["prof"]
             arms[prec] = {"value": o["value"], "unit": "GS/s", "x_realtime": o["x_realtime"],
                           "ms_per_step": o["ms_per_step"], "steps": o["steps"], "e2e": o["e2e"],
-                          "stage_ms_per_step": {"stage_a": op.stage_a_ms / o["steps"],
-                                                "stage_bc": op.stage_bc_ms / o["steps"]},
+                          "stage_ms_per_step": _stage_ms(op, o["steps"]),
                           "vs_headline": o["value"] / value, "precision": precision.get(prec),
                           "roofline": _tc_roofline(op, o["steps"], 3 if prec == "tc16" else 2)
                           if prec != "fp32" else None}
@@ -641,7 +660,7 @@ def _streams8_measure(prec, s8, steps, warmup, local_rank, clocks, wave_arg=0):
 
     def make(shape):
         hs = [Resampler(trim_mhz=TRIM_MHZ, device=local_rank, max_frames=f, wave_batches=shape["wave"],
-                        precision=_prec_code(prec)) for f in frames]
+                        precision=_prec_code(prec), stage_launches=shape.get("stages", 0)) for f in frames]
         outs = [torch.empty(h.output_bytes(f), dtype=torch.uint8, device="cuda") for h, f in zip(hs, frames)]
         return hs, outs
 
@@ -672,6 +691,9 @@ def _streams8_measure(prec, s8, steps, warmup, local_rank, clocks, wave_arg=0):
     key = "streams8|" + ("" if prec == "fp32" else prec + "|") + ",".join(map(str, frames))
     default = {"wave": wave_arg or 64, "per_launch": len(frames)}
     space = {"wave": [wave_arg] if wave_arg else [16, 32, 48, 64], "per_launch": [1, 2, len(frames)]}
+    if prec == "tc16fast":  # the fast form's waves: one fused launch (1) or a launch per stage (3)
+        default["stages"] = 1
+        space["stages"] = [1, 3]
     shape, table = autotune.tune_shape(key, measure, space, default)
     default_ms = table.get(autotune._shape_key(default))
     wave, per_launch = shape["wave"], shape["per_launch"]
@@ -696,6 +718,9 @@ def _streams8_measure(prec, s8, steps, warmup, local_rank, clocks, wave_arg=0):
     for q in profs[per_launch::per_launch]:
         prof.stage_a_ms += q.stage_a_ms
         prof.stage_bc_ms += q.stage_bc_ms
+        prof.fused_ms += q.fused_ms
+        prof.fused_launches += q.fused_launches
+        prof.fused_chunks += q.fused_chunks
     n_launches = sum(int(q.launches) for q in profs)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -931,7 +956,7 @@ def run_stress(args):
                       "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
                       "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes}),
         "thresholds_after_run": {"pol0": float(st.threshold[0]), "pol1": float(st.threshold[1])},
-        "stage_ms_per_step": {"stage_a": prof.stage_a_ms / n_passes, "stage_bc": prof.stage_bc_ms / n_passes},
+        "stage_ms_per_step": _stage_ms(prof, n_passes),
         "e2e": {"value": n_passes * samples / e2e_s / 1e9, "unit": "GS/s", "ms_per_step": e2e_s / n_passes * 1e3,
                 "h2d_bytes_per_step": int(pkt_bytes), "d2h_bytes_per_step": int(n_streams * out_bytes),
                 "api": "process_multi(host pinned buffers, asynchronous) per group, sdbe_sync at the end"},
@@ -958,6 +983,9 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc16", "tc16fast"],
                     help="fp32 radix kernels (default) or an FP16 tensor-core form "
                          "(tc16: data and DFT matrix split hi+lo; tc16fast: DFT matrix split, data FP16)")
+    ap.add_argument("--stages", default="default", choices=list(STAGES),
+                    help="tc16fast waves: one fused launch for stages A, B and C, or a launch per stage "
+                         "(default: the library's)")
     ap.add_argument("--workload", default="group512", choices=["group512", "streams8", "stress32"],
                     help="group512: one 512-frame packet stream (default); streams8: 8 uneven streams, multi "
                          "pass; stress32: 32 impaired streams x 2048 frames, windowed thresholds")

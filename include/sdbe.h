@@ -78,6 +78,8 @@ extern "C" {
  * (two products).  All entry points and threshold modes. */
 #define SDBE_PRECISION_TC16 1
 #define SDBE_PRECISION_TC16_FAST 2
+#define SDBE_STAGES_FUSED 1
+#define SDBE_STAGES_SPLIT 3
 
 /* sdbe_process flags */
 #define SDBE_IN_HOST 1u            /* packets are in host memory (copied in)             */
@@ -104,7 +106,11 @@ typedef struct sdbe_config {
                                /* max_frames cannot fill 64; scratch 37.5 MB per batch     */
     int32_t threshold_window;  /* SDBE_THRESH_WINDOW: batches in the window (0 = 64)        */
     int32_t precision;         /* SDBE_PRECISION_*                                          */
-    int32_t reserved[7];
+    int32_t stage_launches;    /* SDBE_PRECISION_TC16_FAST waves: SDBE_STAGES_FUSED (one
+                                  persistent launch runs stages A, B and C on a device work
+                                  queue) or SDBE_STAGES_SPLIT (a launch per stage); 0 =
+                                  SDBE_STAGES_FUSED.  Other precisions ignore it.          */
+    int32_t reserved[6];
 } sdbe_config;
 
 typedef struct sdbe_state {
@@ -298,7 +304,8 @@ int sdbe_reset(sdbe_resampler *h);
 /* Per-stage GPU timing, the counterpart of the reference's GPU_DEBUG event
  * timing (vdif_inout_gpu_thread.cu:594-621).  While enabled, sdbe_process
  * records CUDA events around every stage-A (SwarmC2R) and stage-BC (fused
- * SwarmR2C + R2dbeC2R + quantize2bit) launch on the stream it runs on.
+ * SwarmR2C + R2dbeC2R + quantize2bit) launch on the stream it runs on, and
+ * around each one-launch wave of SDBE_STAGES_FUSED (fused_*).
  * sdbe_profile_read waits for the recorded events, returns the totals since
  * the last read and clears them.  launches counts every kernel sdbe_process
  * launched since the last read, enabled or not. */
@@ -310,7 +317,10 @@ typedef struct sdbe_profile {
     int64_t stage_bc_launches;
     int64_t stage_bc_chunks;
     double stage_bc_ms;
-    int64_t reserved[4];
+    int64_t fused_launches;      /* SDBE_STAGES_FUSED waves: one launch for stages A, B, C */
+    int64_t fused_chunks;        /* chunks of those waves (snapshots = chunks * 143 / 128)  */
+    double fused_ms;
+    int64_t reserved[1];
 } sdbe_profile;
 int sdbe_profile_enable(sdbe_resampler *h, int32_t enable);
 int sdbe_profile_read(sdbe_resampler *h, sdbe_profile *out);

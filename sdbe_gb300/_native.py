@@ -28,6 +28,7 @@ THRESH_FIRST_BATCH, THRESH_FIXED, THRESH_WINDOW = 0, 1, 2
 THRESH_BLOCK = 16
 MAP_APHIDS, MAP_MAR2015 = 0, 1
 PRECISION_FP32, PRECISION_TC16, PRECISION_TC16_FAST = 0, 1, 2
+STAGES_FUSED, STAGES_SPLIT = 1, 3
 IN_HOST, OUT_HOST, OUT_FRAMED, SYNC, ASYNC, OUT_ALIGNED, IN_8PAC = 1, 2, 4, 8, 16, 32, 64
 PAC8_BYTES = 8504
 NOALLOC_MAX_SAMPLES = 134217728
@@ -37,7 +38,7 @@ class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("trim_mhz", C.c_int32), ("max_frames", C.c_int32),
                 ("threshold_mode", C.c_int32), ("pol1_uses_pol0_threshold", C.c_int32),
                 ("channel_map", C.c_int32), ("wave_batches", C.c_int32), ("threshold_window", C.c_int32),
-                ("precision", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("precision", C.c_int32), ("stage_launches", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class State(C.Structure):
@@ -55,7 +56,8 @@ class Result(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("launches", C.c_int64), ("stage_a_launches", C.c_int64), ("stage_a_snapshots", C.c_int64),
                 ("stage_a_ms", C.c_double), ("stage_bc_launches", C.c_int64), ("stage_bc_chunks", C.c_int64),
-                ("stage_bc_ms", C.c_double), ("reserved", C.c_int64 * 4)]
+                ("stage_bc_ms", C.c_double), ("fused_launches", C.c_int64), ("fused_chunks", C.c_int64),
+                ("fused_ms", C.c_double), ("reserved", C.c_int64 * 1)]
 
 
 class TimeTemplate(C.Structure):

@@ -9,6 +9,10 @@ The shape of a pass over several streams has three parts:
 * ``per_launch``: how many stream handles share one fused launch
   (``sdbe_process_multi``); fewer per launch gives shorter launches that the
   next call can overlap, more gives fuller persistent grids.
+* ``stages``: for ``SDBE_PRECISION_TC16_FAST``, whether a wave's three
+  transform stages run as one persistent launch on a device work queue
+  (``SDBE_STAGES_FUSED``: no grid tail and launch gap between the stages)
+  or as a launch per stage (``SDBE_STAGES_SPLIT``).
 * ``precision``: the FFT form, when the caller admits more than one
   (``SDBE_PRECISION_FP32`` and ``SDBE_PRECISION_TC16_FAST`` both meet the
   99.9% 2-bit agreement bar; which is faster depends on the stream mix).

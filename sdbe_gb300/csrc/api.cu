@@ -84,6 +84,7 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->tcf_tabs);
     cudaFree(h->tcf_bins);
     cudaFree(h->tcf_half);
+    cudaFree(h->tcf_chain);
     if (h->tc_status_host) cudaFreeHost(h->tc_status_host);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);
@@ -583,6 +584,8 @@ int sdbe_create(const sdbe_config *cfg, sdbe_resampler **out) {
     if (cfg->precision != SDBE_PRECISION_FP32 && cfg->precision != SDBE_PRECISION_TC16 &&
         cfg->precision != SDBE_PRECISION_TC16_FAST)
         return fail(nullptr, SDBE_ERR_ARG, "unknown precision");
+    if (cfg->stage_launches != 0 && cfg->stage_launches != SDBE_STAGES_FUSED && cfg->stage_launches != SDBE_STAGES_SPLIT)
+        return fail(nullptr, SDBE_ERR_ARG, "stage_launches must be 0, SDBE_STAGES_FUSED or SDBE_STAGES_SPLIT");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
         cudaGetLastError();
@@ -831,6 +834,10 @@ int sdbe_profile_read(sdbe_resampler *h, sdbe_profile *out) {
             out->stage_a_launches += 1;
             out->stage_a_snapshots += t.units;
             out->stage_a_ms += ms;
+        } else if (t.kind == 2) {
+            out->fused_launches += 1;
+            out->fused_chunks += t.units;
+            out->fused_ms += ms;
         } else {
             out->stage_bc_launches += 1;
             out->stage_bc_chunks += t.units;

@@ -89,6 +89,8 @@ struct sdbe_resampler {
     int64_t tcf_bins_bytes = 0;
     void *tcf_half = nullptr;     // FP16 time series of sdbe_resample_chunks inputs (on first use)
     int64_t tcf_half_bytes = 0;
+    uint8_t *tcf_chain = nullptr; // tickets and stage counters of the one-launch waves (on first use)
+    int64_t tcf_chain_bytes = 0;
     int *tc_status_host = nullptr;  // 1 after a tensor-core barrier time-out (pinned, mapped)
     int *tc_status = nullptr;       // its device address
     int64_t tc_test_timeout_ns = 0; // > 0: the next fast tensor-core launch withholds a signal (test hook)

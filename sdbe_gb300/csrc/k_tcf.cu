@@ -161,13 +161,14 @@ __device__ __forceinline__ void l2_prefetch_piece(const void *src, uint32_t byte
 }
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Every bulk group of this thread but the newest complete.
+__device__ __forceinline__ void bulk_wait_all_but_newest() { asm volatile("cp.async.bulk.wait_group 1;" ::: "memory"); }
 
 // Common kernel state: barriers, tensor memory, error flag.
 constexpr int kFull = 18;           // completion barriers, one per tile of a whole stage
 struct Ctl {
-    uint64_t full[kFull], ready[2], done, stg;
+    uint64_t full[kFull], ready[2], done, stg, b13;  // b13: an item's DFT-13 MMAs retired (chain)
     uint64_t lim;  // bound of every mbarrier wait (ns)
-    uint32_t tmem_base;
     int err;
 };
 
@@ -178,6 +179,7 @@ __device__ __forceinline__ void ctl_init(Ctl &c, uint64_t lim) {
     mbar_init(&c.ready[1], kEpiWarps);
     mbar_init(&c.done, 1);
     mbar_init(&c.stg, 1);
+    mbar_init(&c.b13, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     c.err = 0;
 }
@@ -196,10 +198,12 @@ struct Issuer {
     // stage issues without waiting; the epilogue's publish of the next
     // operand (after its last tensor-memory read) orders the next stage's
     // writes after this stage's reads.
+    // With `mark` (an item's first stage), returns false without issuing when
+    // the epilogue published the end mark (*mark < 0) instead of an operand.
     template <int KSTEPS>
-    __device__ void stage_all(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, uint32_t kstep_bytes, uint32_t lbo,
+    __device__ bool stage_all(int buf, uint32_t xa, int tiles, uint32_t tile_bytes, uint32_t kstep_bytes, uint32_t lbo,
                               uint32_t sbo, uint32_t layout, uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n,
-                              uint32_t col_w) {
+                              uint32_t col_w, const volatile int64_t *mark = nullptr) {
         asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
         uint64_t gh[KSTEPS], gl[KSTEPS];
 #pragma unroll
@@ -213,6 +217,7 @@ struct Issuer {
         rphase ^= 1u << buf;
         __syncwarp();
         fence_after();
+        if (mark && *mark < 0) return false;
         const bool ok = !err_set(*c);
         for (int j = 0; j < tiles; ++j) {
             if (ok) {
@@ -227,6 +232,7 @@ struct Issuer {
             }
             commit_elect(&c->full[j]);
         }
+        return true;
     }
     __device__ void finish() {  // every MMA retired before tensor memory is freed
         commit_elect(&c->done);
@@ -281,22 +287,6 @@ struct Epi {
     }
 };
 
-__device__ __forceinline__ void tmem_alloc_all(Ctl &c, int warp) {
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&c.tmem_base)),
-                     "r"(kTmemCols));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-}
-
-__device__ __forceinline__ void teardown(Ctl &c, int *status, int warp) {
-    fence_before();
-    __syncthreads();
-    if (threadIdx.x == 0 && err_set(c)) *reinterpret_cast<volatile int *>(status) = 1;
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem_base), "r"(kTmemCols));
-}
-
 template <class A>
 __device__ __forceinline__ int seg_index(const A &a, int64_t item) {
     int j = 0;
@@ -304,6 +294,57 @@ __device__ __forceinline__ int seg_index(const A &a, int64_t item) {
     return j;
 }
 
+
+// Item order and cross-stage dependencies of a persistent stage loop.  Static
+// (ticket null): CTA b takes items b, b + G, b + 2G, ... (G CTAs).  Chain (one
+// launch runs stages A, B and C of a wave, k_tcf_chain): items are tickets
+// from a global counter, handed out in order to running CTAs, and a CTA takes
+// the next stage's tickets only once the current stage's run out, so every
+// item a later stage waits for is already held by a running CTA; each wait is
+// bounded.
+struct Sched {
+    unsigned *ticket;      // null: static order
+    const unsigned *dep;   // counters the items wait for (stage B: per stage-A batch; stage C: per stage-B item)
+    unsigned *done;        // counters the items bump once their output is in global memory
+};
+
+// Bounded wait (global time) until *p >= want, with acquire ordering.
+__device__ __forceinline__ bool wait_count(const unsigned *p, unsigned want, uint64_t limit_ns) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    if (v >= want) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        __nanosleep(256);
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        if (v >= want) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+// A counter bump after this thread's (or, behind a barrier, its CTA's) global
+// writes, with release ordering: a wait_count that sees it sees the writes.
+__device__ __forceinline__ void bump(unsigned *p) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(p) : "memory");
+}
+// Generic-proxy accesses ordered with this thread's bulk (async-proxy) copies of global memory.
+__device__ __forceinline__ void fence_proxy_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc_cols(uint32_t *dst) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_free_cols(uint32_t base) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(kTmemCols));
+}
+
+// Shared item slots of a chain phase: [t] team t's current item, its issuer's
+// mark (< 0: end), [2 + 4 t + 2 p ..] team t's (item, next) pair p, [10 + s %
+// 4] the item of stage C's staging fill s, [14 + k % 2] stage B's k-th item,
+// [18 + t] team t's item whose stage-A series awaits its completion signal.
+// The team leaders keep this state here rather than in registers: the stage-A
+// loop body runs at the register cap.
+constexpr int kSlots = 20;
 
 // ============================================================================
 // k_tcf_inv: 16384-point inverse transforms (stages A and C)
@@ -357,16 +398,29 @@ static_assert(kStgPacked == 2 * 8192, "packed staging: one 8 KB snapshot per tea
 
 struct CtlInv {
     uint64_t ready[2], mma[2], stg[2], done[2];
-    uint32_t tmem_base;
     int err;
 };
 
-template <int IN, int OUT>
-__global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
+// The kernels' control state in static shared memory: the inverse phases'
+// barriers (two sets, for stages A and C of a chain), the forward phase's,
+// the teams' FP64 partial sums, the item slots and the tensor-memory base.
+__shared__ __align__(8) CtlInv g_ctl_inv[2];
+__shared__ __align__(8) Ctl g_ctl_fwd;
+__shared__ double g_red[2][2 * kTeamEpiWarps];
+__shared__ int64_t g_slots[kSlots];
+__shared__ uint32_t g_tmem_base;
+
+// One stage-A or stage-C loop over its items (a whole k_tcf_inv launch, or a
+// phase of k_tcf_chain): sm is the 1024-byte aligned dynamic shared memory,
+// tmem_base the CTA's 512 tensor-memory columns.  Ends with a CTA barrier,
+// every MMA retired and every bulk store complete.
+template <int IN, int OUT, int CI, bool CHAIN>
+__device__ __forceinline__ void inv_phase(const ArgsInv &a, const Sched sc, uint8_t *sm, uint32_t tmem_base) {
+    CtlInv &ctl = g_ctl_inv[CI];
+    auto &red = g_red;
+    volatile int64_t *slots = g_slots;
     constexpr bool kBins = IN == IN_BINS;
     constexpr bool kQuant = OUT == OUT_QUANT || OUT == OUT_QUANT_SUMS;  // 2-bit payload out, bulk-stored
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint32_t *stg_all = reinterpret_cast<uint32_t *>(sm + kInvOffStg);
     float2 *tab = reinterpret_cast<float2 *>(sm + kInvOffStg + (kBins ? kStgBins : kStgPacked));
     // C2R pairing of two 2-bit code nibbles y and ym (re code at bits 2-3, im
@@ -376,8 +430,6 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
     // (Re e, Re d) = (yr + mr, yr - mr), entry 16 + (yi << 2 | mi) holds
     // (Im e, Im d) = (yi - mi, yi + mi)
     float2 *pair_lut = tab + kInvTabLen;
-    __shared__ __align__(8) CtlInv ctl;
-    __shared__ double red[2][2 * kTeamEpiWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int t = warp >= 9 ? 1 : 0;          // team
     const int tw = warp - 9 * t;              // warp within the team: 0 issuer, 1-8 epilogue
@@ -403,28 +455,56 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             pair_lut[tid] = tid < 16 ? make_float2(y + m, y - m) : make_float2(y - m, y + m);
         }
     }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ctl.tmem_base)),
-                     "r"(kTmemCols));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tb = ctl.tmem_base + 256u * t;
+    const uint32_t tb = tmem_base + 256u * t;
     auto err_on = [&]() { return *reinterpret_cast<const volatile int *>(&ctl.err) != 0; };
     auto raise = [&]() { *reinterpret_cast<volatile int *>(&ctl.err) = 1; };
     auto item_of = [&](int64_t m) { return static_cast<int64_t>(blockIdx.x) + m * gridDim.x; };
     const uint64_t lim = a.wait_ns;
+
+    auto item_in = [&](int64_t item) -> const void * {
+        const SegInv &s = a.s[seg_index(a, item)];
+        const int64_t local = item - s.item0;
+        const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
+        if constexpr (kBins)
+            return static_cast<const uint32_t *>(s.in) +
+                   (pol * s.in_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen));
+        else
+            return static_cast<const uint32_t *>(s.in) + pol * s.in_pol_stride + (s.first + loc) * kGroups;
+    };
+    // Chain, stage C: the bins staging is filled in the CTA's fill sequence
+    // by the MMA issuer of the team that has read the fill before (fill s + 1
+    // once team s % 2 has published its stage-1 operand).  A fill takes a
+    // ticket, waits for that item's bins, records the item in slot 10 + s % 4
+    // and copies; without an item it ends both teams (fills s and s + 1 marked
+    // -1, both staging barriers released).
+    auto fill_stg = [&](int64_t fs) {
+        int64_t z = static_cast<int64_t>(atomicAdd(sc.ticket, 1u));
+        if (z >= a.n_items) z = -1;
+        slots[10 + (fs & 3)] = z;
+        if (z < 0) {
+            slots[10 + ((fs + 1) & 3)] = -1;
+            mbar_arrive(&ctl.stg[fs & 1]);
+            mbar_arrive(&ctl.stg[(fs + 1) & 1]);
+            return;
+        }
+        if (!err_on() && !wait_count(sc.dep + z, 1u, lim)) raise();
+        fence_proxy_global();
+        fence_async_smem();
+        bulk_g2s(stg_all, item_in(z), kStgBins, &ctl.stg[fs & 1]);
+    };
 
     if (tw == 0) {
         // ---- MMA issuer of team t (whole warp; an elected lane issues) ----
         const uint32_t g32 = smem_u32(sm + kInvOffG), g16 = g32 + kG32Bytes;
         uint32_t rph = 0;
         bool withhold = a.withhold != 0 && t == 0;
+        // One GEMM stage; the first of an item returns false at the end mark.
         auto stage = [&](auto ksteps_c, int tiles, uint32_t tile_bytes, uint32_t lbo, uint32_t sbo, uint32_t layout,
-                         uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n, uint32_t col_w) {
+                         uint32_t g, uint32_t g_sbo, uint32_t g_lo, int n, uint32_t col_w, bool first) -> bool {
             constexpr int KSTEPS = decltype(ksteps_c)::value;
             uint32_t xa = smem_u32(X);
             asm volatile("" : "+r"(g), "+r"(xa));  // descriptors built here, not hoisted out of the item loop
@@ -440,6 +520,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             rph ^= 1u;
             __syncwarp();
             fence_after();
+            if (first && slots[t] < 0) return false;  // the team has no more items
             if (!err_on()) {
                 for (int j = 0; j < tiles; ++j) {
                     const uint64_t xj = x0 + ((j * tile_bytes) >> 4);
@@ -455,11 +536,29 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
                 withhold = false;  // test of the time-out path: this stage's completion is never signalled
             else
                 commit_elect(&ctl.mma[t]);
+            return true;
         };
-        for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
-            stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64);
-            stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64);
-            stage(std::integral_constant<int, 2>{}, 8, 8192, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);
+        if constexpr (CHAIN) {
+            // the team's items until its epilogue publishes the end mark; in
+            // stage C the issuer also makes the fill after the team's (in its
+            // idle time, after the stage-1 MMAs are issued)
+            int64_t fs = t;
+            if (kBins && t == 0 && lane == 0) fill_stg(0);
+            __syncwarp();
+            while (stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64,
+                         true)) {
+                if (kBins && lane == 0) fill_stg(fs + 1);
+                __syncwarp();
+                fs += 2;
+                stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64, false);
+                stage(std::integral_constant<int, 2>{}, 8, 8192, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32, false);
+            }
+        } else {
+            for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
+                stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64, false);
+                stage(std::integral_constant<int, 4>{}, 4, 16384, 16, 1024, kSwizzle128, g32, 1024, 8192, 64, 64, false);
+                stage(std::integral_constant<int, 2>{}, 8, 8192, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32, false);
+            }
         }
         commit_elect(&ctl.done[t]);  // every MMA of the team retired before tensor memory is freed
         if (!mbar_wait(&ctl.done[t], 0)) raise();  // real completion of issued MMAs: the default bound
@@ -484,30 +583,17 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.ready[t]);
         };
-        auto item_in = [&](int64_t item) -> const void * {
-            const SegInv &s = a.s[seg_index(a, item)];
-            const int64_t local = item - s.item0;
-            const int64_t pol = local >= s.n ? 1 : 0, loc = local - pol * s.n;
-            if constexpr (kBins)
-                return static_cast<const uint32_t *>(s.in) +
-                       (pol * s.in_pol_stride + loc * static_cast<int64_t>(kTcfBinsLen));
-            else
-                return static_cast<const uint32_t *>(s.in) + pol * s.in_pol_stride + (s.first + loc) * kGroups;
-        };
-        // bins input: one staging buffer, filled in item order (the team that
-        // has read item m's bins starts the copy of item m + 1's)
-        auto fetch_bins = [&](int64_t m) {
-            if (item_of(m) >= a.n_items) return;
-            fence_async_smem();
-            bulk_g2s(stg_all, item_in(item_of(m)), kStgBins, &ctl.stg[m & 1]);
-        };
         // packed input: each thread holds 32 bytes of the team's next snapshot
         uint4 pre0 = make_uint4(0, 0, 0, 0), pre1 = pre0;
-        auto prefetch = [&](int64_t m) {
-            if (item_of(m) >= a.n_items) return;
-            const uint4 *src = reinterpret_cast<const uint4 *>(item_in(item_of(m)));
+        auto prefetch = [&](int64_t z) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(item_in(z));
             pre0 = __ldg(src + 2 * et);
             pre1 = __ldg(src + 2 * et + 1);
+        };
+        // chain: a stage-A ticket of this team, -1 at the end
+        auto ticket_a = [&]() -> int64_t {
+            const int64_t z = static_cast<int64_t>(atomicAdd(sc.ticket, 1u));
+            return z < a.n_items ? z : -1;
         };
         auto land = [&]() {  // staged word w at stg_pos(w)
 #pragma unroll
@@ -788,39 +874,11 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             }
         };
 
-        if constexpr (kBins) {
-            if (t == 0 && et == 0) fetch_bins(0);
-        } else {
-            prefetch(t);
-            // team 1 starts once team 0 has written its first operand, so that
-            // the teams' MMA waits fall in each other's CUDA-core steps
-            if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0, lim)) raise();
-        }
-        for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
-            const int64_t item = item_of(m);
-            if constexpr (kBins) {
-                if (!err_on() && !mbar_wait(&ctl.stg[t], sph, lim)) raise();
-                sph ^= 1u;
-                if constexpr (kQuant) {  // the last item's payload has left X
-                    if (et == 0) bulk_wait_read();
-                    team_sync();
-                }
-                input_row(et);
-                input_row(et + 256);
-                team_sync();  // staging read: it takes the next item's bins
-                if (et == 0) fetch_bins(m + 1);
-                // this team's next bins to L2, so that their copy into the staging
-                // (once the other team has read item m + 1's) reads L2, not HBM
-                if (et < 5 && item_of(m + 2) < a.n_items) l2_prefetch_piece(item_in(item_of(m + 2)), kStgBins, et);
-            } else {
-                if (OUT == OUT_TS_HALF && et == 0) bulk_wait_read();  // the last item's series has left X
-                land();
-                // the team's next snapshot into registers now, a whole item ahead of its use
-                prefetch(m + 2);
-                team_sync();
-                input_n3(e, std::true_type{});
-                input_n3(15 - e, std::false_type{});
-            }
+        // The part of an item after its input step: three GEMM stages, their
+        // epilogues, the output.  The item is read before this warp's stage-3
+        // publish in a chain (the leader writes the next item's slot only
+        // after the stage-3 MMAs, which wait for every warp's publish).
+        auto item_body = [&](int64_t item_static) {
             publish();
             wait_mma();
             epi1(h);
@@ -829,6 +887,7 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             wait_mma();
             epi2(h);
             epi2(h + 2);
+            const int64_t item = CHAIN ? static_cast<int64_t>(slots[t]) : item_static;
             publish();
             const SegInv &s = a.s[seg_index(a, item)];
             const int64_t local = item - s.item0;
@@ -839,9 +898,20 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             if constexpr (OUT == OUT_TS_HALF) {  // the time series (64 KB, natural order) to global
                 fence_async_smem();
                 team_sync();
-                if (et == 0)
+                if (et == 0) {
+                    if (CHAIN && slots[18 + t] >= 0) {
+                        // chain: the last item's series, stored an item ago, is
+                        // complete in global memory: stage B may read its
+                        // batch.  Signalled here, where no store or load of
+                        // this thread is in flight.
+                        bulk_wait_all();
+                        fence_proxy_global();
+                        bump(sc.done + slots[18 + t] / kBatchSnaps);
+                    }
                     bulk_s2g(static_cast<__half *>(s.out) + pol * s.out_pol_stride + loc * static_cast<int64_t>(kNA), X,
                              kNA * 2);
+                    if (CHAIN) slots[18 + t] = item;
+                }
             }
             if constexpr (kQuant) {  // the payload (8192 bytes, natural order) to global
                 fence_async_smem();
@@ -852,15 +922,138 @@ __global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constan
             }
             chunk_stats(s, pol, loc);
             fence_before();  // tensor-memory reads done before the next item's stage-1 MMAs (after its publish)
+        };
+
+        if constexpr (!CHAIN) {
+            // Static order: team t takes items b + m G, m = t, t + 2, ...; the
+            // staging of the bins input is filled in item order (the team that
+            // has read item m's bins starts the copy of item m + 1's).
+            auto fetch_bins = [&](int64_t m) {
+                if (item_of(m) >= a.n_items) return;
+                fence_async_smem();
+                bulk_g2s(stg_all, item_in(item_of(m)), kStgBins, &ctl.stg[m & 1]);
+            };
+            if constexpr (kBins) {
+                if (t == 0 && et == 0) fetch_bins(0);
+            } else {
+                if (item_of(t) < a.n_items) prefetch(item_of(t));
+                // team 1 starts once team 0 has written its first operand, so that
+                // the teams' MMA waits fall in each other's CUDA-core steps
+                if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0, lim)) raise();
+            }
+            for (int64_t m = t; item_of(m) < a.n_items; m += 2) {
+                const int64_t item = item_of(m);
+                if constexpr (kBins) {
+                    if (!err_on() && !mbar_wait(&ctl.stg[t], sph, lim)) raise();
+                    sph ^= 1u;
+                    if constexpr (kQuant) {  // the last item's payload has left X
+                        if (et == 0) bulk_wait_read();
+                        team_sync();
+                    }
+                    input_row(et);
+                    input_row(et + 256);
+                    team_sync();  // staging read: it takes the next item's bins
+                    if (et == 0) fetch_bins(m + 1);
+                    // this team's next bins to L2, so that their copy into the staging
+                    // (once the other team has read item m + 1's) reads L2, not HBM
+                    if (et < 5 && item_of(m + 2) < a.n_items) l2_prefetch_piece(item_in(item_of(m + 2)), kStgBins, et);
+                } else {
+                    if (OUT == OUT_TS_HALF && et == 0) bulk_wait_read();  // the last item's series has left X
+                    land();
+                    // the team's next snapshot into registers now, a whole item ahead of its use
+                    if (item_of(m + 2) < a.n_items) prefetch(item_of(m + 2));
+                    team_sync();
+                    input_n3(e, std::true_type{});
+                    input_n3(15 - e, std::false_type{});
+                }
+                item_body(item);
+            }
+            if ((OUT == OUT_TS_HALF || kQuant) && et == 0) bulk_wait_all();
+        } else {
+            // Chain: stage A's pair j % 2 holds the team's item j and item j + 1,
+            // and its leader holds the ticket after those (pend), taken an item
+            // ahead so the ticket's latency stays off the critical path; stage
+            // C's item of the team's fill is read after the staging barrier.
+            // After the last item the issuer gets the end mark.
+            int64_t pend = -1;
+            int fs = t;
+            if constexpr (!kBins) {
+                if (et == 0) {
+                    slots[18 + t] = -1;
+                    slots[2 + 4 * t] = ticket_a();
+                    slots[2 + 4 * t + 1] = ticket_a();
+                    pend = ticket_a();
+                }
+                team_sync();
+                if (slots[2 + 4 * t] >= 0) prefetch(slots[2 + 4 * t]);
+                if (t == 1 && !err_on() && !mbar_wait(&ctl.ready[0], 0, lim)) raise();
+            }
+            for (int j = 0;; ++j) {
+                if constexpr (kBins) {
+                    if (!err_on() && !mbar_wait(&ctl.stg[t], sph, lim)) raise();
+                    sph ^= 1u;
+                    const int64_t item = slots[10 + (fs & 3)];
+                    if (item < 0) break;
+                    if (et == 0) slots[t] = item;
+                    if constexpr (kQuant) {  // the last item's payload has left X
+                        if (et == 0) bulk_wait_read();
+                        team_sync();
+                    }
+                    input_row(et);
+                    input_row(et + 256);
+                    team_sync();  // staging read (the issuer makes the next fill after the publish)
+                    fs += 2;
+                } else {
+                    const int pa = 2 + 4 * t + 2 * (j & 1);
+                    const int64_t item = slots[pa];
+                    if (item < 0) break;
+                    if (OUT == OUT_TS_HALF && et == 0) bulk_wait_read();  // the last item's series has left X
+                    land();
+                    // the team's next snapshot into registers now, a whole item ahead of its use
+                    if (slots[pa + 1] >= 0) prefetch(slots[pa + 1]);
+                    if (et == 0) {
+                        slots[t] = item;
+                        const int pb = 2 + 4 * t + 2 * ((j + 1) & 1);
+                        slots[pb] = slots[pa + 1];
+                        slots[pb + 1] = pend;
+                        pend = pend >= 0 ? ticket_a() : -1;
+                    }
+                    team_sync();
+                    input_n3(e, std::true_type{});
+                    input_n3(15 - e, std::false_type{});
+                }
+                item_body(0);
+            }
+            // end mark for the team's issuer
+            if (et == 0) slots[t] = -1;
+            publish();
+            if ((OUT == OUT_TS_HALF || kQuant) && et == 0) {
+                bulk_wait_all();
+                if (OUT == OUT_TS_HALF && slots[18 + t] >= 0) {
+                    fence_proxy_global();
+                    bump(sc.done + slots[18 + t] / kBatchSnaps);
+                }
+            }
         }
-        if ((OUT == OUT_TS_HALF || kQuant) && et == 0) bulk_wait_all();
     }
     fence_before();
     __syncthreads();
     if (threadIdx.x == 0 && *reinterpret_cast<const volatile int *>(&ctl.err) != 0)
         *reinterpret_cast<volatile int *>(a.status) = 1;
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(ctl.tmem_base), "r"(kTmemCols));
+}
+
+template <int IN, int OUT>
+__global__ void __launch_bounds__(kInvThreads, 1) k_tcf_inv(const __grid_constant__ ArgsInv a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) tmem_alloc_cols(&g_tmem_base);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tb = g_tmem_base;
+    inv_phase<IN, OUT, 0, false>(a, Sched{nullptr, nullptr, nullptr}, sm, tb);
+    if (warp == 0) tmem_free_cols(tb);
 }
 
 // ============================================================================
@@ -884,6 +1077,7 @@ struct SegFwd {
     int64_t out_pol_stride;  // bins
     int64_t n, item0;        // chunks per pol
     int skip;
+    int64_t dep0;            // chain: stage-A batch counter of the segment's first batch (pol 0)
 };
 struct ArgsFwd {
     int64_t n_items;
@@ -895,16 +1089,19 @@ struct ArgsFwd {
     uint64_t wait_ns;        // bound of every mbarrier wait
 };
 
-__global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__ ArgsFwd a) {
-    extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+// One stage-B loop over its items (a whole k_tcf_fwd launch, or a phase of
+// k_tcf_chain): warps 0-16 work, further warps of the block only join the
+// CTA barriers.  Ends with a CTA barrier and every MMA retired.
+template <bool CHAIN>
+__device__ __forceinline__ void fwd_phase(const ArgsFwd &a, const Sched sc, uint8_t *sm, uint32_t tmem_base) {
+    Ctl &ctl = g_ctl_fwd;
+    volatile int64_t *slots = g_slots;
     uint8_t *X0 = sm, *X1 = sm + kFwdX0;
     float2 *tab = reinterpret_cast<float2 *>(sm + kFwdOffTab);
-    __shared__ __align__(8) Ctl ctl;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) ctl_init(ctl, a.wait_ns);
-    {
+    if (tid < kThreads) {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.g);
         uint4 *dst = reinterpret_cast<uint4 *>(sm + kFwdOffG);
         for (int i = tid; i < static_cast<int>((kG16f + kG8f + kG11f + kG13f) / 16); i += kThreads)
@@ -914,45 +1111,111 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
         uint4 *z = reinterpret_cast<uint4 *>(sm);
         for (int i = tid; i < static_cast<int>((kFwdX0 + kFwdX1) / 16); i += kThreads) z[i] = make_uint4(0, 0, 0, 0);
     }
-    tmem_alloc_all(ctl, warp);
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tb = ctl.tmem_base;
+    const uint32_t tb = tmem_base;
+    auto item_pos = [&](int64_t item, int64_t &pol, int64_t &loc) -> int {
+        const int si = seg_index(a, item);
+        const int64_t local = item - a.s[si].item0;
+        pol = local >= a.s[si].n ? 1 : 0;
+        loc = local - pol * a.s[si].n;
+        return si;
+    };
+    auto chunk_in = [&](int64_t z) -> const __half * {  // the item's 36608 FP16 samples
+        int64_t pol, loc;
+        const SegFwd &s = a.s[item_pos(z, pol, loc)];
+        return s.in + pol * s.in_pol_stride + loc * static_cast<int64_t>(kNB);
+    };
 
     if (warp == 0) {
         Issuer is{&ctl, tb};
         const uint32_t g16 = smem_u32(sm + kFwdOffG), g8 = g16 + kG16f, g11 = g8 + kG8f, g13 = g11 + kG11f;
         const uint32_t x0 = smem_u32(X0), x1 = smem_u32(X1);
-        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-            is.stage_all<2>(1, x1, 9, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);     // DFT-16
+        auto rest = [&]() {
             is.stage_all<1>(0, x0, 18, 4096, 32, 16, 256, kSwizzle32, g8, 256, 512, 16, 16);      // DFT-8
             is.stage_all<2>(1, x1, 13, 6144, 256, 128, 384, kNoSwizzle, g11, 512, 2048, 32, 32);  // DFT-11
             is.stage_all<2>(0, x0, 11, 8192, 32, 16, 512, kSwizzle64, g13, 512, 2048, 32, 32);    // DFT-13
+        };
+        if constexpr (CHAIN) {
+            // The issuer also feeds the chain, in its idle time between MMA
+            // stages (lane 0): the CTA's items as tickets (one taken ahead,
+            // its chunk prefetched to L2), each item's wait for its stage-A
+            // batch and the copy of its chunk into X0 once the last item's
+            // DFT-13 MMAs have retired, and the completion signal of the last
+            // item's bins once the epilogue has moved on.  Slot 14 + k % 2
+            // tells the epilogue the k-th item (-1: end).
+            auto ticket = [&]() -> int64_t {
+                const int64_t z = static_cast<int64_t>(atomicAdd(sc.ticket, 1u));
+                return z < a.n_items ? z : -1;
+            };
+            auto feed = [&](int64_t k, int64_t z) {
+                slots[14 + (k & 1)] = z;
+                if (z < 0) {
+                    mbar_arrive(&ctl.stg);
+                    return;
+                }
+                int64_t pol, loc;
+                const SegFwd &s = a.s[item_pos(z, pol, loc)];
+                const unsigned *d = sc.dep + s.dep0 + pol * (s.n / kChunks) + loc / kChunks;
+                if (!err_set(ctl) && !wait_count(d, static_cast<unsigned>(kBatchSnaps), ctl.lim)) raise_err(ctl);
+                fence_proxy_global();
+                bulk_g2s(X0, chunk_in(z), kNB * 2, &ctl.stg);
+            };
+            auto prefetch_l2 = [&](int64_t z) {
+                if (z >= 0)
+                    for (int i = 0; i < 5; ++i) l2_prefetch_piece(chunk_in(z), kNB * 2, i);
+            };
+            int64_t cur = -1, pend = -1, prev = -1;
+            if (lane == 0) {
+                cur = ticket();
+                feed(0, cur);
+                pend = cur >= 0 ? ticket() : -1;
+                prefetch_l2(pend);
+            }
+            cur = __shfl_sync(0xffffffffu, cur, 0);
+            uint32_t b13ph = 0;
+            for (int64_t k = 0;; ++k) {
+                if (cur < 0) {  // the epilogue's end mark follows its last item
+                    if (!err_set(ctl) && !mbar_wait(&ctl.ready[1], (is.rphase >> 1) & 1u, ctl.lim)) raise_err(ctl);
+                    is.rphase ^= 2u;
+                    if (lane == 0 && prev >= 0) bump(sc.done + prev);
+                    __syncwarp();
+                    break;
+                }
+                is.stage_all<2>(1, x1, 9, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);  // DFT-16
+                // the epilogue has finished the last item (its bins are written): signal them
+                if (lane == 0 && prev >= 0) bump(sc.done + prev);
+                rest();
+                commit_elect(&ctl.b13);
+                if (!err_set(ctl) && !mbar_wait(&ctl.b13, b13ph, ctl.lim)) raise_err(ctl);
+                b13ph ^= 1u;
+                int64_t nxt = -1;
+                if (lane == 0) {  // X0 is free: the next item's chunk
+                    nxt = pend;
+                    feed(k + 1, nxt);
+                    pend = nxt >= 0 ? ticket() : -1;
+                    prefetch_l2(pend);
+                }
+                __syncwarp();
+                prev = cur;
+                cur = __shfl_sync(0xffffffffu, nxt, 0);
+            }
+        } else {
+            for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+                is.stage_all<2>(1, x1, 9, 8192, 32, 16, 512, kSwizzle64, g16, 512, 2048, 32, 32);  // DFT-16
+                rest();
+            }
         }
         is.finish();
-    } else {
+    } else if (warp <= kEpiWarps) {
         Epi ep{&ctl, lane, (warp - 1) >> 2, warp & 3, (warp - 1) * 32 + lane,
                tb + (static_cast<uint32_t>((warp & 3) * 32) << 16)};
         const int e = warp - 1, q = ep.q, et = ep.et;
         const uint32_t *raw = reinterpret_cast<const uint32_t *>(X0);
         uint32_t *Z = reinterpret_cast<uint32_t *>(X1);
 
-        auto item_pos = [&](int64_t item, int64_t &pol, int64_t &loc) -> int {
-            const int si = seg_index(a, item);
-            const int64_t local = item - a.s[si].item0;
-            pol = local >= a.s[si].n ? 1 : 0;
-            loc = local - pol * a.s[si].n;
-            return si;
-        };
-        auto fetch = [&](int64_t item) {  // the item's 36608 FP16 samples -> X0 (73,216 bytes)
-            if (item >= a.n_items || et != 0) return;
-            int64_t pol, loc;
-            const SegFwd &s = a.s[item_pos(item, pol, loc)];
-            fence_async_smem();
-            bulk_g2s(X0, s.in + pol * s.in_pol_stride + loc * static_cast<int64_t>(kNB), kNB * 2, &ctl.stg);
-        };
         // input step: raw (natural order) -> DFT-16 operand.  A warp writes the
         // 512-byte row group of one nA' (rows 8 nA' + n8): lane = (n8, 16-byte
         // chunk c of n16 = 4c .. 4c + 3).  Its i-th gather takes n16 = 4c +
@@ -1131,17 +1394,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             }
         };
 
-        if (blockIdx.x < a.n_items) fetch(blockIdx.x);
-        for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-            ep.wait_staging();
-            // the CTA's next chunk to L2 (five pieces), so that its copy into X0
-            // after this chunk's DFT-13 reads L2, not HBM
-            if (et < 5 && item + gridDim.x < a.n_items) {
-                int64_t pn, ln;
-                const SegFwd &sn = a.s[item_pos(item + gridDim.x, pn, ln)];
-                l2_prefetch_piece(sn.in + pn * sn.in_pol_stride + ln * static_cast<int64_t>(kNB), kNB * 2, et);
-            }
+        // An item from its landed chunk to Z complete (after_input() runs
+        // between the input step and its publish), and then its R2C pairing.
+        auto front = [&](auto after_input) {
             input();
+            after_input();
             ep.publish_all(1);
             // B1: tiles 0-7 two per group, the ninth split by columns
             for (int j = ep.grp; j < 8; j += 4) {
@@ -1159,14 +1416,91 @@ __global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__
             ep.stage_group(11, 32, 2, [&](int j, uint32_t t) { epi4(j, t); });
             fence_before();
             named_sync_epi();  // Z complete; every DFT-13 MMA retired: X0 takes the next chunk
-            fetch(item + gridDim.x);
+        };
+        auto back = [&](int64_t item) {
             int64_t pol, loc;
             const SegFwd &s = a.s[item_pos(item, pol, loc)];
             pairing(s, pol, loc);
-            named_sync_epi();  // Z read: X1 takes the next input step
+            named_sync_epi();  // Z read: X1 takes the next input step; the bins are written
+        };
+
+        if constexpr (!CHAIN) {
+            // static order: CTA b takes items b, b + G, ...
+            auto fetch_static = [&](int64_t item) {  // the item's 36608 FP16 samples -> X0 (73,216 bytes)
+                if (item >= a.n_items || et != 0) return;
+                int64_t pol, loc;
+                const SegFwd &s = a.s[item_pos(item, pol, loc)];
+                fence_async_smem();
+                bulk_g2s(X0, s.in + pol * s.in_pol_stride + loc * static_cast<int64_t>(kNB), kNB * 2, &ctl.stg);
+            };
+            if (blockIdx.x < a.n_items) fetch_static(blockIdx.x);
+            for (int64_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+                ep.wait_staging();
+                // the CTA's next chunk to L2 (five pieces), so that its copy into
+                // X0 after this chunk's DFT-13 reads L2, not HBM
+                if (et < 5 && item + gridDim.x < a.n_items) l2_prefetch_piece(chunk_in(item + gridDim.x), kNB * 2, et);
+                front([] {});
+                fetch_static(item + gridDim.x);
+                back(item);
+            }
+        } else {
+            for (int64_t k = 0;; ++k) {
+                ep.wait_staging();
+                const int64_t item = slots[14 + (k & 1)];
+                if (item < 0) break;
+                front([] {});
+                back(item);
+            }
+            // end mark for the issuer
+            ep.publish_all(1);
         }
     }
-    teardown(ctl, a.status, warp);
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0 && err_set(ctl)) *reinterpret_cast<volatile int *>(a.status) = 1;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_tcf_fwd(const __grid_constant__ ArgsFwd a) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) tmem_alloc_cols(&g_tmem_base);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tb = g_tmem_base;
+    fwd_phase<false>(a, Sched{nullptr, nullptr, nullptr}, sm, tb);
+    if (warp == 0) tmem_free_cols(tb);
+}
+
+// Stages A, B and C of one wave in one persistent launch: every CTA runs the
+// stage-A loop, then stage B's, then stage C's, each on tickets of its stage
+// (q[0], q[1], q[2]); a stage-B item waits until its stage-A batch is
+// complete (q[3 + batch] = 143 snapshots), a stage-C item until its stage-B
+// item is (q[3 + n_batches + item] = 1).  q is zeroed before the launch.
+struct ChainArgs {
+    ArgsInv A;
+    ArgsFwd B;
+    ArgsInv C;
+    unsigned *q;
+    int64_t n_batches;
+};
+
+template <int OUTC>
+__global__ void __launch_bounds__(kInvThreads, 1) k_tcf_chain(const __grid_constant__ ChainArgs c) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *sm = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) tmem_alloc_cols(&g_tmem_base);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tb = g_tmem_base;
+    unsigned *dep_a = c.q + 3, *done_b = c.q + 3 + c.n_batches;
+    inv_phase<IN_PACKED, OUT_TS_HALF, 0, true>(c.A, Sched{c.q, nullptr, dep_a}, sm, tb);
+    fwd_phase<true>(c.B, Sched{c.q + 1, dep_a, done_b}, sm, tb);
+    inv_phase<IN_BINS, OUTC, 1, true>(c.C, Sched{c.q + 2, done_b, nullptr}, sm, tb);
+    if (warp == 0) tmem_free_cols(tb);
 }
 
 // Float time series -> FP16 x 2^-2 (sdbe_resample_chunks in this form).
@@ -1282,6 +1616,19 @@ cudaError_t launch_inv(const ArgsInv &args, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+template <int OUTC>
+cudaError_t launch_chain(const ChainArgs &args, cudaStream_t st) {
+    if (args.A.n_items <= 0) return cudaSuccess;
+    unsigned grid = 0;
+    cudaError_t e = grid_for(args.B.n_items, &grid);  // every CTA finds stage-B and stage-C work
+    constexpr uint32_t smem = inv_smem(true) > kFwdSmem ? inv_smem(true) : kFwdSmem;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tcf_chain<OUTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k_tcf_chain<OUTC><<<grid, kInvThreads, smem, st>>>(args);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fwd(const ArgsFwd &args, cudaStream_t st) {
     if (args.n_items <= 0) return cudaSuccess;
     unsigned grid = 0;
@@ -1296,6 +1643,7 @@ cudaError_t launch_fwd(const ArgsFwd &args, cudaStream_t st) {
 const uint8_t *blob_of(const sdbe_resampler *h) { return static_cast<const uint8_t *>(h->tcf_tabs); }
 
 constexpr uint64_t kWaitNs = 1000000000ull;  // 1 s: far above any legitimate wait
+constexpr bool kFusedByDefault = true;        // stage_launches 0: one launch per wave
 
 }  // namespace
 
@@ -1325,10 +1673,8 @@ int tcf_prepare(sdbe_resampler *h, cudaStream_t st) {
 // launch: per segment, snapshots [snap0, snap0 + n_snaps) of n_pols pols of
 // the packed spectra -> time series out + pol * out_pol_stride (elements),
 // [n_snaps][32768] per pol, FP16 x 2^-2 (half_out) or FP32.
-int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, bool half_out, cudaStream_t st) {
-    if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
-    if (int rc = tcf_prepare(h, st)) return rc;
-    ArgsInv A{};
+namespace {
+void build_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, ArgsInv &A) {
     for (int i = 0; i < n_segs; ++i) {
         const TcfASeg &g = segs[i];
         SegInv s{};
@@ -1346,6 +1692,14 @@ int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, 
     A.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
     A.status = h->tc_status;
     A.wait_ns = kWaitNs;
+}
+}  // namespace
+
+int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, bool half_out, cudaStream_t st) {
+    if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
+    if (int rc = tcf_prepare(h, st)) return rc;
+    ArgsInv A{};
+    build_a(h, segs, n_segs, n_pols, A);
     if (h->tc_test_timeout_ns > 0) {  // test hook: one withheld signal, short waits
         A.wait_ns = static_cast<uint64_t>(h->tc_test_timeout_ns);
         A.withhold = 1;
@@ -1360,11 +1714,8 @@ int tcf_stage_a(sdbe_resampler *h, const TcfASeg *segs, int n_segs, int n_pols, 
 // bins (scratch) -> the output `mode` asks for: 0 2-bit payload, 1 floats +
 // per-chunk (n, mean, M2), 3 2-bit payload + per-chunk (n, sum, sum of
 // squares), 5 floats.
-int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols, int mode, cudaStream_t st) {
-    if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
-    if (int rc = tcf_prepare(h, st)) return rc;
-    ArgsFwd B{};
-    ArgsInv C{};
+namespace {
+void build_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols, ArgsFwd &B, ArgsInv &C) {
     for (int i = 0; i < n_segs; ++i) {
         const TcfBCSeg &g = segs[i];
         B.s[B.n++] = SegFwd{static_cast<const __half *>(g.ts), g.bins, g.ts_pol_stride, g.bins_pol_stride, g.n_chunks,
@@ -1387,6 +1738,15 @@ int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols
     C.tab = reinterpret_cast<const float2 *>(blob_of(h) + kBlobInvTab);
     C.status = h->tc_status;
     C.wait_ns = kWaitNs;
+}
+}  // namespace
+
+int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols, int mode, cudaStream_t st) {
+    if (n_segs < 1 || n_segs > kMaxSegs) return fail(h, SDBE_ERR_ARG, "bad segment count");
+    if (int rc = tcf_prepare(h, st)) return rc;
+    ArgsFwd B{};
+    ArgsInv C{};
+    build_bc(h, segs, n_segs, n_pols, B, C);
     SDBE_CK(h, launch_fwd(B, st));
     switch (mode) {
         case 0: SDBE_CK(h, (launch_inv<IN_BINS, OUT_QUANT>(C, st))); break;
@@ -1397,10 +1757,18 @@ int tcf_stage_bc(sdbe_resampler *h, const TcfBCSeg *segs, int n_segs, int n_pols
     return SDBE_OK;
 }
 
+// Whether a wave's three stages run as one persistent launch (the handle's
+// stage_launches; the time-out test hook needs the separate launches).
+bool tcf_fused(const sdbe_resampler *h) {
+    if (h->tc_test_timeout_ns > 0) return false;
+    return h->cfg.stage_launches == SDBE_STAGES_FUSED ||
+           (h->cfg.stage_launches == 0 && kFusedByDefault);
+}
+
 // One wave of the fast tensor-core chain over several handles (one stream
 // pair each): stage A of every handle's batches in one launch (FP16 time
 // series into the handle's stage-A scratch), then stages B and C in one launch
-// each, writing the payloads.  With `first` each item is its handle's first
+// each, writing the payloads; or all three stages in one persistent launch.  With `first` each item is its handle's first
 // batch: stage C writes floats and FP64 moments, the thresholds are set from
 // them, then the floats are packed, as the FP32 path does.
 int tcf_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st) {
@@ -1451,6 +1819,22 @@ int tcf_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st
     }
     const int n = static_cast<int>(w.size());
     size_t slot = 0;
+    if (!first && tcf_fused(h0)) {
+        // stages A, B and C in one persistent launch (k_tcf_chain), on tickets
+        ChainArgs c{};
+        build_a(h0, sa.data(), n, 2, c.A);
+        build_bc(h0, sb.data(), n, 2, c.B, c.C);
+        for (int i = 0; i < c.B.n; ++i) c.B.s[i].dep0 = c.A.s[i].item0 / kBatchSnaps;
+        c.n_batches = c.A.n_items / kBatchSnaps;
+        const int64_t words = 3 + c.n_batches + c.B.n_items;
+        if (int rc = grow(h0, &h0->tcf_chain, &h0->tcf_chain_bytes, words * 4, "the stage-chain counters")) return rc;
+        c.q = reinterpret_cast<unsigned *>(h0->tcf_chain);
+        SDBE_CK(h0, cudaMemsetAsync(c.q, 0, static_cast<size_t>(words) * 4, st));
+        SDBE_CK(h0, timed_begin(h0, 2, units_bc, st, &slot));
+        SDBE_CK(h0, (any_win ? launch_chain<OUT_QUANT_SUMS>(c, st) : launch_chain<OUT_QUANT>(c, st)));
+        SDBE_CK(h0, timed_end(h0, slot, st));
+        h0->launches -= 2;  // one launch instead of three (counted below)
+    } else {
     if (!first) SDBE_CK(h0, timed_begin(h0, 0, units_a, st, &slot));
     if (int rc = tcf_stage_a(h0, sa.data(), n, 2, true, st)) return rc;
     if (!first) {
@@ -1458,6 +1842,7 @@ int tcf_wave_multi(const std::vector<TcWaveItem> &w, bool first, cudaStream_t st
         SDBE_CK(h0, timed_begin(h0, 1, units_bc, st, &slot));
     }
     if (int rc = tcf_stage_bc(h0, sb.data(), n, 2, first ? 1 : (any_win ? 3 : 0), st)) return rc;
+    }
     WinUpds U{};
     for (const auto &it : w) {
         sdbe_resampler *h = it.h;

@@ -65,7 +65,7 @@ class Resampler:
     def __init__(self, trim_mhz: int = 150, device: int = 0, max_frames: int = 143,
                  threshold_mode: int = N.THRESH_FIRST_BATCH, pol1_uses_pol0_threshold: bool = False,
                  channel_map: int = N.MAP_APHIDS, wave_batches: int = 0, threshold_window: int = 0,
-                 precision: int = N.PRECISION_FP32):
+                 precision: int = N.PRECISION_FP32, stage_launches: int = 0):
         self._lib = N.lib()
         cfg = N.Config()
         cfg.device = device
@@ -77,6 +77,7 @@ class Resampler:
         cfg.wave_batches = wave_batches
         cfg.threshold_window = threshold_window
         cfg.precision = precision
+        cfg.stage_launches = stage_launches
         h = C.c_void_p()
         N.check(self._lib.sdbe_create(C.byref(cfg), C.byref(h)))
         self._h = h
