@@ -85,6 +85,7 @@ void free_all(sdbe_resampler *h) {
     cudaFree(h->tcf_bins);
     cudaFree(h->tcf_half);
     cudaFree(h->tcf_chain);
+    cudaFree(h->pol_scr);
     if (h->tc_status_host) cudaFreeHost(h->tc_status_host);
     cudaFree(h->left[0]);
     cudaFree(h->left[1]);

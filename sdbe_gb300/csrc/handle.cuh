@@ -69,6 +69,8 @@ struct sdbe_resampler {
     int64_t ipfb_y_bytes = 0;
     uint8_t *ipfb_scr = nullptr;  // factors [nblock][ntap][32768] f64
     int64_t ipfb_scr_bytes = 0;
+    uint8_t *pol_scr = nullptr;   // group assembly on the device: state, result, bins, codes
+    int64_t pol_scr_bytes = 0;
     int64_t b_first = -1;
     int64_t ing_ref = 0;
     int64_t g_count[4] = {0, 0, 0, 0};
@@ -183,6 +185,29 @@ inline int window_after_wave(sdbe_resampler *h, const double *partials, int64_t 
     h->launches += 1;
     return SDBE_OK;
 }
+
+// Group assembly state (the ingest policy of vdif_in_databuf.c:96-167) as the
+// device walk reads and writes it: the first b-count, the oldest open group,
+// packets per ring slot and per slot and frame, and the statistics (packets,
+// invalid, before_start, too_far_ahead, used, overflow, groups_shipped,
+// groups_incomplete).
+struct PolState {
+    long long b_first, ref;
+    long long count[4];
+    long long st[8];
+    int fcount[4 * 143];
+};
+constexpr int kPolWindow = 16384;    // B-frames a batch may span from the oldest open group
+constexpr int kPolMaxGroups = 128;   // groups shipped or touched by one batch (bounded by the window)
+struct PolOut {
+    PolState s;                      // the state after the batch
+    long long base;                  // b-count of the window's first frame (-1: no valid packet yet)
+    int n_ships, n_touched, n_capped, window_exceeded;
+    long long ships[kPolMaxGroups], touched[kPolMaxGroups];
+};
+// The policy on the device for a batch (k_policy.cu): header words (w0, w4,
+// w5) of n packets at hdr -> accept[n] on the device, the result in res.
+int policy_device(sdbe_resampler *h, const uint32_t *hdr, int64_t n, uint8_t *accept, PolOut *res, cudaStream_t st);
 
 // The FFT chain of sdbe_process on a tensor-core handle (k_tc.cu): same
 // arguments as fft_chain (on_wave(lo, hi) after the wave that completes

@@ -1,7 +1,9 @@
 // Group assembly for packets as received: the ingest thread's windowing,
 // limits and flush policy (software/aphids/vdif_in_net_thread.c:255-500,
-// vdif_in_databuf.c:96-167) decided on the host from the packet headers, the
-// scatter, zero fill and resampling of every shipped group on the device.
+// vdif_in_databuf.c:96-167) decided on the device from the packet headers
+// (k_policy.cu), then the scatter, zero fill and resampling of every shipped
+// group.  The host keeps the ring's life cycle: it reads the batch's result
+// (ships, touched groups, the state after the batch) and launches the work.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,93 +59,17 @@ void ship(Policy &p, std::vector<int64_t> &ships) {
     p.ref += 1;
 }
 
-// Header words w0, w4, w5 of packet i: at base + i*stride, offsets 0, o4, o5
-// (host packets, or the [n][3] words read back from the device).
-struct HdrView {
-    const uint8_t *base;
-    int64_t stride;
-    int o4, o5;
-    uint32_t word(int64_t i, int off) const {
-        uint32_t v;
-        std::memcpy(&v, base + i * stride + off, sizeof(v));
-        return v;
-    }
-};
-
-// One received batch through the policy: accept[i] for packet i, the groups
-// that ship in order, and the groups that received packets.
-void run_policy(Policy &p, const HdrView &hv, int64_t n, std::vector<uint8_t> &accept, std::vector<int64_t> &ships,
-                std::vector<int64_t> &touched) {
-    std::vector<int64_t> key(n);
-    std::vector<uint8_t> inval(n);
-    for (int64_t i = 0; i < n; ++i) {
-        const uint32_t w0 = hv.word(i, 0), w4 = hv.word(i, hv.o4), w5 = hv.word(i, hv.o5);
-        inval[i] = static_cast<uint8_t>(w0 >> 31);
-        const int64_t b = static_cast<int64_t>((static_cast<uint64_t>(w4) << 8) | (w5 >> 24));
-        key[i] = inval[i] ? INT64_MIN : b;  // compar_beng: invalid first, then by b
-    }
-    std::vector<int64_t> order(n);
-    std::iota(order.begin(), order.end(), int64_t{0});
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
-    accept.assign(n, 0);
-    p.st.packets += n;
-    if (p.b_first < 0) {
-        int64_t k = 0;
-        while (k < n && inval[order[k]]) ++k;
-        if (k == n) {
-            p.st.invalid += n;
-            return;
-        }
-        p.b_first = key[order[k]];
-        p.ref = 0;
-    }
-    for (int64_t k = 0; k < n; ++k) {
-        const int64_t i = order[k];
-        const int64_t b = key[i];
-        while (true) {
-            if (inval[i]) {
-                p.st.invalid += 1;
-                break;
-            }
-            const int64_t lo = group_start(p, p.ref);
-            if (b < lo) {
-                p.st.before_start += 1;
-                break;
-            }
-            int64_t off = (b - lo) / kGroupFrames;
-            if (off >= kRing) {
-                // vdif_in_databuf.c:107-120: the search ends with its upper
-                // bound at the last frame of the group after the four it checked
-                const int64_t lu_last = group_start(p, p.ref + kRing + 1) - 1;
-                if (b > lu_last + int64_t(kRing) * kGroupFrames) {
-                    p.st.too_far_ahead += 1;
-                    break;
-                }
-                off = kRing;
-            }
-            if (off > kLookAhead) {  // force the oldest group out, look again
-                ship(p, ships);
-                continue;
-            }
-            const int64_t g = p.ref + off;
-            const int s = static_cast<int>(g % kRing);
-            const int64_t frame = b - group_start(p, g);
-            p.st.used += 1;
-            int32_t &fc = p.fcount[s * kGroupFrames + frame];
-            if (fc < kPktsPerFrame && p.count[s] < kGroupPackets) {
-                fc += 1;
-                p.count[s] += 1;
-                accept[i] = 1;
-                if (touched.empty() || touched.back() != g) touched.push_back(g);
-            } else {
-                p.st.overflow += 1;
-            }
-            if (p.count[p.ref % kRing] == kGroupPackets) ship(p, ships);
-            break;
-        }
-    }
-    std::sort(touched.begin(), touched.end());
-    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+// The state after a batch from the device walk.
+Policy after_batch(const sdbe_resampler *h, const PolOut &r) {
+    Policy p = snapshot(h);
+    p.b_first = r.s.b_first;
+    p.ref = r.s.ref;
+    for (int i = 0; i < kRing; ++i) p.count[i] = r.s.count[i];
+    p.fcount.assign(r.s.fcount, r.s.fcount + kRing * kGroupFrames);
+    int64_t *st[8] = {&p.st.packets, &p.st.invalid, &p.st.before_start, &p.st.too_far_ahead, &p.st.used,
+                      &p.st.overflow, &p.st.groups_shipped, &p.st.groups_incomplete};
+    for (int i = 0; i < 8; ++i) *st[i] = r.s.st[i];
+    return p;
 }
 
 int ensure_ring(sdbe_resampler *h) {
@@ -253,14 +179,14 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
     const int64_t n_pk = pac8 ? 8 * n_packets : n_packets;
     const uint8_t *dev_pkts = nullptr;
     sdbe_reform_state reform = h->reform;
-    std::vector<uint32_t> hdr;
-    HdrView hv{static_cast<const uint8_t *>(packets), kPktBytes, 16, 20};
     int rc = SDBE_OK;
-    if ((pac8 || !in_host) && n_pk > 0) {
-        // The policy reads the headers on the host: produce them on the device
-        // (after the 8pac unpack and header reform) and read back 12 B a packet.
+    uint32_t *hdr = nullptr;
+    if (n_pk > 0) {
+        // the policy reads the header words on the device: after the 8pac unpack
+        // and header reform, or gathered from the packets
         rc = grow(h, &h->ing_hdr, &h->ing_hdr_bytes, n_pk * 12, "ingest header words");
         if (rc) return rc;
+        hdr = reinterpret_cast<uint32_t *>(h->ing_hdr);
         if (pac8) {
             const void *src = packets;
             if (in_host) {
@@ -273,26 +199,29 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
             if (rc) return rc;
             if (!h->reform_dev) SDBE_CK(h, cudaMalloc(&h->reform_dev, sizeof(sdbe_reform_state)));
             SDBE_CK(h, launch_unpack_8pac(src, n_packets, h->ing_batch, st));
-            SDBE_CK(h, launch_beng_reform(h->ing_batch, n_pk, h->reform, h->reform_dev,
-                                          reinterpret_cast<uint32_t *>(h->ing_hdr), st));
+            SDBE_CK(h, launch_beng_reform(h->ing_batch, n_pk, h->reform, h->reform_dev, hdr, st));
             SDBE_CK(h, cudaMemcpyAsync(&reform, h->reform_dev, sizeof(reform), cudaMemcpyDeviceToHost, st));
             h->launches += 2;
             dev_pkts = h->ing_batch;
         } else {
-            SDBE_CK(h, launch_gather_headers(packets, n_pk, reinterpret_cast<uint32_t *>(h->ing_hdr), st));
+            if (in_host) {
+                rc = grow(h, &h->ing_batch, &h->ing_batch_bytes, n_pk * kPktBytes, "ingest batch");
+                if (rc) return rc;
+                SDBE_CK(h, cudaMemcpyAsync(h->ing_batch, packets, n_pk * kPktBytes, cudaMemcpyHostToDevice, st));
+                dev_pkts = h->ing_batch;
+            } else {
+                dev_pkts = static_cast<const uint8_t *>(packets);
+            }
+            SDBE_CK(h, launch_gather_headers(dev_pkts, n_pk, hdr, st));
             h->launches += 1;
-            dev_pkts = static_cast<const uint8_t *>(packets);
         }
-        hdr.resize(static_cast<size_t>(n_pk) * 3);
-        SDBE_CK(h, cudaMemcpyAsync(hdr.data(), h->ing_hdr, n_pk * 12, cudaMemcpyDeviceToHost, st));
-        SDBE_CK(h, cudaStreamSynchronize(st));
-        hv = HdrView{reinterpret_cast<const uint8_t *>(hdr.data()), 12, 4, 8};
+        rc = grow(h, &h->ing_accept, &h->ing_accept_bytes, n_pk, "ingest mask");
+        if (rc) return rc;
     }
-    Policy p = snapshot(h);
-    std::vector<uint8_t> accept;
-    std::vector<int64_t> ships, touched;
-    run_policy(p, hv, n_pk, accept, ships, touched);
-    const int64_t n_ships = static_cast<int64_t>(ships.size());
+    PolOut res;
+    rc = policy_device(h, hdr, n_pk, h->ing_accept, &res, st);  // waits for the stream
+    if (rc) return rc;
+    const int64_t n_ships = res.n_ships;
     if (n_ships > out_groups) {
         if (n_groups) *n_groups = static_cast<int32_t>(n_ships);
         return fail(h, SDBE_ERR_CAPACITY, "output has room for fewer groups than ship");
@@ -300,17 +229,8 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
     if (n_ships > 0 && !out) return fail(h, SDBE_ERR_ARG, "null output");
     rc = ensure_ring(h);
     if (rc) return rc;
-    if (n_pk > 0) {
-        if (!dev_pkts) {  // plain host packets
-            rc = grow(h, &h->ing_batch, &h->ing_batch_bytes, n_pk * kPktBytes, "ingest batch");
-            if (rc) return rc;
-            SDBE_CK(h, cudaMemcpyAsync(h->ing_batch, packets, n_pk * kPktBytes, cudaMemcpyHostToDevice, st));
-            dev_pkts = h->ing_batch;
-        }
-        rc = grow(h, &h->ing_accept, &h->ing_accept_bytes, n_pk, "ingest mask");
-        if (rc) return rc;
-        SDBE_CK(h, cudaMemcpyAsync(h->ing_accept, accept.data(), n_pk, cudaMemcpyHostToDevice, st));
-    }
+    const Policy p = after_batch(h, res);
+    const std::vector<int64_t> ships(res.ships, res.ships + n_ships), touched(res.touched, res.touched + res.n_touched);
     uint8_t *dev_out = out_target(h, out, n_ships, flags, &rc);
     if (rc) return rc;
     rc = run_device(h, p, dev_pkts, n_pk, h->ing_accept, ships, touched, dev_out, flags, st);

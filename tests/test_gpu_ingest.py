@@ -174,3 +174,47 @@ def test_ingest_rejects_mar2015_map(S):
         with pytest.raises(N.SdbeError) as e:
             rs.ingest(p)
         assert e.value.code == N.ERR_STATE
+
+
+@pytest.mark.parametrize("case", ["sparse", "overflow", "boundary", "far", "complete"])
+def test_device_policy_on_reference_scenarios(S, case):
+    """The group assembly decisions, made on the device, over the seeded
+    ingest scenarios whose per-packet outcomes and ships the reference's own
+    C code recorded (tests/golden/hostlogic.npz, through the oracle it pins):
+    invalid, early, late and too-far packets, frames over 2048 packets (the
+    first ones in arrival order kept), look-ahead and completion ships.  After
+    every batch the statistics and the shipped groups equal the oracle's, and
+    each shipped group equals sdbe_process over the packets the oracle let
+    into it (random payloads, so that a different choice among duplicates
+    shows)."""
+    import os
+    import sys
+
+    from sdbe_gb300 import Resampler
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_hostlogic_golden as HG
+
+    hdr, cuts = HG.scenario(case)
+    rng = np.random.default_rng(sum(map(ord, case)))
+    pk = np.concatenate([hdr, rng.integers(0, 256, (hdr.shape[0], O.IN_PKT_BYTES - 32), dtype=np.uint8)], axis=1)
+    st = O.IngestState()
+    accepted = {}
+    with Resampler(max_frames=G) as rs, Resampler(max_frames=G) as ref:
+        pos = 0
+        for m in cuts:
+            batch = pk[pos:pos + m]
+            pos += m
+            acc, ships = O.ingest_policy(batch, st)
+            got = batch[acc]
+            gid = (_b_of(got) - st.b_first - 1) // G
+            for g in np.unique(gid):
+                prev = accepted.get(int(g))
+                new = got[gid == g]
+                accepted[int(g)] = new if prev is None else np.concatenate([prev, new])
+            groups, n = rs.ingest(batch)
+            assert n == len(ships), (case, pos)
+            for i, g in enumerate(ships):
+                want, _ = ref.process(accepted.pop(g, np.zeros((0, O.IN_PKT_BYTES), np.uint8)), G, st.start(g))
+                assert np.array_equal(groups[i], want), (case, g)
+            _stats_equal(rs, st)
