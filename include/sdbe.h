@@ -453,6 +453,13 @@ int sdbe_fp32_fma_rate(int32_t device, double *tflops, double *ms);
  * by the tests of the failure path; limit_ns must be in [1e3, 1e9]. */
 int sdbe_test_tc_timeout(sdbe_resampler *h, int64_t limit_ns);
 
+/* ---- test hook: group assembly decisions (no counterpart in the reference) */
+/* Copies to host memory the accept flag (1: inserted into a group) that the
+ * device policy gave each packet of the last sdbe_ingest batch of h, in
+ * arrival order (for 8pac input, of the 8 n unpacked packets).  n must equal
+ * that batch's packet count.  Used by the tests of the group assembly. */
+int sdbe_test_ingest_accept(const sdbe_resampler *h, uint8_t *mask, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -132,6 +132,7 @@ SIGNATURES = {
     "sdbe_reorder_mar2015": (C.c_int, [vp, i32, vp, vp]),
     "sdbe_fp32_fma_rate": (C.c_int, [i32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "sdbe_test_tc_timeout": (C.c_int, [vp, i64]),
+    "sdbe_test_ingest_accept": (C.c_int, [vp, vp, i64]),
 }
 
 SYNTH_SIGNATURES = {

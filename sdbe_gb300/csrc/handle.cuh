@@ -71,6 +71,7 @@ struct sdbe_resampler {
     int64_t ipfb_scr_bytes = 0;
     uint8_t *pol_scr = nullptr;   // group assembly on the device: state, result, bins, codes
     int64_t pol_scr_bytes = 0;
+    int64_t ing_last_n = 0;       // packets of the last sdbe_ingest batch (their flags in ing_accept)
     int64_t b_first = -1;
     int64_t ing_ref = 0;
     int64_t g_count[4] = {0, 0, 0, 0};

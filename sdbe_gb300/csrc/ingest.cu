@@ -221,6 +221,7 @@ int sdbe_ingest(sdbe_resampler *h, const void *packets, int64_t n_packets, void 
     PolOut res;
     rc = policy_device(h, hdr, n_pk, h->ing_accept, &res, st);  // waits for the stream
     if (rc) return rc;
+    h->ing_last_n = n_pk;
     const int64_t n_ships = res.n_ships;
     if (n_ships > out_groups) {
         if (n_groups) *n_groups = static_cast<int32_t>(n_ships);
@@ -272,6 +273,17 @@ int sdbe_ingest_flush(sdbe_resampler *h, void *out, int64_t out_groups, uint32_t
 int sdbe_ingest_reform_state(const sdbe_resampler *h, sdbe_reform_state *st) {
     if (!h || !st) return SDBE_ERR_ARG;
     *st = h->reform;
+    return SDBE_OK;
+}
+
+int sdbe_test_ingest_accept(const sdbe_resampler *h, uint8_t *mask, int64_t n) {
+    if (!h || n < 0 || (n > 0 && !mask)) return SDBE_ERR_ARG;
+    if (n != h->ing_last_n) return fail(const_cast<sdbe_resampler *>(h), SDBE_ERR_ARG, "n is not the last batch's size");
+    if (n == 0) return SDBE_OK;
+    DeviceGuard g(h->cfg.device);
+    if (!g.ok) return SDBE_ERR_CUDA;
+    if (cudaMemcpy(mask, h->ing_accept, static_cast<size_t>(n), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(const_cast<sdbe_resampler *>(h), SDBE_ERR_CUDA, "copy of the accept flags failed");
     return SDBE_OK;
 }
 

@@ -183,10 +183,11 @@ def test_device_policy_on_reference_scenarios(S, case):
     C code recorded (tests/golden/hostlogic.npz, through the oracle it pins):
     invalid, early, late and too-far packets, frames over 2048 packets (the
     first ones in arrival order kept), look-ahead and completion ships.  After
-    every batch the statistics and the shipped groups equal the oracle's, and
-    each shipped group equals sdbe_process over the packets the oracle let
-    into it (random payloads, so that a different choice among duplicates
-    shows)."""
+    every batch the device's accept flag of every packet, the statistics and
+    the shipped groups equal the oracle's, and each shipped group equals
+    sdbe_process over the packets the oracle let into it.  A packet's payload
+    is a function of its (b, c, f) slot, so duplicates carry the same data
+    and the groups do not depend on which duplicate a frame keeps."""
     import os
     import sys
 
@@ -196,8 +197,10 @@ def test_device_policy_on_reference_scenarios(S, case):
     import make_hostlogic_golden as HG
 
     hdr, cuts = HG.scenario(case)
-    rng = np.random.default_rng(sum(map(ord, case)))
-    pk = np.concatenate([hdr, rng.integers(0, 256, (hdr.shape[0], O.IN_PKT_BYTES - 32), dtype=np.uint8)], axis=1)
+    w = np.ascontiguousarray(hdr).view("<u4")
+    slot = (_b_of(hdr) * 2048 + (w[:, 5] & 0xFF) * 8 + ((w[:, 5] >> 16) & 7)).astype(np.int64)
+    payload = ((slot[:, None] * 2654435761 + np.arange(O.IN_PKT_BYTES - 32)[None, :] * 40503) >> 7) & 0xFF
+    pk = np.concatenate([hdr, payload.astype(np.uint8)], axis=1)
     st = O.IngestState()
     accepted = {}
     with Resampler(max_frames=G) as rs, Resampler(max_frames=G) as ref:
@@ -213,6 +216,10 @@ def test_device_policy_on_reference_scenarios(S, case):
                 new = got[gid == g]
                 accepted[int(g)] = new if prev is None else np.concatenate([prev, new])
             groups, n = rs.ingest(batch)
+            mask = np.zeros(m, np.uint8)
+            assert rs._lib.sdbe_test_ingest_accept(rs.handle, mask.ctypes.data, m) == 0
+            bad = np.flatnonzero(mask.astype(bool) != acc)
+            assert bad.size == 0, (case, pos, bad[:10])
             assert n == len(ships), (case, pos)
             for i, g in enumerate(ships):
                 want, _ = ref.process(accepted.pop(g, np.zeros((0, O.IN_PKT_BYTES), np.uint8)), G, st.start(g))
