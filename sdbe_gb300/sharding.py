@@ -28,3 +28,21 @@ def allgather_counts(n: int):
     out = [torch.zeros_like(t) for _ in range(dist.get_world_size())]
     dist.all_gather(out, t)
     return [int(x.item()) for x in out]
+
+
+def process_shard(streams, run, rank: int, world: int):
+    """Run ``run(index, stream)`` on this rank's streams (round-robin) and
+    gather the results of every rank: returns ``{index: result}`` for all
+    streams on every rank (results must be picklable, e.g. digests of the
+    payloads).  Without torch.distributed (world 1) it is a plain loop."""
+    import torch.distributed as dist
+
+    mine = {i: run(i, s) for i, s in enumerate(streams) if i % world == rank}
+    if not (dist.is_available() and dist.is_initialized()) or world == 1:
+        return mine
+    parts = [None] * world
+    dist.all_gather_object(parts, mine)
+    out = {}
+    for p in parts:
+        out.update(p)
+    return out

@@ -122,6 +122,58 @@ def test_streams_shard_over_ranks_gloo(tmp_path):
     assert sorted(list(r0[2:]) + list(r1[2:])) == list(range(7))
 
 
+def _digest_worker(rank, world, port, out_dir):
+    import hashlib
+
+    import torch.distributed as dist
+
+    from oracle import sdbe_oracle as O
+    from sdbe_gb300 import sharding, synth
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    specs = [synth.config1(stream=i) for i in range(5)]
+    for sp in specs:
+        sp.n_frames = 2
+
+    def run(i, sp):  # the stage's CPU restatement on this rank's stream
+        out = O.process_group(synth.generate(sp), sp.b_start, sp.n_frames, 150)
+        return hashlib.sha256(out.tobytes()).hexdigest()
+
+    got = sharding.process_shard(specs, run, rank, world)
+    np.save(os.path.join(out_dir, f"d{rank}.npy"), np.array([f"{k}:{v}" for k, v in sorted(got.items())]))
+    dist.destroy_process_group()
+
+
+def test_shard_results_equal_single_process_gloo(tmp_path, synth):
+    """Two ranks over gloo each process their round-robin share of five
+    streams and gather the digests of their outputs: every rank holds all
+    five, equal to one process running them all."""
+    import hashlib
+    import socket
+
+    import torch.multiprocessing as mp
+
+    from sdbe_gb300 import sharding
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    mp.spawn(_digest_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    d0, d1 = np.load(tmp_path / "d0.npy"), np.load(tmp_path / "d1.npy")
+    specs = [synth.config1(stream=i) for i in range(5)]
+    for sp in specs:
+        sp.n_frames = 2
+    single = sharding.process_shard(
+        specs, lambda i, sp: hashlib.sha256(O.process_group(synth.generate(sp), sp.b_start, 2, 150).tobytes()).hexdigest(),
+        0, 1)
+    want = np.array([f"{k}:{v}" for k, v in sorted(single.items())])
+    assert len(want) == 5
+    assert np.array_equal(d0, want) and np.array_equal(d1, want)
+
+
 def test_oracle_mar2015_stream_split_equals_single(synth):
     """Mar-2015 mode holds one frame back; splitting the stream changes nothing."""
     spec = synth.config1()
