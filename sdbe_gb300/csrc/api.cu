@@ -265,7 +265,10 @@ int ship_call(CallPlan &c, int64_t lo, int64_t hi) {
     return SDBE_OK;
 }
 
-int prepare_call(CallPlan &c) {
+// With `batch` (sdbe_process_multi, APHIDS map) the call's unpack and zero
+// fill join the batch's launches, which the caller makes after every call is
+// prepared (and records the staging slots' pkt_free after them).
+int prepare_call(CallPlan &c, UnpackSegs *batch = nullptr) {
     sdbe_resampler *h = c.h;
     cudaStream_t st = c.st;
     c.sg = &h->stage[h->stage_idx];
@@ -309,11 +312,17 @@ int prepare_call(CallPlan &c) {
         const int64_t snap0 = mar ? static_cast<int64_t>(h->raw_carry) * kSnapsPerFrame : h->carry;
         SDBE_CK(h, cudaMemsetAsync(h->bitmap, 0, static_cast<size_t>(n_frames) * 256, st));
         SDBE_CK(h, cudaMemsetAsync(h->counts, 0, (static_cast<size_t>(h->cfg.max_frames) + 1) * sizeof(int32_t), st));
-        SDBE_CK(h, launch_unpack(src, c.n_packets, c.b_zero, n_frames, map, dst, dst_stride, snap0, h->bitmap, h->counts,
-                                 h->counts + h->cfg.max_frames, st));
-        if (c.host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
-        SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, dst, dst_stride, snap0, st));
-        h->launches += c.n_packets > 0 ? 2 : 1;
+        if (batch && !mar) {
+            unpack_segs_add(*batch, UnpackSeg{static_cast<const uint8_t *>(src), c.n_packets, c.b_zero, n_frames, map,
+                                              dst, dst_stride, snap0, h->bitmap, h->counts,
+                                              h->counts + h->cfg.max_frames, nullptr, 0, 0});
+        } else {
+            SDBE_CK(h, launch_unpack(src, c.n_packets, c.b_zero, n_frames, map, dst, dst_stride, snap0, h->bitmap,
+                                     h->counts, h->counts + h->cfg.max_frames, st));
+            if (c.host_in) SDBE_CK(h, cudaEventRecord(sg.pkt_free, st));
+            SDBE_CK(h, launch_fill_missing(h->bitmap, n_frames, map, dst, dst_stride, snap0, st));
+            h->launches += c.n_packets > 0 ? 2 : 1;
+        }
         if (mar) {
             const int n_in = h->raw_carry + n_frames;
             for (int pol = 0; pol < 2 && n_in >= 2; ++pol) {
@@ -706,8 +715,18 @@ int sdbe_process_multi(sdbe_resampler *const *hs, const sdbe_stream_desc *d, int
                            flags, st, c[i]);
         if (rc) return rc;
     }
+    // every stream's unpack and zero fill in one launch each
+    UnpackSegs U{};
     for (auto &ci : c)
-        if (int rc = prepare_call(ci)) return rc;
+        if (int rc = prepare_call(ci, &U)) return rc;
+    if (U.n > 0) {
+        SDBE_CK(hs[0], launch_unpack_segs(U, st));
+        for (auto &ci : c)
+            if (ci.host_in && ci.n_frames > 0 && ci.h->cfg.channel_map != SDBE_MAP_MAR2015)
+                SDBE_CK(ci.h, cudaEventRecord(ci.sg->pkt_free, st));
+        SDBE_CK(hs[0], launch_fill_missing_segs(U, st));
+        hs[0]->launches += U.blocks > 0 ? 2 : 1;
+    }
     if (int rc = fft_chain_multi(c)) return rc;
     for (int i = 0; i < n; ++i)
         if (int rc = complete_call(c[i], results ? results + i : nullptr)) return rc;

@@ -7,6 +7,7 @@
 // the second = channels 7,6,5,4; in each byte bits 0-1/2-3 are pol-1
 // imag/real and bits 4-5/6-7 pol-0 imag/real (.cu:464-495).
 #include "fft_core.cuh"
+#include "launchers.cuh"
 #include "sdbe_internal.cuh"
 
 namespace sdbe {
@@ -60,20 +61,33 @@ constexpr int kTilePkts = 32;
 // Phase 2: lanes = packets, so each store instruction writes the 32 packets'
 // channel groups of one snapshot row (128 contiguous bytes for in-order
 // packets).
-__global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict__ pkts, int64_t n_pkts,
-                                                       uint64_t b_zero, int n_frames, int map,
-                                                       uint32_t *__restrict__ spec, int64_t pol_stride,
-                                                       int64_t snap0, uint32_t *__restrict__ bitmap,
-                                                       int32_t *__restrict__ counts,
-                                                       int32_t *__restrict__ rejected,
-                                                       const uint8_t *__restrict__ accept) {
+// Segment of a unpack launch that serves several calls (one per stream
+// pair): its blocks start at block blk0 of the grid.
+__device__ __forceinline__ const UnpackSeg &unpack_seg(const UnpackSegs &S, int64_t blk) {
+    int j = 0;
+    while (j + 1 < S.n && blk >= S.s[j + 1].blk0) ++j;
+    return S.s[j];
+}
+
+__global__ void __launch_bounds__(256) k_unpack_packed(const __grid_constant__ UnpackSegs S) {
+    const UnpackSeg &G = unpack_seg(S, blockIdx.x);
+    const uint8_t *__restrict__ pkts = G.pkts;
+    const int64_t n_pkts = G.n_pkts;
+    const uint64_t b_zero = G.b_zero;
+    const int n_frames = G.n_frames, map = G.map;
+    uint32_t *__restrict__ spec = G.spec;
+    const int64_t pol_stride = G.pol_stride, snap0 = G.snap0;
+    uint32_t *__restrict__ bitmap = G.bitmap;
+    int32_t *__restrict__ counts = G.counts;
+    int32_t *__restrict__ rejected = G.rejected;
+    const uint8_t *__restrict__ accept = G.accept;
     __shared__ uint4 tile[2][kTilePkts][32];
     __shared__ int64_t s_row[kTilePkts];
     __shared__ int s_group[kTilePkts];
     __shared__ int s_frame[kTilePkts];  // -1 not taken, -2 no packet
     __shared__ uint32_t s_cf[kTilePkts];  // c | f << 8
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t p_base = static_cast<int64_t>(blockIdx.x) * kTilePkts;
+    const int64_t p_base = (static_cast<int64_t>(blockIdx.x) - G.blk0) * kTilePkts;
 
     uint32_t w0[4], w4[4], w5[4];
     uint4 a[4], b[4];
@@ -164,9 +178,16 @@ __global__ void __launch_bounds__(256) k_unpack_packed(const uint8_t *__restrict
 // Missing packets read as zero (the reference pre-zeroes its buffers,
 // .cu:897-898): every (frame, c, f) slot whose completion bit is unset gets
 // code 2/2 in all 128 snapshots of both pols.
-__global__ void k_fill_missing(const uint32_t *__restrict__ bitmap, int n_frames, int map,
-                               uint32_t *__restrict__ spec, int64_t pol_stride, int64_t snap0) {
-    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+__global__ void k_fill_missing(const __grid_constant__ UnpackSegs S) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int j = 0;
+    while (j + 1 < S.n && t >= S.s[j + 1].fill0) ++j;
+    const UnpackSeg &G = S.s[j];
+    const uint32_t *__restrict__ bitmap = G.bitmap;
+    const int n_frames = G.n_frames, map = G.map;
+    uint32_t *__restrict__ spec = G.spec;
+    const int64_t pol_stride = G.pol_stride, snap0 = G.snap0;
+    const int64_t idx = t - G.fill0;
     if (idx >= static_cast<int64_t>(n_frames) * kPktsPerFrame) return;
     const int64_t frame = idx / kPktsPerFrame;
     const uint32_t cf = static_cast<uint32_t>(idx % kPktsPerFrame);
@@ -261,24 +282,44 @@ __global__ void k_beng_to_complex(const int8_t *__restrict__ beng, int64_t n_spe
 }
 
 // ---- launchers ---------------------------------------------------------------
+void unpack_segs_add(UnpackSegs &S, const UnpackSeg &g) {
+    UnpackSeg &d = S.s[S.n++];
+    d = g;
+    d.blk0 = S.blocks;
+    d.fill0 = S.fill_threads;
+    S.blocks += (g.n_pkts + kTilePkts - 1) / kTilePkts;
+    S.fill_threads += static_cast<int64_t>(g.n_frames) * kPktsPerFrame;
+}
+
+cudaError_t launch_unpack_segs(const UnpackSegs &S, cudaStream_t st) {
+    if (S.blocks <= 0) return cudaSuccess;
+    k_unpack_packed<<<static_cast<unsigned>(S.blocks), 256, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_missing_segs(const UnpackSegs &S, cudaStream_t st) {
+    if (S.fill_threads <= 0) return cudaSuccess;
+    k_fill_missing<<<static_cast<unsigned>((S.fill_threads + 255) / 256), 256, 0, st>>>(S);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_unpack(const void *pkts, int64_t n_pkts, uint64_t b_zero, int n_frames, int map,
                           uint32_t *spec, int64_t pol_stride, int64_t snap0, uint32_t *bitmap,
                           int32_t *counts, int32_t *rejected, cudaStream_t st, const uint8_t *accept) {
     if (n_pkts <= 0) return cudaSuccess;
-    const int64_t blocks = (n_pkts + kTilePkts - 1) / kTilePkts;
-    k_unpack_packed<<<static_cast<unsigned>(blocks), 256, 0, st>>>(
-        static_cast<const uint8_t *>(pkts), n_pkts, b_zero, n_frames, map, spec, pol_stride, snap0, bitmap,
-        counts, rejected, accept);
-    return cudaGetLastError();
+    UnpackSegs S{};
+    unpack_segs_add(S, UnpackSeg{static_cast<const uint8_t *>(pkts), n_pkts, b_zero, n_frames, map, spec, pol_stride,
+                                 snap0, bitmap, counts, rejected, accept, 0, 0});
+    return launch_unpack_segs(S, st);
 }
 
 cudaError_t launch_fill_missing(const uint32_t *bitmap, int n_frames, int map, uint32_t *spec,
                                 int64_t pol_stride, int64_t snap0, cudaStream_t st) {
-    const int64_t n = static_cast<int64_t>(n_frames) * kPktsPerFrame;
-    if (n <= 0) return cudaSuccess;
-    k_fill_missing<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(bitmap, n_frames, map, spec,
-                                                                           pol_stride, snap0);
-    return cudaGetLastError();
+    if (n_frames <= 0) return cudaSuccess;
+    UnpackSegs S{};
+    unpack_segs_add(S, UnpackSeg{nullptr, 0, 0, n_frames, map, spec, pol_stride, snap0,
+                                 const_cast<uint32_t *>(bitmap), nullptr, nullptr, nullptr, 0, 0});
+    return launch_fill_missing_segs(S, st);
 }
 
 cudaError_t launch_vdif_to_beng_ref(const void *pkts, int64_t n_pkts, uint64_t b_zero, int n_frames, int map,

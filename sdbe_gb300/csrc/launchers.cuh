@@ -43,6 +43,28 @@ cudaError_t launch_swarm_c2r_segs(const SegsA &, const Twiddles &, cudaStream_t)
 cudaError_t launch_resample_segs(int mode, const SegsB &, const Twiddles &, cudaStream_t);
 cudaError_t launch_unpack(const void *, int64_t, uint64_t, int, int, uint32_t *, int64_t, int64_t, uint32_t *,
                           int32_t *, int32_t *, cudaStream_t, const uint8_t *accept = nullptr);
+// The packet unpack and zero fill of several calls (one segment each) in one
+// launch each: per segment the arguments of launch_unpack / launch_fill_missing.
+struct UnpackSeg {
+    const uint8_t *pkts;
+    int64_t n_pkts;
+    uint64_t b_zero;
+    int n_frames, map;
+    uint32_t *spec;
+    int64_t pol_stride, snap0;
+    uint32_t *bitmap;
+    int32_t *counts, *rejected;
+    const uint8_t *accept;
+    int64_t blk0, fill0;  // first block of the unpack grid, first thread of the fill grid (set by unpack_segs_add)
+};
+struct UnpackSegs {
+    int n;
+    int64_t blocks, fill_threads;
+    UnpackSeg s[kMaxSegs];
+};
+void unpack_segs_add(UnpackSegs &S, const UnpackSeg &g);
+cudaError_t launch_unpack_segs(const UnpackSegs &S, cudaStream_t st);
+cudaError_t launch_fill_missing_segs(const UnpackSegs &S, cudaStream_t st);
 cudaError_t launch_fill_missing(const uint32_t *, int, int, uint32_t *, int64_t, int64_t, cudaStream_t);
 cudaError_t launch_vdif_to_beng_ref(const void *, int64_t, uint64_t, int, int, int8_t *, int8_t *, cudaStream_t);
 cudaError_t launch_reorder_mar2015(const uint32_t *, int, uint32_t *, cudaStream_t);
