@@ -395,12 +395,11 @@ int sdbe_summary_stats(const float *in, int64_t n, double *out_host, void *strea
  * 131,088-byte device array (8192 FP64 partial pairs + the result) that every
  * device loading the library holds until exit; n may be at most
  * SDBE_NOALLOC_MAX_SAMPLES (8192 partials x 16384 samples), larger n returns
- * SDBE_ERR_CAPACITY.  The first call on a device looks up the array's device
- * address with that device current; make that first call before any stream
- * capture.  The address stays valid for the life of the device's context (a
- * cudaDeviceReset ends it: make no call on that device after a reset).  Each
- * call waits for its stream before returning, since the result goes to host
- * memory.  All calls share the array: calls that overlap on the GPU (other
+ * SDBE_ERR_CAPACITY.  Each call looks up the array's address in the current
+ * device's context, so calls after a cudaDeviceReset use the reloaded array.
+ * Each call synchronizes its stream before returning (the result goes to host
+ * memory), so no call can be made on a stream that is being captured into a
+ * CUDA graph.  All calls share the array: calls that overlap on the GPU (other
  * streams, other host threads) race, so callers serialize them.  Nothing
  * accumulates in it across calls, so it needs no clearing.  Allocates
  * nothing, device or host. */

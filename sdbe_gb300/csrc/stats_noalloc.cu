@@ -13,7 +13,6 @@
 // caller's host memory.  The call waits for its stream before it returns.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "launchers.cuh"
@@ -23,7 +22,6 @@ namespace sdbe {
 
 constexpr int kNoallocBlocks = 8192;          // partial pairs the array holds
 constexpr int64_t kNoallocSamplesPerBlock = 256 * 64;
-constexpr int kNoallocMaxDevices = 64;
 
 // 8192 partial pairs + (mean, std): 131,088 bytes on every device that loads
 // the library, held until the process exits.
@@ -45,21 +43,15 @@ __global__ void k_noalloc_finalize(const float *in, int blocks, int64_t n) {
 }
 
 namespace {
-std::mutex g_noalloc_mutex;
-double *g_noalloc_addr[kNoallocMaxDevices] = {};
-
-// Device address of the array on the current device, looked up once per
-// device (host code only sees a host-side stand-in under the array's name).
-cudaError_t noalloc_scratch(int device, double **out) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_addr[device] = static_cast<double *>(p);
-    }
-    *out = g_noalloc_addr[device];
-    return cudaSuccess;
+// Device address of the array in the current device's context.  Looked up on
+// every call (a host-side query that allocates nothing): an address kept from
+// an earlier call would dangle once that context is torn down
+// (cudaDeviceReset) and the module is loaded again.
+cudaError_t noalloc_scratch(double **out) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    *out = static_cast<double *>(p);
+    return e;
 }
 }  // namespace
 
@@ -78,11 +70,8 @@ extern "C" int sdbe_summary_stats_noalloc(const float *in, int64_t n, double *ou
                          " samples (its fixed device array holds 8192 partial sums)");
         return SDBE_ERR_CAPACITY;
     }
-    int device = 0;
-    cudaError_t e = cudaGetDevice(&device);
-    if (e == cudaSuccess && (device < 0 || device >= kNoallocMaxDevices)) e = cudaErrorInvalidDevice;
     double *scratch = nullptr;
-    if (e == cudaSuccess) e = noalloc_scratch(device, &scratch);
+    cudaError_t e = noalloc_scratch(&scratch);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int blocks = static_cast<int>((n + kNoallocSamplesPerBlock - 1) / kNoallocSamplesPerBlock);
     if (e == cudaSuccess) e = launch_stats_partial(in, n, scratch, blocks, st);
