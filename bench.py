@@ -387,6 +387,21 @@ def fp32_fma_peak(device):
     return tf.value, ms.value
 
 
+def _fp32_bc_roofline(prof, device, kernel):
+    """FP32-issue roofline of the FP32 path's stage-BC launches: nominal FFT
+    flops per chunk x chunks per launch / CUDA-event time per launch, against
+    the measured FP32 FMA rate."""
+    fma_tf, fma_ms = fp32_fma_peak(device)
+    bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
+    bc_units = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1)
+    ach = FLOP_BC * bc_units / (bc_ms * 1e-3) / 1e12 if bc_ms else None
+    return {"bound": "fp32_issue", "kernel": kernel, "achieved": ach, "peak": fma_tf,
+            "unit": "TFLOP/s", "frac": ach / fma_tf if ach else None, "traffic": None,
+            "peak_kind": f"measured FP32 FMA rate (sdbe_fp32_fma_rate, {fma_ms:.1f} ms launch)",
+            "ms_per_launch": bc_ms, "flop_per_launch": FLOP_BC * bc_units, "flop_per_unit": FLOP_BC,
+            "units_per_launch": bc_units}
+
+
 # Nominal FFT work per unit (2.5 N log2 N per real transform): stage A one
 # C2R 32768 per snapshot; stage BC one R2C 36608 + one C2R 32768 per chunk.
 FLOP_A = 2.5 * 32768 * 15
@@ -807,14 +822,7 @@ def run_streams(args):
                           args.wave)
     prof = r["prof"]
     if args.precision == "fp32":
-        fma_tf, fma_ms = fp32_fma_peak(local_rank)
-        bc_ms = prof.stage_bc_ms / max(prof.stage_bc_launches, 1)
-        bc_units = prof.stage_bc_chunks / max(prof.stage_bc_launches, 1)
-        ach = FLOP_BC * bc_units / (bc_ms * 1e-3) / 1e12 if bc_ms else None
-        roofline = {"bound": "fp32_issue", "kernel": "k_resample<0> (stage BC)", "achieved": ach, "peak": fma_tf,
-                    "unit": "TFLOP/s", "frac": ach / fma_tf if ach else None, "traffic": None,
-                    "peak_kind": f"measured FP32 FMA rate (sdbe_fp32_fma_rate, {fma_ms:.1f} ms launch)",
-                    "ms_per_launch": bc_ms, "flop_per_launch": FLOP_BC * bc_units}
+        roofline = _fp32_bc_roofline(prof, local_rank, "k_resample<0> (stage BC)")
     else:
         roofline = _tc_roofline(prof, 1, 3 if args.precision == "tc16" else 2)
     frames = s8["frames"]
@@ -952,9 +960,10 @@ def run_stress(args):
         "whole_pipeline_hbm": {"algorithmic_gbs": whole_bytes / (ms_total * 1e-3) / 1e9, "peak": peak,
                                "frac": whole_bytes / (ms_total * 1e-3) / 1e9 / peak},
         "roofline": (_tc_roofline(prof, n_passes, 3 if args.precision == "tc16" else 2) if tc else
-                     {"bound": "hbm", "kernel": "stage_bc", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                      "frac": achieved / peak if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                      "ms_per_launch": bc_ms, "algorithmic_bytes_per_launch": bc_bytes}),
+                     _fp32_bc_roofline(prof, local_rank, "k_resample<3> (stage BC + chunk statistics)")),
+        "stage_bc_hbm": (None if tc else
+                         {"achieved_gbs": achieved, "peak": peak, "frac": achieved / peak if achieved else None,
+                          "peak_kind": peak_kind, "ms_per_launch": bc_ms, "io_bytes_per_launch": bc_bytes}),
         "thresholds_after_run": {"pol0": float(st.threshold[0]), "pol1": float(st.threshold[1])},
         "stage_ms_per_step": _stage_ms(prof, n_passes),
         "e2e": {"value": n_passes * samples / e2e_s / 1e9, "unit": "GS/s", "ms_per_step": e2e_s / n_passes * 1e3,
