@@ -91,6 +91,31 @@ def test_error_paths_without_gpu(built):
     assert lib.sdbe_beng_reform(C.byref(st), None, 0, None) == built.OK   # nothing to do
 
 
+@pytest.mark.parametrize("field,value,word", [
+    ("threshold_mode", 7, "threshold_mode"),
+    ("threshold_window", -1, "threshold_window"),
+    ("channel_map", 5, "channel_map"),
+    ("wave_batches", 65, "wave_batches"),
+    ("precision", 9, "precision"),
+    ("stage_launches", 2, "stage_launches"),
+    ("device", -1, "device"),
+])
+def test_create_rejects_each_bad_config_field(built, field, value, word):
+    """sdbe_create checks every field of the configuration before it touches
+    a device: one bad field gives SDBE_ERR_ARG, no handle, and a message that
+    names it."""
+    lib = built.lib()
+    cfg = built.Config()
+    cfg.max_frames = 143
+    cfg.trim_mhz = 150
+    setattr(cfg, field, value)
+    h = C.c_void_p(12345)
+    assert lib.sdbe_create(C.byref(cfg), C.byref(h)) == built.ERR_ARG
+    assert h.value is None
+    assert word in built.last_error() or (field == "device" and "CUDA device" in built.last_error())
+    assert lib.sdbe_test_ingest_accept(None, None, 0) == built.ERR_ARG
+
+
 def test_header_template_matches_oracle(built):
     """sdbe_header_template (host-only) == fill_vdif_header_template restated."""
     from oracle import sdbe_oracle as O
