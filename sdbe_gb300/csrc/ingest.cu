@@ -17,7 +17,6 @@ namespace sdbe {
 namespace {
 
 constexpr int kRing = 4;                                  // BENG_GROUPS_IN_BUFFER
-constexpr int kLookAhead = 2;                             // MAX_INDEX_LOOK_AHEAD
 constexpr int kGroupFrames = 143;                         // BENG_FRAMES_PER_GROUP
 constexpr int64_t kGroupPackets = int64_t(kGroupFrames) * kPktsPerFrame;  // 292864
 constexpr int64_t kGroupSnaps = int64_t(kGroupFrames) * kSnapsPerFrame;   // 18304 = 128 batches

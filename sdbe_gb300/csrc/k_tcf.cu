@@ -161,8 +161,6 @@ __device__ __forceinline__ void l2_prefetch_piece(const void *src, uint32_t byte
 }
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-// Every bulk group of this thread but the newest complete.
-__device__ __forceinline__ void bulk_wait_all_but_newest() { asm volatile("cp.async.bulk.wait_group 1;" ::: "memory"); }
 
 // Common kernel state: barriers, tensor memory, error flag.
 constexpr int kFull = 18;           // completion barriers, one per tile of a whole stage
