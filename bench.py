@@ -729,13 +729,11 @@ def _streams8_measure(prec, s8, steps, warmup, local_rank, clocks, wave_arg=0):
     profs = [h.read_profile() for h in hs]
     for h in hs[::per_launch]:
         h.profile(False)
-    prof = profs[0]  # a fused launch's FFT stages are timed on its first handle
-    for q in profs[per_launch::per_launch]:
-        prof.stage_a_ms += q.stage_a_ms
-        prof.stage_bc_ms += q.stage_bc_ms
-        prof.fused_ms += q.fused_ms
-        prof.fused_launches += q.fused_launches
-        prof.fused_chunks += q.fused_chunks
+    prof = profs[0]  # a shared launch's FFT stages are timed on its first handle
+    for q in profs[per_launch::per_launch]:  # the other launch groups: launches, units and times alike
+        for f in ("stage_a_launches", "stage_a_snapshots", "stage_a_ms", "stage_bc_launches", "stage_bc_chunks",
+                  "stage_bc_ms", "fused_launches", "fused_chunks", "fused_ms"):
+            setattr(prof, f, getattr(prof, f) + getattr(q, f))
     n_launches = sum(int(q.launches) for q in profs)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
